@@ -1,0 +1,144 @@
+// TEST INFRASTRUCTURE ONLY: a small C ABI over the UNMODIFIED reference
+// library, compiled from the reference sources by oracle/build_ref.sh into
+// oracle/_ref/libwndref.so.  It is how the tests and the fixture generator
+// (tests/golden/make_golden.py) obtain the reference's own answers.
+//
+// Pixels are handed over the way ImageMatrix::LoadTIFF stores them
+// (src/cmatrix.cpp:134-163): row-major doubles, stats accumulated in raster
+// order, then finish().
+#include <cstring>
+#include <string>
+#include <vector>
+#include <cfloat>
+#include "cmatrix.h"
+#include "Tasks.h"
+#include "FeatureNames.h"
+#include "ImageTransforms.h"
+#include "FeatureAlgorithms.h"
+#include "wndchrm_src/TrainingSet.h"
+#include "wndchrm_src/signatures.h"
+
+// the "verbosity" global comes from src/wndchrm_error.cpp
+
+static void load_pixels(ImageMatrix &im, const double *pix, int w, int h, int bits) {
+    im.bits = (unsigned short)bits;
+    im.allocate(w, h);
+    writeablePixels pp = im.WriteablePixels();
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) pp(y, x) = im.stats.add(pix[(size_t)y * w + x]);
+    im.finish();
+}
+
+static const FeatureComputationPlan *std_plan(int kind) {
+    if (kind == 1) return StdFeatureComputationPlans::getFeatureSetLong();
+    return StdFeatureComputationPlans::getFeatureSet();
+}
+
+extern "C" {
+
+int wcref_plan_n_features(int kind) { return (int)std_plan(kind)->n_features; }
+
+// Copies the i-th feature name of a standard plan into buf.
+int wcref_plan_feature_name(int kind, int i, char *buf, int buflen) {
+    const std::string &s = std_plan(kind)->getFeatureNameByIndex((size_t)i);
+    std::strncpy(buf, s.c_str(), (size_t)buflen - 1);
+    buf[buflen - 1] = 0;
+    return (int)s.size();
+}
+
+// Runs a whole standard plan (kind 0 = short 1059, 1 = long 2919) through
+// FeatureComputationPlanExecutor::run (src/Tasks.cpp:275-295).
+int wcref_extract_std(int kind, const double *pix, int w, int h, int bits, double *out) {
+    ImageMatrix im;
+    load_pixels(im, pix, w, h, bits);
+    const FeatureComputationPlan *plan = std_plan(kind);
+    std::vector<double> row(plan->n_features, 0.0);
+    FeatureComputationPlanExecutor ex(plan);
+    ex.run(&im, row, 0);
+    std::memcpy(out, row.data(), row.size() * sizeof(double));
+    return (int)row.size();
+}
+
+// Runs one feature group given by its reference name, e.g.
+// "Haralick Textures (Wavelet (Edge ()))".  Returns the feature count.
+int wcref_extract_group(const char *group, const double *pix, int w, int h, int bits, double *out) {
+    ImageMatrix im;
+    load_pixels(im, pix, w, h, bits);
+    FeatureComputationPlan plan("one group");
+    plan.add(std::string(group));
+    plan.finalize();
+    std::vector<double> row(plan.n_features, 0.0);
+    FeatureComputationPlanExecutor ex(&plan);
+    ex.run(&im, row, 0);
+    std::memcpy(out, row.data(), row.size() * sizeof(double));
+    return (int)row.size();
+}
+
+// Applies one registered ImageTransform ("Fourier", "Chebyshev", "Wavelet",
+// "Edge"); out must hold 4*w*h doubles.  Writes the output size.
+int wcref_transform(const char *name, const double *pix, int w, int h, int bits,
+                    double *out, int *ow, int *oh) {
+    ImageMatrix im, res;
+    load_pixels(im, pix, w, h, bits);
+    const ImageTransform *t = FeatureNames::getTransformByName(std::string(name));
+    if (!t) return -1;
+    t->execute(im, res);
+    *ow = (int)res.width;
+    *oh = (int)res.height;
+    readOnlyPixels rp = res.ReadablePixels();
+    for (int y = 0; y < *oh; y++)
+        for (int x = 0; x < *ow; x++) out[(size_t)y * (*ow) + x] = rp(y, x);
+    return 0;
+}
+
+// WND-5 as the CLI runs it: TrainingSet::normalize (TrainingSet.cpp:2090),
+// SetFisherScores(frac) (:2183), then classify2 (:2429) for every test row.
+// train: N x F row-major; labels 1..C.  Feature names are the long plan's when
+// F == 2919, else "Pixel Intensity Statistics () [i]".
+// probs: T x C.  pred: T (1-based).  weights/mins/maxs: F.
+int wcref_wnd(const double *train, int N, int F, const int *labels, int C, double frac,
+              const double *test, int T, double *weights, double *mins, double *maxs,
+              double *probs, int *pred) {
+    TrainingSet *ts = new TrainingSet(N, C);
+    char lab[32];
+    for (int c = 1; c <= C; c++) {
+        snprintf(lab, sizeof lab, "c%04d", c);
+        ts->AddClass(lab);
+    }
+    const FeatureComputationPlan *plan = (F == 2919) ? std_plan(1) : nullptr;
+    char nm[256];
+    for (int s = 0; s < N; s++) {
+        signatures *sg = new signatures();
+        sg->NamesTrainingSet = ts;
+        sg->sample_class = (unsigned short)labels[s];
+        for (int f = 0; f < F; f++) {
+            if (plan) std::strncpy(nm, plan->getFeatureNameByIndex(f).c_str(), sizeof nm - 1), nm[sizeof nm - 1] = 0;
+            else snprintf(nm, sizeof nm, "Pixel Intensity Statistics () [%d]", f);
+            sg->Add(nm, train[(size_t)s * F + f]);
+        }
+        ts->AddSample(sg);
+    }
+    ts->normalize();
+    data_split split;
+    ts->SetFisherScores(frac, 0, &split);
+    for (int f = 0; f < F; f++) {
+        weights[f] = ts->SignatureWeights[f];
+        mins[f] = ts->SignatureMins[f];
+        maxs[f] = ts->SignatureMaxes[f];
+    }
+    std::vector<double> p(C + 1);
+    for (int t = 0; t < T; t++) {
+        signatures *sg = new signatures();
+        for (int f = 0; f < F; f++) sg->Add(nullptr, test[(size_t)t * F + f]);
+        double nf = 0;
+        char nmx[8] = "t";
+        long c = ts->classify2(nmx, t, sg, p.data(), &nf);
+        pred[t] = (int)c;
+        for (int k = 1; k <= C; k++) probs[(size_t)t * C + k - 1] = p[k];
+        delete sg;
+    }
+    delete ts;
+    return 0;
+}
+
+}  // extern "C"

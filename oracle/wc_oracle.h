@@ -1,0 +1,45 @@
+// TEST INFRASTRUCTURE ONLY: the CPU oracle for the WND-CHARM hot path.
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+// load it, and only as a checker / baseline.  The shipped GPU library never
+// links or calls it.
+//
+// It restates, in plain C++ written for this project, the reference
+// algorithms of the feature-extraction DAG and of WND-5; every function in
+// wc_oracle.cpp cites the reference file:line it follows.  It is pinned
+// against the reference's golden fixtures and against the unmodified
+// reference library built by oracle/build_ref.sh (tests/test_oracle_*.py).
+#pragma once
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Standard plans: 0 = short (1059 features), 1 = long (2919 features).
+int wco_plan_n_features(int kind);
+int wco_plan_feature_name(int kind, int i, char *buf, int buflen);
+
+// Whole plan on one grayscale image (row-major doubles, width w, height h).
+int wco_extract_std(int kind, const double *pix, int w, int h, int bits, double *out);
+
+// Whole plan, many images, run on nthreads host threads (one image each).
+// pix_offsets[i] indexes pix; out is n x n_features.
+int wco_extract_std_batch(int kind, const double *pix, const long *pix_offsets,
+                          const int *ws, const int *hs, int n, int bits,
+                          double *out, int nthreads);
+
+// One group by reference name, e.g. "Zernike Coefficients (Fourier ())".
+int wco_extract_group(const char *group, const double *pix, int w, int h, int bits, double *out);
+
+// One transform ("Fourier", "Chebyshev", "Wavelet", "Edge"); out holds >= 4*w*h.
+int wco_transform(const char *name, const double *pix, int w, int h, double *out, int *ow, int *oh);
+
+// Haralick per-angle tone count Ng of an image (diagnostic for cost models).
+int wco_haralick_tones(const double *pix, int w, int h);
+
+// WND-5, CLI semantics (TrainingSet::normalize, SetFisherScores, classify2).
+int wco_wnd(const double *train, int N, int F, const int *labels, int C, double frac,
+            const double *test, int T, double *weights, double *mins, double *maxs,
+            double *probs, int *pred);
+
+#ifdef __cplusplus
+}
+#endif

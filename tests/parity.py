@@ -1,0 +1,65 @@
+"""Per-family parity rules shared by the oracle tests and the GPU tests.
+
+Feature families are identified by the group name of each feature.  Three
+kinds of comparison:
+  * "float": |a-b| <= rtol*|b| + atol;
+  * "counts": histogram-like groups whose values come from binning a
+    floating-point quantity: they may differ by a few single-count moves
+    between neighbouring bins (each move changes two entries by 1); the
+    number of such moves per group is budgeted;
+  * "f14": Haralick maximal-correlation-coefficient entries (in-group
+    indices 16, 17): sqrt of eigenvalue #2 in Schur order, which depends on
+    the eigen-solver's rounding (two builds of the reference itself differ);
+    reported, never gated beyond "finite and in [0, 1.5]".
+"""
+import numpy as np
+
+F14 = (16, 17)
+COUNT_GROUPS = ("Chebyshev-Fourier Coefficients", "Chebyshev Coefficients", "Comb Moments",
+                "Radon Coefficients", "Multiscale Histograms")
+
+
+def group_of(name):
+    return name.rsplit(" [", 1)[0]
+
+
+def index_of(name):
+    return int(name.rsplit("[", 1)[1].rstrip("]"))
+
+
+def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=2, skip=()):
+    """Compare feature rows a (candidate) and b (expected).  Returns a dict of
+    failures keyed by group name; empty when everything is within rules."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    groups = {}
+    for i, n in enumerate(names):
+        groups.setdefault(group_of(n), []).append(i)
+    fails = {}
+    for g, idx in groups.items():
+        if any(g.startswith(s) for s in skip):
+            continue
+        idx = np.array(idx)
+        alg = g.split(" (")[0]
+        va, vb = a[idx], b[idx]
+        if alg == "Haralick Textures":
+            f14 = np.array([index_of(names[i]) in F14 for i in idx])
+            bad14 = ~np.isfinite(va[f14]) | (va[f14] < 0) | (va[f14] > 1.5)
+            if bad14.any():
+                fails[g] = ("f14 out of range", va[f14])
+            va, vb = va[~f14], vb[~f14]
+        if alg in COUNT_GROUPS:
+            d = np.abs(va - vb)
+            if alg == "Multiscale Histograms":
+                ok = np.allclose(va, vb, rtol=rtol, atol=0.02)
+            else:
+                ok = (np.abs(np.round(d) - d) < 1e-9).all() and d.sum() <= 2 * count_moves
+            if not ok:
+                fails[g] = ("counts", d.sum(), np.nonzero(d)[0][:8])
+            continue
+        tol = rtol * np.abs(vb) + atol
+        bad = np.abs(va - vb) > tol
+        if bad.any():
+            j = np.nonzero(bad)[0]
+            fails[g] = ("float", j[:8].tolist(), va[j[:4]].tolist(), vb[j[:4]].tolist())
+    return fails

@@ -1,0 +1,125 @@
+/* wndcharm_gb300.h: C ABI of the GB300 (sm_103a) WND-CHARM hot path.
+ *
+ * The drop-in boundary for the reference's feature-plan API and its WND-5
+ * classifier.  Plain pointers and sizes only; every call returns an int status
+ * (WC_OK or a negative WC_ERR_*) and never aborts.  wc_last_error() gives the
+ * message of the last failure on the calling thread.
+ *
+ * Reference interfaces replaced (paths inside the wnd-charm source tree):
+ *   StdFeatureComputationPlans::getFeatureSet / getFeatureSetLong   src/Tasks.h:355-377, src/Tasks.cpp:313-352
+ *   FeatureComputationPlan::add(name), n_features, getFeatureNameByIndex
+ *                                                                    src/Tasks.h:272-316, src/Tasks.cpp:118-173
+ *   FeatureComputationPlanExecutor::run(const ImageMatrix*, std::vector<double>&, size_t)
+ *                                                                    src/Tasks.h:318-348, src/Tasks.cpp:275-295
+ *   ImageTransform::execute (Fourier, Chebyshev, Wavelet, Edge)      src/ImageTransforms.h:45-51, src/ImageTransforms.cpp:59-112
+ *   TrainingSet::normalize, SetFisherScores, classify2               src/wndchrm_src/TrainingSet.h:205-243,
+ *                                                                    src/wndchrm_src/TrainingSet.cpp:2090-2123, 2183-2324, 2429-2586
+ *   signatures::normalize                                            src/wndchrm_src/signatures.cpp:196-215
+ */
+#ifndef WNDCHARM_GB300_H
+#define WNDCHARM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define WC_OK 0
+#define WC_ERR_ARG (-1)         /* bad argument (null pointer, size, unknown name) */
+#define WC_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define WC_ERR_NOMEM (-3)       /* device allocation failed */
+#define WC_ERR_UNSUPPORTED (-4) /* request outside what this build supports */
+#define WC_ERR_DEVICE (-5)      /* a kernel reported a bounded-wait timeout or an internal check */
+
+/* plan kinds: the reference's standard feature sets */
+#define WC_PLAN_SHORT 0 /* 1059 features, StdFeatureComputationPlans::getFeatureSet */
+#define WC_PLAN_LONG 1  /* 2919 features, StdFeatureComputationPlans::getFeatureSetLong */
+
+/* pixel types accepted for input images */
+#define WC_U8 0
+#define WC_U16 1
+#define WC_F32 2
+#define WC_F64 3
+
+/* arithmetic form of an engine */
+#define WC_PREC_FP64 0  /* plain FP64 form: every family in double precision */
+#define WC_PREC_MIXED 1 /* batched mixed-precision form (FP32 + tensor cores, FP64 where required) */
+
+typedef struct wc_plan wc_plan;     /* a feature computation plan (groups, offsets, names) */
+typedef struct wc_engine wc_engine; /* one GPU: device, stream, device memory pools */
+
+/* One input image.  `pixels` is a host pointer unless `on_device` is set, in
+ * which case it is a device pointer on the engine's GPU.  Row-major, width
+ * `width`, height `height`, elements of type `dtype`; `bits` is the image's
+ * intensity depth (8 or 16), kept for the ImageMatrix::bits field. */
+typedef struct {
+    const void *pixels;
+    int dtype;
+    int width;
+    int height;
+    int bits;
+    int on_device;
+} wc_image_desc;
+
+const char *wc_last_error(void);
+const char *wc_version(void);
+
+/* ---- plans (host only, no GPU needed) ---- */
+/* Standard plan, shared and immutable; do not free.  Replaces
+ * StdFeatureComputationPlans::getFeatureSet{,Long} (src/Tasks.cpp:313-352). */
+int wc_plan_get(int kind, const wc_plan **out);
+/* Plan from feature-group names such as "Zernike Coefficients (Fourier (Edge ()))",
+ * in the given order; replaces FeatureComputationPlan::add(name) (src/Tasks.cpp:156-158). */
+int wc_plan_from_names(const char *const *groups, int n, wc_plan **out);
+void wc_plan_free(wc_plan *plan);
+/* FeatureComputationPlan::n_features (src/Tasks.h:280). */
+int wc_plan_n_features(const wc_plan *plan);
+/* FeatureComputationPlan::getFeatureNameByIndex (src/Tasks.cpp:160-169): copies the
+ * name, e.g. "Haralick Textures (Wavelet (Edge ())) [17]"; returns its length. */
+int wc_plan_feature_name(const wc_plan *plan, int index, char *buf, int buflen);
+int wc_plan_n_groups(const wc_plan *plan);
+/* group name and its column offset in a feature row (FeatureComputationPlan::getFGoffset) */
+int wc_plan_group(const wc_plan *plan, int g, char *buf, int buflen, int *offset, int *n_features);
+
+/* ---- engines ---- */
+int wc_engine_create(int device, int precision, wc_engine **out);
+void wc_engine_destroy(wc_engine *engine);
+/* CUDA stream the engine launches on (as a cudaStream_t cast to void*); 0 = legacy default */
+int wc_engine_set_stream(wc_engine *engine, void *stream);
+/* kernels launched by this engine since creation (counts every launch) */
+long long wc_engine_launch_count(const wc_engine *engine);
+
+/* ---- feature extraction ----
+ * FeatureComputationPlanExecutor::run for one image: writes plan->n_features
+ * doubles to out_row (host memory).  Synchronous. */
+int wc_extract(wc_engine *engine, const wc_plan *plan, const void *pixels, int dtype, int width, int height,
+               int bits, double *out_row);
+/* Batched form: n images of any sizes, out is n x n_features row-major.  If
+ * out_on_device is set, `out` is a device pointer and the call returns once the
+ * work is queued on the engine's stream; otherwise it is host memory and the
+ * call returns when the rows are written. */
+int wc_extract_batch(wc_engine *engine, const wc_plan *plan, const wc_image_desc *images, int n, double *out,
+                     int out_on_device);
+/* One transform ("Fourier", "Chebyshev", "Wavelet", "Edge"), host buffers; out
+ * must hold out_capacity doubles; writes the output size.  ImageTransform::execute
+ * (src/ImageTransforms.cpp:59-112). */
+int wc_transform(wc_engine *engine, const char *name, const double *pixels, int width, int height, double *out,
+                 long long out_capacity, int *out_width, int *out_height);
+
+/* ---- WND-5 (CLI semantics), host buffers ----
+ * wc_wnd_fit: TrainingSet::normalize + SetFisherScores(frac): per-feature min/max of the
+ * training rows, Fisher scores, all weights below the score at sorted rank
+ * floor(frac*F+0.5) set to 0.  train: N x F, labels in 1..C. */
+int wc_wnd_fit(wc_engine *engine, const double *train, int N, int F, const int *labels, int C, double frac,
+               double *weights, double *mins, double *maxs);
+/* wc_wnd_classify: signatures::normalize of each test row against (mins, maxs),
+ * then TrainingSet::classify2 against the training rows normalised the same way:
+ * probs T x C marginal probabilities, pred T predicted classes (1-based, -1 if none). */
+int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const int *labels, int C,
+                    const double *weights, const double *mins, const double *maxs, const double *test, int T,
+                    double *probs, int *pred);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WNDCHARM_GB300_H */

@@ -97,15 +97,23 @@ static Moments2 stats_of(const Img &im) {
     return s;
 }
 
+// bin = (unsigned long)((v - lo) * scale), clamped to nbins - 1
+// (src/cmatrix.cpp:1097-1099).  A NaN goes to the last bin, as the x86-64
+// build of the reference converts it (so the oracle gives the same answer on
+// aarch64 hosts, where the raw conversion would give 0).
+static inline unsigned long bin_of(double v, double lo, double scale, unsigned long nbins) {
+    double t = (v - lo) * scale;
+    if (!(t < (double)nbins)) return nbins - 1;
+    if (t < 0) return 0;
+    unsigned long b = (unsigned long)t;
+    return b >= nbins ? nbins - 1 : b;
+}
+
 // ImageMatrix::histogram, src/cmatrix.cpp:1069-1103 (bins over [lo, hi]).
 static void histogram(const double *v, size_t n, int nbins, double lo, double hi, double *bins) {
     double scale = (hi - lo > 0) ? (double)nbins / double(hi - lo) : 0;
     for (int b = 0; b < nbins; b++) bins[b] = 0;
-    for (size_t a = 0; a < n; a++) {
-        unsigned long bin = (unsigned long)(((v[a] - lo) * scale));
-        if (bin >= (unsigned long)nbins) bin = nbins - 1;
-        bins[bin] += 1.0;
-    }
+    for (size_t a = 0; a < n; a++) bins[bin_of(v[a], lo, scale, nbins)] += 1.0;
 }
 
 // ImageMatrix::get_median, src/cmatrix.cpp:780-800.
@@ -403,11 +411,7 @@ static void f_cheb_fourier(const Img &src, double *out) {
     for (int a = 0; a < 32; a++) out[a] = 0;
     if (mx - mn > 0) {
         double sc = 32.0 / double(mx - mn);
-        for (size_t a = 0; a < NN * NN; a++) {
-            unsigned long bin = (unsigned long)(((c[a] - mn) * sc));
-            if (bin >= 32) bin = 31;
-            out[bin] += 1;
-        }
+        for (size_t a = 0; a < NN * NN; a++) out[bin_of(c[a], mn, sc, 32)] += 1;
     }
 }
 
@@ -1270,9 +1274,7 @@ static void f_objects(const Img &im, double *out) {
         if (amax - amin > 0)
             for (unsigned long o = 0; o < count; o++) {
                 ss += std::pow(area[o] - amean, 2);
-                unsigned long b = (unsigned long)(((double)area[o] - amin) * sc);
-                if (b >= 10) b = 9;
-                ahist[b] += 1;
+                ahist[bin_of((double)area[o], (double)amin, sc, 10)] += 1;
             }
         avar = (count > 1) ? ss / (count - 1) : ss;
         std::sort(dist.begin(), dist.end());
@@ -1283,9 +1285,7 @@ static void f_objects(const Img &im, double *out) {
         double sd = 0;
         for (unsigned long o = 0; o < count; o++) {
             sd += std::pow(dist[o] - dmean, 2);
-            unsigned long b = (unsigned long)((dist[o] - dmin) * dsc);
-            if (b >= 10) b = 9;
-            dhist[b] += 1;
+            dhist[bin_of(dist[o], dmin, dsc, 10)] += 1;
         }
         dvar = (count > 1) ? sd / (count - 1) : sd;
     }

@@ -1,0 +1,573 @@
+// The engine: host-side executor of a feature plan over a batch of images on
+// one GPU, and the C ABI (include/wndcharm_gb300.h).
+//
+// Replaces FeatureComputationPlanExecutor::run (src/Tasks.cpp:275-295).  The
+// reference walks the plan's node tree one image at a time and caches each
+// transform result by node key; here every node of every image in the batch
+// is a plane in one HBM arena, each transform runs as one launch over all
+// (source, destination) plane pairs of its depth, and each feature family runs
+// as one launch over all (plane, output column) jobs of the batch.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/wndcharm_gb300.h"
+#include "wc_features.h"
+#include "kernels.h"
+#include "plan.h"
+
+namespace wc {
+
+static thread_local std::string g_err;
+int set_err(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                         \
+    do {                                                                                              \
+        cudaError_t e_ = (x);                                                                         \
+        if (e_ != cudaSuccess) return set_err(WC_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_)); \
+    } while (0)
+
+// grow-only device buffer
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes) {
+        if (bytes <= cap) return WC_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes + bytes / 4 + 4096;
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(WC_ERR_NOMEM, "cudaMalloc of %zu bytes failed", want);
+        }
+        cap = want;
+        return WC_OK;
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+// Host-computed tables kept on the device: Chebyshev bases, FFT twiddles.
+struct Tables {
+    std::vector<double> host;
+    std::map<std::string, long long> idx;
+    DevBuf dev;
+    bool dirty = true;
+    long long add(const std::string &key, const std::vector<double> &v) {
+        auto it = idx.find(key);
+        if (it != idx.end()) return it->second;
+        long long off = (long long)host.size();
+        host.insert(host.end(), v.begin(), v.end());
+        while (host.size() % 32) host.push_back(0.0);
+        idx[key] = off;
+        dirty = true;
+        return off;
+    }
+    int sync(cudaStream_t st) {
+        if (!dirty) return WC_OK;
+        int r = dev.ensure(host.size() * sizeof(double));
+        if (r) return r;
+        CK(cudaMemcpyAsync(dev.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        dirty = false;
+        return WC_OK;
+    }
+    const double *d() const { return (const double *)dev.p; }
+};
+
+// Chebyshev basis of Chebyshev2D for a line of `len` samples and N terms:
+// tab[x*N + j] = T_j(x_x) * (j ? 2 : 1) / len / 2, x_x = 2(x+1)/len - 1,
+// T_j = cos(j * acos(x)) (TNx and getChCoeff1D, src/transforms/chebyshev.cpp:39-102).
+std::vector<double> cheb_table(int len, int N) {
+    std::vector<double> t((size_t)len * N);
+    for (int a = 0; a < len; a++) {
+        double x = 2 * (double)(a + 1) / (double)len - 1;
+        double ac = (std::fabs(x) > 1) ? 0 : std::acos(x);
+        for (int j = 0; j < N; j++) {
+            double T = (j == 0) ? 1.0 : std::cos(ac * j);
+            double tj = (j == 0) ? T / (double)len : T * 2 / (double)len;
+            t[(size_t)a * N + j] = tj / 2;
+        }
+    }
+    return t;
+}
+
+FFTPlan fft_plan(Tables &tabs, int n) {
+    FFTPlan P;
+    memset(&P, 0, sizeof P);
+    P.n = n;
+    int m = n;
+    std::vector<int> r;
+    while (m % 8 == 0) { r.push_back(8); m /= 8; }
+    while (m % 4 == 0) { r.push_back(4); m /= 4; }
+    while (m % 2 == 0) { r.push_back(2); m /= 2; }
+    for (int p = 3; (long)p * p <= m; p += 2)
+        while (m % p == 0) { r.push_back(p); m /= p; }
+    if (m > 1) r.push_back(m);
+    P.nstages = (int)r.size();
+    for (size_t i = 0; i < r.size() && i < 16; i++) P.radix[i] = r[i];
+    std::vector<double> tw(2 * (size_t)n);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int k = 0; k < n; k++) {
+        double a = two_pi * (double)k / (double)n;
+        tw[2 * k] = std::cos(a);
+        tw[2 * k + 1] = -std::sin(a);
+    }
+    P.tw_off = tabs.add("tw" + std::to_string(n), tw);
+    return P;
+}
+
+}  // namespace wc
+
+using namespace wc;
+
+struct wc_engine {
+    int dev = 0;
+    cudaStream_t st = 0;
+    int prec = WC_PREC_FP64;
+    int sms = 1;
+    long long launches = 0;
+    DevBuf arena, feat, ws, meta, stage;
+    Tables tabs;
+    std::vector<char> hmeta;
+    std::mutex mu;
+};
+
+namespace wc {
+
+// Bump allocator over a byte region; `plan` mode only measures.
+struct Bump {
+    size_t used = 0;
+    size_t take(size_t bytes) {
+        size_t off = (used + 255) & ~(size_t)255;
+        used = off + bytes;
+        return off;
+    }
+};
+
+struct Node {
+    int parent, xf, depth;
+    std::vector<int> chain;
+};
+
+static int out_shape(int xf, int w, int h, int &ow, int &oh) {
+    switch (xf) {
+        case X_FOURIER: ow = w; oh = h; return 0;
+        case X_EDGE: ow = w; oh = h; return 0;
+        case X_WAVELET: ow = 2 * ((w + 9) / 2); oh = 2 * ((h + 9) / 2); return 0;
+        case X_CHEBYSHEV: {
+            int N = w < h ? w : h;
+            ow = N;
+            oh = h < N ? h : N;
+            return 0;
+        }
+    }
+    return -1;
+}
+
+// Runs `plan` over `n` images; `dfeat` receives n x n_features on the device.
+int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, double *dfeat,
+              std::vector<Plane> *planes_out = nullptr) {
+    Ctx ctx{E->st, &E->launches, E->prec, E->sms};
+    // ---- nodes: every prefix of every group's transform chain
+    std::vector<Node> nodes(1);
+    nodes[0] = {-1, -1, 0, {}};
+    std::map<std::vector<int>, int> node_of;
+    node_of[{}] = 0;
+    std::vector<int> group_node(plan.groups.size());
+    for (size_t g = 0; g < plan.groups.size(); g++) {
+        std::vector<int> pre;
+        int cur = 0;
+        for (int t : plan.groups[g].chain) {
+            pre.push_back(t);
+            auto it = node_of.find(pre);
+            if (it == node_of.end()) {
+                Node nd{cur, t, (int)pre.size(), pre};
+                nodes.push_back(nd);
+                it = node_of.emplace(pre, (int)nodes.size() - 1).first;
+            }
+            cur = it->second;
+        }
+        group_node[g] = cur;
+    }
+    const int NN = (int)nodes.size();
+    int maxdepth = 0;
+    for (auto &nd : nodes) maxdepth = std::max(maxdepth, nd.depth);
+
+    // ---- planes
+    std::vector<Plane> planes((size_t)n * NN);
+    size_t arena_elems = 0;
+    for (int b = 0; b < n; b++) {
+        if (imgs[b].width < 1 || imgs[b].height < 1 || !imgs[b].pixels)
+            return set_err(WC_ERR_ARG, "image %d: bad size or null pixels", b);
+        for (int k = 0; k < NN; k++) {
+            Plane &P = planes[(size_t)b * NN + k];
+            if (k == 0) {
+                P.w = imgs[b].width;
+                P.h = imgs[b].height;
+            } else {
+                const Plane &Q = planes[(size_t)b * NN + nodes[k].parent];
+                out_shape(nodes[k].xf, Q.w, Q.h, P.w, P.h);
+            }
+            P.off = (long long)arena_elems;
+            arena_elems += ((size_t)P.w * P.h + 31) & ~(size_t)31;
+        }
+    }
+    int r = E->arena.ensure(arena_elems * sizeof(double));
+    if (r) return r;
+    double *arena = (double *)E->arena.p;
+
+    // ---- transform jobs, grouped by (depth, transform)
+    struct TGroup { std::vector<TJob> jobs; int maxw = 0, maxh = 0; };
+    std::vector<std::vector<TGroup>> tg(maxdepth + 1, std::vector<TGroup>(X_COUNT));
+    for (int k = 1; k < NN; k++)
+        for (int b = 0; b < n; b++) {
+            TGroup &G = tg[nodes[k].depth][nodes[k].xf];
+            int src = b * NN + nodes[k].parent, dst = b * NN + k;
+            G.jobs.push_back({src, dst});
+            G.maxw = std::max(G.maxw, planes[src].w);
+            G.maxh = std::max(G.maxh, planes[src].h);
+        }
+
+    // ---- feature jobs per algorithm
+    std::vector<std::vector<FJob>> fj(A_COUNT);
+    for (size_t g = 0; g < plan.groups.size(); g++)
+        for (int b = 0; b < n; b++)
+            fj[plan.groups[g].alg].push_back({b * NN + group_node[g], b, (long long)b * plan.n_features + plan.groups[g].offset});
+
+    // ---- host metadata + workspace plan
+    Bump meta, ws;
+    struct Blob { size_t off; const void *src; size_t bytes; };
+    std::vector<Blob> blobs;
+    std::vector<std::vector<char>> owned;
+    auto put = [&](const void *p, size_t bytes) -> size_t {
+        size_t off = meta.take(bytes ? bytes : 1);
+        blobs.push_back({off, p, bytes});
+        return off;
+    };
+    auto put_vec = [&](auto &v) -> size_t { return put(v.data(), v.size() * sizeof(v[0])); };
+    auto put_copy = [&](const void *p, size_t bytes) -> size_t {
+        owned.emplace_back((const char *)p, (const char *)p + bytes);
+        return put(owned.back().data(), bytes);
+    };
+    const size_t m_planes = put_vec(planes);
+    const size_t m_stats = meta.take(sizeof(PlaneStats) * planes.size());
+
+    struct TL { size_t jobs, aux1, aux2, aux3; size_t ws; };
+    std::vector<std::vector<TL>> tl(maxdepth + 1, std::vector<TL>(X_COUNT));
+    for (int d = 1; d <= maxdepth; d++)
+        for (int x = 0; x < X_COUNT; x++) {
+            TGroup &G = tg[d][x];
+            if (G.jobs.empty()) continue;
+            TL &L = tl[d][x];
+            L.jobs = put_vec(G.jobs);
+            std::vector<long long> offs;
+            if (x == X_WAVELET) {
+                size_t tot = 0;
+                for (auto &j : G.jobs) {
+                    offs.push_back((long long)tot);
+                    tot += (size_t)planes[j.src].w * ((planes[j.src].h + 9) / 2) * 2 + 32;
+                }
+                L.ws = ws.take(tot * sizeof(double));
+                L.aux1 = put_copy(offs.data(), offs.size() * sizeof(long long));
+            } else if (x == X_FOURIER) {
+                size_t tot = 0;
+                std::vector<FFTPlan> fp;
+                std::map<int, int> idx;
+                std::vector<int> py, px;
+                for (auto &j : G.jobs) {
+                    const Plane &S = planes[j.src];
+                    offs.push_back((long long)tot);
+                    tot += (size_t)S.w * (S.h / 2 + 1) * 2 + 32;
+                    for (int len : {S.h, S.w}) {
+                        if (len > kMaxFFT) return set_err(WC_ERR_UNSUPPORTED, "Fourier: side %d > %d", len, kMaxFFT);
+                        if (!idx.count(len)) { idx[len] = (int)fp.size(); fp.push_back(fft_plan(E->tabs, len)); }
+                    }
+                    py.push_back(idx[S.h]);
+                    px.push_back(idx[S.w]);
+                }
+                L.ws = ws.take(tot * sizeof(double));
+                L.aux1 = put_copy(offs.data(), offs.size() * sizeof(long long));
+                L.aux2 = put_copy(fp.data(), fp.size() * sizeof(FFTPlan));
+                std::vector<int> pyx(py);
+                pyx.insert(pyx.end(), px.begin(), px.end());
+                L.aux3 = put_copy(pyx.data(), pyx.size() * sizeof(int));
+            } else if (x == X_CHEBYSHEV) {
+                size_t tot = 0;
+                std::vector<long long> toff;
+                for (auto &j : G.jobs) {
+                    const Plane &S = planes[j.src];
+                    int N = std::min(S.w, S.h);
+                    offs.push_back((long long)tot);
+                    tot += (size_t)S.h * N + 32;
+                    toff.push_back(E->tabs.add("ch" + std::to_string(S.w) + "_" + std::to_string(N), cheb_table(S.w, N)));
+                    toff.push_back(E->tabs.add("ch" + std::to_string(S.h) + "_" + std::to_string(N), cheb_table(S.h, N)));
+                }
+                L.ws = ws.take(tot * sizeof(double));
+                L.aux1 = put_copy(offs.data(), offs.size() * sizeof(long long));
+                L.aux2 = put_copy(toff.data(), toff.size() * sizeof(long long));
+            }
+        }
+
+    // feature-family preparation (tables, workspace, metadata)
+    FeatureSetup fs;
+    fs.planes = &planes;
+    fs.fj = &fj;
+    fs.tabs_add = [&](const std::string &k, const std::vector<double> &v) { return E->tabs.add(k, v); };
+    fs.fft_plan = [&](int len) { return fft_plan(E->tabs, len); };
+    fs.put_copy = put_copy;
+    fs.ws_take = [&](size_t bytes) { return ws.take(bytes); };
+    fs.meta_take = [&](size_t bytes) { return meta.take(bytes); };
+    r = features_prepare(fs);
+    if (r) return r;
+
+    // ---- device buffers and uploads
+    size_t in_bytes = 0;
+    std::vector<size_t> in_off(n);
+    for (int b = 0; b < n; b++) {
+        if (imgs[b].on_device) continue;
+        size_t es = imgs[b].dtype == WC_U8 ? 1 : imgs[b].dtype == WC_U16 ? 2 : imgs[b].dtype == WC_F32 ? 4 : 8;
+        in_off[b] = in_bytes;
+        in_bytes += ((size_t)imgs[b].width * imgs[b].height * es + 255) & ~(size_t)255;
+    }
+    if ((r = E->meta.ensure(meta.used + 256))) return r;
+    if ((r = E->ws.ensure(ws.used + 256))) return r;
+    if ((r = E->stage.ensure(in_bytes + 256))) return r;
+    if ((r = E->tabs.sync(E->st))) return r;
+    E->hmeta.resize(meta.used + 256);
+    for (auto &bl : blobs)
+        if (bl.bytes) memcpy(E->hmeta.data() + bl.off, bl.src, bl.bytes);
+    char *dm = (char *)E->meta.p;
+    char *dw = (char *)E->ws.p;
+    CK(cudaMemcpyAsync(dm, E->hmeta.data(), meta.used, cudaMemcpyHostToDevice, E->st));
+    for (int b = 0; b < n; b++) {
+        const wc_image_desc &I = imgs[b];
+        size_t es = I.dtype == WC_U8 ? 1 : I.dtype == WC_U16 ? 2 : I.dtype == WC_F32 ? 4 : 8;
+        const void *src = I.pixels;
+        if (!I.on_device) {
+            CK(cudaMemcpyAsync((char *)E->stage.p + in_off[b], I.pixels, (size_t)I.width * I.height * es,
+                               cudaMemcpyHostToDevice, E->st));
+            src = (char *)E->stage.p + in_off[b];
+        }
+        launch_convert(ctx, src, I.dtype, arena + planes[(size_t)b * NN].off, (long long)I.width * I.height);
+    }
+    const Plane *dplanes = (const Plane *)(dm + m_planes);
+    PlaneStats *dstats = (PlaneStats *)(dm + m_stats);
+
+    // ---- transforms, depth by depth
+    for (int d = 1; d <= maxdepth; d++)
+        for (int x = 0; x < X_COUNT; x++) {
+            TGroup &G = tg[d][x];
+            if (G.jobs.empty()) continue;
+            TL &L = tl[d][x];
+            const TJob *dj = (const TJob *)(dm + L.jobs);
+            const int nj = (int)G.jobs.size();
+            if (x == X_EDGE) launch_edge(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh);
+            else if (x == X_WAVELET)
+                launch_wavelet(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh, (double *)(dw + L.ws),
+                               (const long long *)(dm + L.aux1));
+            else if (x == X_FOURIER)
+                launch_fourier(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh, (const FFTPlan *)(dm + L.aux2),
+                               (const int *)(dm + L.aux3), (const int *)(dm + L.aux3) + nj, E->tabs.d(),
+                               (double *)(dw + L.ws), (const long long *)(dm + L.aux1));
+            else
+                launch_chebyshev(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh, E->tabs.d(),
+                                 (const long long *)(dm + L.aux2), (double *)(dw + L.ws),
+                                 (const long long *)(dm + L.aux1));
+        }
+    launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats);
+
+    FeatureRun fr;
+    fr.ctx = &ctx;
+    fr.arena = arena;
+    fr.planes = dplanes;
+    fr.stats = dstats;
+    fr.meta = dm;
+    fr.ws = dw;
+    fr.tabs = E->tabs.d();
+    fr.feat = dfeat;
+    r = features_launch(fs, fr);
+    if (r) return r;
+    CK(cudaGetLastError());
+    if (planes_out) *planes_out = planes;
+    return WC_OK;
+}
+
+}  // namespace wc
+
+namespace wc {
+int engine_device(wc_engine *E, cudaStream_t *st, long long **launches) {
+    CK(cudaSetDevice(E->dev));
+    *st = E->st;
+    *launches = &E->launches;
+    return WC_OK;
+}
+}  // namespace wc
+
+// ================================================================= C ABI
+extern "C" {
+
+const char *wc_last_error(void) { return g_err.c_str(); }
+const char *wc_version(void) { return "wndcharm-gb300 0.1 (sm_103a)"; }
+
+int wc_plan_get(int kind, const wc_plan **out) {
+    if (!out || (kind != WC_PLAN_SHORT && kind != WC_PLAN_LONG)) return set_err(WC_ERR_ARG, "wc_plan_get: bad kind");
+    *out = static_cast<const wc_plan *>(standard_plan(kind));
+    return WC_OK;
+}
+
+int wc_plan_from_names(const char *const *groups, int n, wc_plan **out) {
+    if (!out || !groups || n < 1) return set_err(WC_ERR_ARG, "wc_plan_from_names: bad arguments");
+    std::string err;
+    Plan *p = plan_from_names(groups, n, err);
+    if (!p) return set_err(WC_ERR_ARG, "%s", err.c_str());
+    *out = static_cast<wc_plan *>(p);
+    return WC_OK;
+}
+
+void wc_plan_free(wc_plan *plan) {
+    if (plan && !plan->standard) delete plan;
+}
+
+int wc_plan_n_features(const wc_plan *plan) { return plan ? plan->n_features : set_err(WC_ERR_ARG, "null plan"); }
+
+int wc_plan_feature_name(const wc_plan *plan, int i, char *buf, int buflen) {
+    if (!plan || !buf || buflen < 1 || i < 0 || i >= plan->n_features) return set_err(WC_ERR_ARG, "bad feature index");
+    const std::string &s = plan->names[i];
+    strncpy(buf, s.c_str(), (size_t)buflen - 1);
+    buf[buflen - 1] = 0;
+    return (int)s.size();
+}
+
+int wc_plan_n_groups(const wc_plan *plan) { return plan ? (int)plan->groups.size() : set_err(WC_ERR_ARG, "null plan"); }
+
+int wc_plan_group(const wc_plan *plan, int g, char *buf, int buflen, int *offset, int *nf) {
+    if (!plan || g < 0 || g >= (int)plan->groups.size()) return set_err(WC_ERR_ARG, "bad group index");
+    const Group &G = plan->groups[g];
+    if (buf && buflen > 0) {
+        strncpy(buf, G.name.c_str(), (size_t)buflen - 1);
+        buf[buflen - 1] = 0;
+    }
+    if (offset) *offset = G.offset;
+    if (nf) *nf = kAlgN[G.alg];
+    return WC_OK;
+}
+
+int wc_engine_create(int device, int precision, wc_engine **out) {
+    if (!out) return set_err(WC_ERR_ARG, "null out");
+    if (precision != WC_PREC_FP64 && precision != WC_PREC_MIXED) return set_err(WC_ERR_ARG, "bad precision");
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return set_err(WC_ERR_ARG, "no CUDA device %d", device);
+    CK(cudaSetDevice(device));
+    wc_engine *E = new wc_engine;
+    E->dev = device;
+    E->prec = precision;
+    cudaDeviceGetAttribute(&E->sms, cudaDevAttrMultiProcessorCount, device);
+    double cs[8];
+    const double th[4] = {0, 45, 90, 135};
+    for (int k = 0; k < 4; k++) {
+        double a = (th[k] * M_PI) / 180;
+        cs[2 * k] = cos(a);
+        cs[2 * k + 1] = sin(a);
+    }
+    set_radon_table(cs);
+    features_init();
+    *out = E;
+    return WC_OK;
+}
+
+void wc_engine_destroy(wc_engine *E) {
+    if (!E) return;
+    cudaSetDevice(E->dev);
+    cudaStreamSynchronize(E->st);
+    delete E;
+}
+
+int wc_engine_set_stream(wc_engine *E, void *stream) {
+    if (!E) return set_err(WC_ERR_ARG, "null engine");
+    E->st = (cudaStream_t)stream;
+    return WC_OK;
+}
+
+long long wc_engine_launch_count(const wc_engine *E) { return E ? E->launches : 0; }
+
+int wc_extract_batch(wc_engine *E, const wc_plan *plan, const wc_image_desc *images, int n, double *out,
+                     int out_on_device) {
+    if (!E || !plan || !images || n < 1 || !out) return set_err(WC_ERR_ARG, "wc_extract_batch: bad arguments");
+    std::lock_guard<std::mutex> lk(E->mu);
+    CK(cudaSetDevice(E->dev));
+    double *dfeat = out;
+    size_t fbytes = (size_t)n * plan->n_features * sizeof(double);
+    if (!out_on_device) {
+        int r = E->feat.ensure(fbytes);
+        if (r) return r;
+        dfeat = (double *)E->feat.p;
+    }
+    CK(cudaMemsetAsync(dfeat, 0, fbytes, E->st));
+    int r = run_batch(E, *plan, images, n, dfeat);
+    if (r) return r;
+    if (!out_on_device) {
+        CK(cudaMemcpyAsync(out, dfeat, fbytes, cudaMemcpyDeviceToHost, E->st));
+        CK(cudaStreamSynchronize(E->st));
+    }
+    int dev_err = 0;
+    if ((r = features_check(E->st, &dev_err))) return r;
+    if (dev_err) return set_err(WC_ERR_DEVICE, "a kernel reported error code %d", dev_err);
+    return WC_OK;
+}
+
+int wc_transform(wc_engine *E, const char *name, const double *pixels, int width, int height, double *out,
+                 long long cap, int *ow, int *oh) {
+    if (!E || !name || !pixels || !out || !ow || !oh || width < 1 || height < 1)
+        return set_err(WC_ERR_ARG, "wc_transform: bad arguments");
+    int xf = -1;
+    for (int i = 0; i < X_COUNT; i++)
+        if (!strcmp(name, kXfName[i])) xf = i;
+    if (xf < 0) return set_err(WC_ERR_ARG, "wc_transform: unknown transform '%s'", name);
+    std::lock_guard<std::mutex> lk(E->mu);
+    CK(cudaSetDevice(E->dev));
+    Plan p;
+    Group g;
+    g.alg = A_MSHIST;
+    g.chain = {xf};
+    g.offset = 0;
+    p.groups.push_back(g);
+    p.n_features = kAlgN[A_MSHIST];
+    int r = E->feat.ensure(p.n_features * sizeof(double));
+    if (r) return r;
+    wc_image_desc d{pixels, WC_F64, width, height, 16, 0};
+    std::vector<Plane> planes;
+    if ((r = run_batch(E, p, &d, 1, (double *)E->feat.p, &planes))) return r;
+    const Plane &Q = planes[1];
+    if ((long long)Q.w * Q.h > cap) return set_err(WC_ERR_ARG, "wc_transform: output needs %d x %d", Q.w, Q.h);
+    CK(cudaMemcpyAsync(out, (double *)E->arena.p + Q.off, sizeof(double) * Q.w * Q.h, cudaMemcpyDeviceToHost, E->st));
+    CK(cudaStreamSynchronize(E->st));
+    *ow = Q.w;
+    *oh = Q.h;
+    return WC_OK;
+}
+
+int wc_extract(wc_engine *E, const wc_plan *plan, const void *pixels, int dtype, int width, int height, int bits,
+               double *out_row) {
+    wc_image_desc d{pixels, dtype, width, height, bits, 0};
+    return wc_extract_batch(E, plan, &d, 1, out_row, 0);
+}
+
+}  // extern "C"

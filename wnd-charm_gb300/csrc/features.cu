@@ -1,0 +1,134 @@
+// Per-family preparation and launch for one batch: builds each family's job
+// list, tables and workspace on the host, then launches the family kernels.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "../../include/wndcharm_gb300.h"
+#include "wc_features.h"
+#include "kcommon.cuh"
+
+namespace wc {
+
+__device__ int g_dev_err = 0;
+
+std::vector<double> cheb_table(int len, int N);
+
+void features_init() {}
+
+int features_check(cudaStream_t st, int *dev_err) {
+    int v = 0;
+    if (cudaMemcpyFromSymbolAsync(&v, g_dev_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return set_err(WC_ERR_CUDA, "reading the device error word failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (v) {
+        int z = 0;
+        cudaMemcpyToSymbolAsync(g_dev_err, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+        cudaStreamSynchronize(st);
+    }
+    *dev_err = v;
+    return WC_OK;
+}
+
+static int maxw_of(const std::vector<Plane> &P, const std::vector<FJob> &J) {
+    int m = 0;
+    for (auto &j : J) m = std::max(m, P[j.plane].w);
+    return m;
+}
+static int maxh_of(const std::vector<Plane> &P, const std::vector<FJob> &J) {
+    int m = 0;
+    for (auto &j : J) m = std::max(m, P[j.plane].h);
+    return m;
+}
+
+int features_prepare(FeatureSetup &fs) {
+    const auto &P = *fs.planes;
+    const auto &fj = *fs.fj;
+    for (int a = 0; a < A_COUNT; a++)
+        if (!fj[a].empty()) fs.off["jobs" + std::to_string(a)] = fs.put_copy(fj[a].data(), fj[a].size() * sizeof(FJob));
+
+    // planes that need a sorted copy: PixStats, Gini
+    std::map<int, int> slot_of;
+    std::vector<int> sort_planes;
+    for (int a : {A_PIXSTATS, A_GINI})
+        for (auto &j : fj[a])
+            if (!slot_of.count(j.plane)) {
+                slot_of[j.plane] = (int)sort_planes.size();
+                sort_planes.push_back(j.plane);
+            }
+    if (!sort_planes.empty()) {
+        std::vector<long long> koff;
+        size_t tot = 0;
+        for (int p : sort_planes) {
+            koff.push_back((long long)tot);
+            tot += ((size_t)P[p].w * P[p].h + 31) & ~(size_t)31;
+        }
+        fs.off["sort_ids"] = fs.put_copy(sort_planes.data(), sort_planes.size() * sizeof(int));
+        fs.off["sort_koff"] = fs.put_copy(koff.data(), koff.size() * sizeof(long long));
+        fs.off["sort_keys"] = fs.ws_take(tot * 8);
+        fs.off["sort_tmp"] = fs.ws_take(tot * 8);
+        fs.off["sort_cnt"] = fs.ws_take(sort_planes.size() * 256 * 512 * sizeof(unsigned int));
+        fs.val["sort_n"] = (long long)sort_planes.size();
+        for (int a : {A_PIXSTATS, A_GINI}) {
+            std::vector<int> slots;
+            for (auto &j : fj[a]) slots.push_back(slot_of[j.plane]);
+            if (!slots.empty()) fs.off["slots" + std::to_string(a)] = fs.put_copy(slots.data(), slots.size() * sizeof(int));
+        }
+    }
+
+    // Chebyshev coefficients: N = min(20, W, H) tables and H x N workspace
+    if (!fj[A_CHEB].empty()) {
+        std::vector<long long> toff, moff;
+        size_t tot = 0;
+        for (auto &j : fj[A_CHEB]) {
+            const Plane &Q = P[j.plane];
+            int N = std::min(20, std::min(Q.w, Q.h));
+            toff.push_back(fs.tabs_add("ch" + std::to_string(Q.w) + "_" + std::to_string(N), cheb_table(Q.w, N)));
+            toff.push_back(fs.tabs_add("ch" + std::to_string(Q.h) + "_" + std::to_string(N), cheb_table(Q.h, N)));
+            moff.push_back((long long)tot);
+            tot += (size_t)Q.h * N + 32;
+        }
+        fs.off["cc_tab"] = fs.put_copy(toff.data(), toff.size() * sizeof(long long));
+        fs.off["cc_moff"] = fs.put_copy(moff.data(), moff.size() * sizeof(long long));
+        fs.off["cc_mid"] = fs.ws_take(tot * sizeof(double));
+    }
+    return WC_OK;
+}
+
+int features_launch(FeatureSetup &fs, FeatureRun &fr) {
+    const auto &P = *fs.planes;
+    const auto &fj = *fs.fj;
+    Ctx &c = *fr.ctx;
+    auto jobs = [&](int a) { return (const FJob *)(fr.meta + fs.off["jobs" + std::to_string(a)]); };
+    auto nj = [&](int a) { return (int)fj[a].size(); };
+
+    if (fs.val.count("sort_n")) {
+        launch_plane_sort(c, fr.arena, fr.planes, (const int *)(fr.meta + fs.off["sort_ids"]), (int)fs.val["sort_n"],
+                          (unsigned long long *)(fr.ws + fs.off["sort_keys"]),
+                          (unsigned long long *)(fr.ws + fs.off["sort_tmp"]),
+                          (const long long *)(fr.meta + fs.off["sort_koff"]),
+                          (unsigned int *)(fr.ws + fs.off["sort_cnt"]));
+        const unsigned long long *keys = (const unsigned long long *)(fr.ws + fs.off["sort_keys"]);
+        const long long *koff = (const long long *)(fr.meta + fs.off["sort_koff"]);
+        if (nj(A_PIXSTATS))
+            launch_pixstats(c, fr.planes, fr.stats, jobs(A_PIXSTATS), nj(A_PIXSTATS),
+                            (const int *)(fr.meta + fs.off["slots" + std::to_string(A_PIXSTATS)]), keys, koff, fr.feat);
+        if (nj(A_GINI))
+            launch_gini(c, fr.planes, jobs(A_GINI), nj(A_GINI),
+                        (const int *)(fr.meta + fs.off["slots" + std::to_string(A_GINI)]), keys, koff, fr.feat);
+    }
+    if (nj(A_MSHIST)) launch_mshist(c, fr.arena, fr.planes, fr.stats, jobs(A_MSHIST), nj(A_MSHIST), fr.feat);
+    if (nj(A_FRACTAL)) launch_fractal(c, fr.arena, fr.planes, jobs(A_FRACTAL), nj(A_FRACTAL), fr.feat);
+    if (nj(A_COMB)) launch_comb(c, fr.arena, fr.planes, jobs(A_COMB), nj(A_COMB), fr.feat);
+    if (nj(A_RADON))
+        launch_radon(c, fr.arena, fr.planes, jobs(A_RADON), nj(A_RADON), maxw_of(P, fj[A_RADON]), maxh_of(P, fj[A_RADON]),
+                     fr.feat);
+    if (nj(A_CHEB))
+        launch_chebcoef(c, fr.arena, fr.planes, jobs(A_CHEB), nj(A_CHEB), fr.tabs,
+                        (const long long *)(fr.meta + fs.off["cc_tab"]), (double *)(fr.ws + fs.off["cc_mid"]),
+                        (const long long *)(fr.meta + fs.off["cc_moff"]), fr.feat);
+    return WC_OK;
+}
+
+}  // namespace wc

@@ -1,0 +1,642 @@
+// Per-plane basics: pixel conversion, plane statistics, the Edge and Wavelet
+// transforms, a per-plane radix sort (medians, Gini), and the light feature
+// families (multiscale histograms, fractal, comb moments, pixel statistics,
+// Gini, Radon, Chebyshev coefficients).  FP64 arithmetic throughout.
+#include <cfloat>
+#include <cmath>
+
+#include "kcommon.cuh"
+#include "kernels.h"
+
+namespace wc {
+
+// ---------------------------------------------------------------- convert
+template <typename T>
+__global__ void k_convert(const T *__restrict__ src, double *__restrict__ dst, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
+}
+
+void launch_convert(Ctx &c, const void *src, int dtype, double *dst, long long n) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > c.sms * 8) blocks = c.sms * 8;
+    if (blocks < 1) blocks = 1;
+    WC_LAUNCH(c);
+    switch (dtype) {
+        case 0: k_convert<unsigned char><<<blocks, 256, 0, c.st>>>((const unsigned char *)src, dst, n); break;
+        case 1: k_convert<unsigned short><<<blocks, 256, 0, c.st>>>((const unsigned short *)src, dst, n); break;
+        case 2: k_convert<float><<<blocks, 256, 0, c.st>>>((const float *)src, dst, n); break;
+        default: k_convert<double><<<blocks, 256, 0, c.st>>>((const double *)src, dst, n); break;
+    }
+}
+
+// ---------------------------------------------------------------- plane stats
+// Moments2 of every plane (src/statistics/Moments.h:61-107): min, max, mean,
+// var = M2/(n-1) for n > 2.  Two deterministic passes per plane, one CTA each.
+__global__ void __launch_bounds__(1024) k_plane_stats(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                      PlaneStats *__restrict__ out) {
+    __shared__ double sh[32];
+    const Plane P = planes[blockIdx.x];
+    const double *p = arena + P.off;
+    const long long n = (long long)P.w * P.h;
+    double mn = DBL_MAX, mx = -DBL_MAX, s = 0;
+    long long cnt = 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = p[i];
+        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;  // Moments2::add skips these
+        mn = fmin(mn, v);
+        mx = fmax(mx, v);
+        s += v;
+        cnt++;
+    }
+    mn = block_min(mn, sh);
+    mx = block_max(mx, sh);
+    s = block_sum(s, sh);
+    __shared__ long long shl[32];
+    cnt = block_sum_ll(cnt, shl);
+    double mean = cnt ? s / cnt : 0.0;
+    double m2 = 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = p[i];
+        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;
+        double d = v - mean;
+        m2 += d * d;
+    }
+    m2 = block_sum(m2, sh);
+    if (threadIdx.x == 0) {
+        PlaneStats r;
+        r.mn = mn;
+        r.mx = mx;
+        r.mean = mean;
+        r.var = cnt > 2 ? m2 / (cnt - 1) : 0.0;
+        r.sum = s;
+        r.n = cnt;
+        out[blockIdx.x] = r;
+    }
+}
+
+void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int nplanes, PlaneStats *out) {
+    if (nplanes <= 0) return;
+    WC_LAUNCH(c);
+    k_plane_stats<<<nplanes, 1024, 0, c.st>>>(arena, planes, out);
+}
+
+// ---------------------------------------------------------------- Edge transform
+// ImageMatrix::EdgeTransform, src/cmatrix.cpp:1294-1311.
+__global__ void k_edge(double *__restrict__ arena, const Plane *__restrict__ planes, const TJob *__restrict__ jobs) {
+    const TJob J = jobs[blockIdx.z];
+    const Plane S = planes[J.src], D = planes[J.dst];
+    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= S.w || y >= S.h) return;
+    const double *in = arena + S.off;
+    const int W = S.w, H = S.h;
+    double c = in[(long long)y * W + x], mx = 0, my = 0;
+    if (y > 0 && y < H - 1) my = fmax(fabs(c - in[(long long)(y - 1) * W + x]), fabs(c - in[(long long)(y + 1) * W + x]));
+    if (x > 0 && x < W - 1) mx = fmax(fabs(c - in[(long long)y * W + x - 1]), fabs(c - in[(long long)y * W + x + 1]));
+    arena[D.off + (long long)y * W + x] = fmax(mx, my);
+}
+
+void launch_edge(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh) {
+    if (njobs <= 0) return;
+    dim3 b(32, 8), g((maxw + 31) / 32, (maxh + 7) / 8, njobs);
+    WC_LAUNCH(c);
+    k_edge<<<g, b, 0, c.st>>>(arena, planes, jobs);
+}
+
+// ---------------------------------------------------------------- Wavelet transform
+// One level of the zero-padded Symlet-5 decomposition
+// (Wavelet::transform2D, src/transforms/wavelet/Wavelet.cpp:136-434, with
+// downsampling_convolution MODE_ZEROPAD, convolution.cpp:86-325):
+// out[o] = sum_j f[j] * x[2o+1-j] over the taps inside the input, j ascending.
+__constant__ double c_sym_lo[10] = {0.027333068345077982, 0.029519490925774643, -0.039134249302383094,
+                                    0.1993975339773936, 0.72340769040242059, 0.63397896345821192,
+                                    0.016602105764522319, -0.17532808990845047, -0.021101834024758855,
+                                    0.019538882735286728};
+__constant__ double c_sym_hi[10] = {-0.019538882735286728, -0.021101834024758855, 0.17532808990845047,
+                                    0.016602105764522319, -0.63397896345821192, 0.72340769040242059,
+                                    -0.1993975339773936, -0.039134249302383094, -0.029519490925774643,
+                                    0.027333068345077982};
+
+// pass 1: along y for each column x: tmp[(x*oy + o)*2 + {0: approx, 1: detail}]
+__global__ void k_wavelet_y(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                            const TJob *__restrict__ jobs, double *__restrict__ tmp, const long long *__restrict__ tmp_off) {
+    const TJob J = jobs[blockIdx.z];
+    const Plane S = planes[J.src];
+    const int X = S.w, Y = S.h, oy = (Y + 9) / 2;
+    int x = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= X || o >= oy) return;
+    const double *in = arena + S.off;
+    const int i = 2 * o + 1;
+    double a = 0, d = 0;
+#pragma unroll
+    for (int j = 0; j < 10; j++) {
+        int k = i - j;
+        if (k >= 0 && k < Y) {
+            double v = in[(long long)k * X + x];
+            a = __dadd_rn(a, __dmul_rn(v, c_sym_lo[j]));
+            d = __dadd_rn(d, __dmul_rn(v, c_sym_hi[j]));
+        }
+    }
+    double *t = tmp + tmp_off[blockIdx.z];
+    t[((long long)x * oy + o) * 2 + 0] = a;
+    t[((long long)x * oy + o) * 2 + 1] = d;
+}
+
+// pass 2: along x for each row o of both pass-1 outputs, placed in quadrants:
+// (y<oy, x<ox) dd, (y>=oy, x<ox) da, (y<oy, x>=ox) ad, (y>=oy, x>=ox) aa.
+__global__ void k_wavelet_x(double *__restrict__ arena, const Plane *__restrict__ planes, const TJob *__restrict__ jobs,
+                            const double *__restrict__ tmp, const long long *__restrict__ tmp_off) {
+    const TJob J = jobs[blockIdx.z];
+    const Plane S = planes[J.src], D = planes[J.dst];
+    const int X = S.w, Y = S.h, ox = (X + 9) / 2, oy = (Y + 9) / 2;
+    int u = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= ox || o >= oy) return;
+    const double *t = tmp + tmp_off[blockIdx.z];
+    const int i = 2 * u + 1;
+    double a1 = 0, d1 = 0, a2 = 0, d2 = 0;
+#pragma unroll
+    for (int j = 0; j < 10; j++) {
+        int k = i - j;
+        if (k >= 0 && k < X) {
+            double va = t[((long long)k * oy + o) * 2 + 0], vd = t[((long long)k * oy + o) * 2 + 1];
+            a1 = __dadd_rn(a1, __dmul_rn(va, c_sym_lo[j]));
+            d1 = __dadd_rn(d1, __dmul_rn(va, c_sym_hi[j]));
+            a2 = __dadd_rn(a2, __dmul_rn(vd, c_sym_lo[j]));
+            d2 = __dadd_rn(d2, __dmul_rn(vd, c_sym_hi[j]));
+        }
+    }
+    double *out = arena + D.off;
+    const int W = D.w;
+    out[(long long)o * W + u] = d2;
+    out[(long long)(oy + o) * W + u] = a2;
+    out[(long long)o * W + ox + u] = d1;
+    out[(long long)(oy + o) * W + ox + u] = a1;
+}
+
+void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
+                    double *tmp, const long long *tmp_off) {
+    if (njobs <= 0) return;
+    int ox = (maxw + 9) / 2, oy = (maxh + 9) / 2;
+    dim3 b(32, 8);
+    WC_LAUNCH(c);
+    k_wavelet_y<<<dim3((maxw + 31) / 32, (oy + 7) / 8, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp, tmp_off);
+    WC_LAUNCH(c);
+    k_wavelet_x<<<dim3((ox + 31) / 32, (oy + 7) / 8, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp, tmp_off);
+}
+
+// ---------------------------------------------------------------- radix sort
+// LSD radix sort of each plane's values (64-bit orderable keys, 8-bit digits),
+// one CTA per plane.  Each thread owns a contiguous segment, so the scatter is
+// stable without in-tile ranking: position = base[d] + count of digit d in
+// earlier segments + count earlier in the own segment.  Passes whose digit is
+// the same for every key are skipped.  `cnt` holds 256 x blockDim counters.
+#define SORT_THREADS 512
+__global__ void __launch_bounds__(SORT_THREADS) k_plane_sort(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                             const int *__restrict__ plane_ids,
+                                                             unsigned long long *__restrict__ keys,
+                                                             unsigned long long *__restrict__ tmp,
+                                                             const long long *__restrict__ key_off,
+                                                             unsigned int *__restrict__ counts) {
+    const Plane P = planes[plane_ids[blockIdx.x]];
+    const long long n = (long long)P.w * P.h;
+    unsigned long long *A = keys + key_off[blockIdx.x], *B = tmp + key_off[blockIdx.x];
+    unsigned int *cnt = counts + (size_t)blockIdx.x * 256 * SORT_THREADS;
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long seg = (n + T - 1) / T, s0 = t * seg, s1 = min(n, s0 + seg);
+    const double *src = arena + P.off;
+    for (long long i = t; i < n; i += T) A[i] = dkey(src[i]);
+    __shared__ unsigned int base[256];
+    __shared__ int skip;
+    __syncthreads();
+    for (int pass = 0; pass < 8; pass++) {
+        const int sh = pass * 8;
+        unsigned int local[256];
+        // count digits of the own segment (registers spill to local memory; fine)
+        for (int d = 0; d < 256; d++) local[d] = 0;
+        for (long long i = s0; i < s1; i++) local[(A[i] >> sh) & 255]++;
+        for (int d = 0; d < 256; d++) cnt[(size_t)d * T + t] = local[d];
+        __syncthreads();
+        // per digit: exclusive scan over threads, digit totals
+        if (t < 256) {
+            unsigned int run = 0;
+            for (int u = 0; u < T; u++) {
+                unsigned int v = cnt[(size_t)t * T + u];
+                cnt[(size_t)t * T + u] = run;
+                run += v;
+            }
+            base[t] = run;
+        }
+        if (t == 0) skip = 0;
+        __syncthreads();
+        if (t == 0) {
+            unsigned int run = 0;
+            for (int d = 0; d < 256; d++) {
+                unsigned int v = base[d];
+                if (v == (unsigned int)n) skip = 1;
+                base[d] = run;
+                run += v;
+            }
+        }
+        __syncthreads();
+        if (!skip) {
+            for (int d = 0; d < 256; d++) local[d] = base[d] + cnt[(size_t)d * T + t];
+            for (long long i = s0; i < s1; i++) {
+                unsigned long long k = A[i];
+                B[local[(k >> sh) & 255]++] = k;
+            }
+            __syncthreads();
+            unsigned long long *x = A;
+            A = B;
+            B = x;
+        }
+        __syncthreads();
+    }
+    // result must end in `keys`
+    if (A != keys + key_off[blockIdx.x]) {
+        for (long long i = t; i < n; i += T) B[i] = A[i];
+    }
+}
+
+void launch_plane_sort(Ctx &c, const double *arena, const Plane *planes, const int *plane_ids, int n,
+                       unsigned long long *keys, unsigned long long *tmp, const long long *key_off,
+                       unsigned int *counts) {
+    if (n <= 0) return;
+    WC_LAUNCH(c);
+    k_plane_sort<<<n, SORT_THREADS, 0, c.st>>>(arena, planes, plane_ids, keys, tmp, key_off, counts);
+}
+
+// ---------------------------------------------------------------- pixel statistics + Gini
+// PixelIntensityStatistics (src/FeatureAlgorithms.cpp:272-294) and
+// GiniCoefficient (src/FeatureAlgorithms.cpp:448-492) from a sorted plane.
+// job.plane indexes `sorted_ids` position via job.img (sort slot).
+__global__ void k_pixstats(const Plane *__restrict__ planes, const PlaneStats *__restrict__ stats,
+                           const FJob *__restrict__ jobs, const int *__restrict__ sort_slot,
+                           const unsigned long long *__restrict__ keys, const long long *__restrict__ key_off,
+                           double *__restrict__ feat) {
+    const FJob J = jobs[blockIdx.x];
+    if (threadIdx.x != 0) return;
+    const Plane P = planes[J.plane];
+    const PlaneStats S = stats[J.plane];
+    const long long n = (long long)P.w * P.h, half = n / 2;
+    const unsigned long long *k = keys + key_off[sort_slot[blockIdx.x]];
+    double med;
+    if (n % 2 == 0) med = (dkey_inv(k[half]) + dkey_inv(k[half - 1])) / 2.0;
+    else med = dkey_inv(k[half]);
+    double *o = feat + J.out;
+    o[0] = S.mean;
+    o[1] = med;
+    o[2] = S.n > 2 ? sqrt(S.var) : 0.0;
+    o[3] = S.mn;
+    o[4] = S.mx;
+}
+
+__global__ void k_gini(const Plane *__restrict__ planes, const FJob *__restrict__ jobs, const int *__restrict__ sort_slot,
+                       const unsigned long long *__restrict__ keys, const long long *__restrict__ key_off,
+                       double *__restrict__ feat) {
+    __shared__ double sh[32];
+    __shared__ long long shl[32];
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const long long n = (long long)P.w * P.h;
+    const unsigned long long *k = keys + key_off[sort_slot[blockIdx.x]];
+    // positives form a suffix of the sorted keys: find its start by binary search
+    long long lo = 0, hi = n;
+    while (lo < hi) {
+        long long mid = (lo + hi) / 2;
+        if (dkey_inv(k[mid]) > 0) hi = mid; else lo = mid + 1;
+    }
+    const long long first = lo, count = n - first;
+    double sum = 0, g = 0;
+    for (long long i = threadIdx.x; i < count; i += blockDim.x) {
+        double v = dkey_inv(k[first + i]);
+        sum += v;
+        g += (2. * (double)(i + 1) - (double)count - 1.) * v;
+    }
+    sum = block_sum(sum, sh);
+    g = block_sum(g, sh);
+    if (threadIdx.x == 0) {
+        double mean = count > 0 ? sum / count : 0.0;
+        feat[J.out] = (count <= 1 || mean <= 0.0) ? 0.0 : g / (mean * count * (count - 1));
+    }
+}
+
+void launch_pixstats(Ctx &c, const Plane *planes, const PlaneStats *stats, const FJob *jobs, int njobs,
+                     const int *sort_slot, const unsigned long long *keys, const long long *key_off, double *feat) {
+    if (njobs <= 0) return;
+    WC_LAUNCH(c);
+    k_pixstats<<<njobs, 32, 0, c.st>>>(planes, stats, jobs, sort_slot, keys, key_off, feat);
+}
+void launch_gini(Ctx &c, const Plane *planes, const FJob *jobs, int njobs, const int *sort_slot,
+                 const unsigned long long *keys, const long long *key_off, double *feat) {
+    if (njobs <= 0) return;
+    WC_LAUNCH(c);
+    k_gini<<<njobs, 512, 0, c.st>>>(planes, jobs, sort_slot, keys, key_off, feat);
+}
+
+// ---------------------------------------------------------------- multiscale histograms
+// ImageMatrix::MultiScaleHistogram, src/cmatrix.cpp:1743-1756.
+__global__ void k_mshist(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                         const PlaneStats *__restrict__ stats, const FJob *__restrict__ jobs, double *__restrict__ feat) {
+    __shared__ unsigned int h[24];
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const PlaneStats S = stats[J.plane];
+    if (threadIdx.x < 24) h[threadIdx.x] = 0;
+    __syncthreads();
+    const double *p = arena + P.off;
+    const long long n = (long long)P.w * P.h;
+    const double s3 = hist_scale(S.mn, S.mx, 3), s5 = hist_scale(S.mn, S.mx, 5), s7 = hist_scale(S.mn, S.mx, 7),
+                 s9 = hist_scale(S.mn, S.mx, 9);
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = p[i];
+        atomicAdd(&h[hist_bin(v, S.mn, s3, 3)], 1u);
+        atomicAdd(&h[3 + hist_bin(v, S.mn, s5, 5)], 1u);
+        atomicAdd(&h[8 + hist_bin(v, S.mn, s7, 7)], 1u);
+        atomicAdd(&h[15 + hist_bin(v, S.mn, s9, 9)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = 0;
+        for (int a = 0; a < 24; a++) mx = fmax(mx, (double)h[a]);
+        for (int a = 0; a < 24; a++) feat[J.out + a] = (double)h[a] / mx;
+    }
+}
+
+void launch_mshist(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
+                   int njobs, double *feat) {
+    if (njobs <= 0) return;
+    WC_LAUNCH(c);
+    k_mshist<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, jobs, feat);
+}
+
+// ---------------------------------------------------------------- fractal
+// FractalFeatures::execute, src/FeatureAlgorithms.cpp:232-267: for the k-th
+// lag (k = 1 + slot*step, k < K), mean absolute difference along y and x.
+__global__ void k_fractal(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                          double *__restrict__ feat) {
+    __shared__ double sh[32];
+    const FJob J = jobs[blockIdx.y];
+    const Plane P = planes[J.plane];
+    const int W = P.w, H = P.h, slot = blockIdx.x;
+    const int K = ((W > H) ? H : W) / 5;
+    int step = K / 20;
+    if (step < 1) step = 1;
+    const int k = 1 + slot * step;
+    if (k >= K) {
+        if (threadIdx.x == 0) feat[J.out + slot] = 0.0;
+        return;
+    }
+    const double *p = arena + P.off;
+    double s = 0;
+    const long long n1 = (long long)W * (H - k), n2 = (long long)(W - k) * H;
+    for (long long i = threadIdx.x; i < n1; i += blockDim.x) {
+        long long y = i / W, x = i - y * W;
+        s += fabs(p[y * W + x] - p[(y + k) * W + x]);
+    }
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+        long long y = i / (W - k), x = i - y * (W - k);
+        s += fabs(p[y * W + x] - p[y * W + x + k]);
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) feat[J.out + slot] = s / (double)(W * (W - k) + H * (H - k));
+}
+
+void launch_fractal(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, double *feat) {
+    if (njobs <= 0) return;
+    WC_LAUNCH(c);
+    k_fractal<<<dim3(20, njobs), 512, 0, c.st>>>(arena, planes, jobs, feat);
+}
+
+// ---------------------------------------------------------------- comb moments
+// CombFirst4Moments2D + matr4moments_to_hist + vd_Comb4Moments,
+// src/statistics/CombFirst4Moments.cpp:47-272.  One warp per comb line: two
+// passes (mean, then central sums) give Moments4's mean/std/skew/kurtosis.
+__device__ __forceinline__ bool comb_pixel(int dir, long long j, long long ii, long long m, long long n, long long n2,
+                                           long long m2, long long &y, long long &x) {
+    if (dir == 0) { y = j; x = j + ii; return x >= 0 && x < n; }
+    if (dir == 1) { y = j; x = n - 1 - j - ii; return x >= 0 && x < n; }
+    if (dir == 2) { x = n2 - 1 - ii; y = j; return x >= 0 && x < n; }
+    y = m2 - 1 - ii; x = j; return y >= 0 && y < m;
+}
+
+__global__ void k_comb(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                       double *__restrict__ feat) {
+    __shared__ double M[4][4][20];  // dir, moment, sample
+    __shared__ int nsamp;
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const long long m = P.h, n = P.w, n2 = n / 2, m2 = m / 2;
+    const double *p = arena + P.off;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) {
+        double step = (double)m / 10.0;
+        if (step < 1.0) step = 1.0;
+        int k = 0;
+        for (double mp = 1.0 - m; mp <= m; mp += step) k++;
+        nsamp = k;
+    }
+    for (int i = threadIdx.x; i < 4 * 4 * 20; i += blockDim.x) (&M[0][0][0])[i] = 0.0;
+    __syncthreads();
+    for (int line = wid; line < 4 * nsamp; line += nw) {
+        const int dir = line / nsamp, si = line % nsamp;
+        double step = (double)m / 10.0;
+        if (step < 1.0) step = 1.0;
+        double mp = 1.0 - m;
+        for (int q = 0; q < si; q++) mp += step;  // same accumulation as the reference loop
+        const long long ii = llround(mp);
+        const long long len = (dir == 3) ? n : m;
+        double s = 0;
+        long long cnt = 0;
+        for (long long j = lane; j < len; j += 32) {
+            long long y, x;
+            if (comb_pixel(dir, j, ii, m, n, n2, m2, y, x)) {
+                double v = p[y * n + x];
+                if (!(isnan(v) || v > FLT_MAX || v < -FLT_MAX)) { s += v; cnt++; }
+            }
+        }
+        s = warp_sum(s);
+        cnt = warp_sum_ll(cnt);
+        s = __shfl_sync(0xffffffffu, s, 0);
+        cnt = __shfl_sync(0xffffffffu, cnt, 0);
+        const double mean = cnt ? s / cnt : 0.0;
+        double a2 = 0, a3 = 0, a4 = 0;
+        for (long long j = lane; j < len; j += 32) {
+            long long y, x;
+            if (comb_pixel(dir, j, ii, m, n, n2, m2, y, x)) {
+                double v = p[y * n + x];
+                if (!(isnan(v) || v > FLT_MAX || v < -FLT_MAX)) {
+                    double d = v - mean, d2 = d * d;
+                    a2 += d2;
+                    a3 += d2 * d;
+                    a4 += d2 * d2;
+                }
+            }
+        }
+        a2 = warp_sum(a2);
+        a3 = warp_sum(a3);
+        a4 = warp_sum(a4);
+        if (lane == 0) {
+            const double nn = (double)cnt;
+            M[dir][0][si] = mean;
+            M[dir][1][si] = cnt > 2 ? sqrt(a2 / (nn - 1)) : 0.0;
+            M[dir][2][si] = cnt > 3 ? (sqrt(nn) * a3) / pow(a2, 1.5) : 0.0;
+            M[dir][3][si] = cnt > 4 ? (nn * a4) / (a2 * a2) : 0.0;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 16) {
+        const int dir = threadIdx.x / 4, a = threadIdx.x % 4;
+        double lo = 10E200, hi = -10E200;
+        for (int b = 0; b < 20; b++) {
+            double v = M[dir][a][b];
+            if (v > hi) hi = v;
+            if (v < lo) lo = v;
+        }
+        const double sc = hist_scale(lo, hi, 3);
+        double bins[3] = {0, 0, 0};
+        for (int b = 0; b < 20; b++) bins[hist_bin(M[dir][a][b], lo, sc, 3)] += 1.0;
+        // raw position (dir*4 + a)*3 + bin, permuted by vd_Comb4Moments
+        const int perm[48] = {45, 46, 47, 36, 37, 38, 42, 43, 44, 39, 40, 41, 33, 34, 35, 24, 25, 26, 30, 31, 32, 27, 28, 29,
+                              9, 10, 11, 0, 1, 2, 6, 7, 8, 3, 4, 5, 21, 22, 23, 12, 13, 14, 18, 19, 20, 15, 16, 17};
+        for (int b = 0; b < 3; b++) {
+            const int raw = (dir * 4 + a) * 3 + b;
+            for (int o = 0; o < 48; o++)
+                if (perm[o] == raw) feat[J.out + o] = bins[b];
+        }
+    }
+}
+
+void launch_comb(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, double *feat) {
+    if (njobs <= 0) return;
+    WC_LAUNCH(c);
+    k_comb<<<njobs, 512, 0, c.st>>>(arena, planes, jobs, feat);
+}
+
+// ---------------------------------------------------------------- Radon
+// cos/sin of (theta*M_PI)/180 for theta = 0, 45, 90, 135, from the host libm
+// (radon.cpp:51-55), so the sub-pixel bin split matches the CPU arithmetic.
+__constant__ double c_radon_cs[8];
+void set_radon_table(const double *cs8) { cudaMemcpyToSymbol(c_radon_cs, cs8, 8 * sizeof(double)); }
+
+// ImageMatrix::RadonTransform2D + radon (MATLAB algorithm: 2x2 sub-pixels,
+// linear split between two bins) + vd_RadonTextures, src/cmatrix.cpp:1463-1514,
+// src/transforms/radon.cpp:14-115.  One CTA per (plane, angle); projections in
+// shared memory, then a 3-bin histogram per angle.
+__global__ void k_radon(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                        double *__restrict__ feat, double *__restrict__ proj_ws, int rsize_max) {
+    extern __shared__ double pr[];
+    __shared__ double sh[32];
+    const FJob J = jobs[blockIdx.y];
+    const Plane P = planes[J.plane];
+    const int W = P.w, H = P.h, ang = blockIdx.x;
+    const int rLast = (int)ceil(sqrt(pow((double)(W - 1 - (W - 1) / 2), 2) + pow((double)(H - 1 - (H - 1) / 2), 2))) + 1;
+    const int rFirst = -rLast, rSize = rLast - rFirst + 1;
+    const int xo = (W - 1) / 2, yo = (H - 1) / 2;
+    for (int i = threadIdx.x; i < rSize; i += blockDim.x) pr[i] = 0.0;
+    __syncthreads();
+    const double cs = c_radon_cs[2 * ang], sn = c_radon_cs[2 * ang + 1];
+    const double *p = arena + P.off;
+    const long long nsub = 4LL * W * H;
+    for (long long q = threadIdx.x; q < nsub; q += blockDim.x) {
+        const int nn = (int)(q / (2 * H)), mm = (int)(q - (long long)nn * 2 * H);
+        double pix = p[(long long)(mm / 2) * W + nn / 2];
+        if (pix != 0.0) {
+            pix *= 0.25;
+            const double xT = -xo - 0.25 + 0.5 * nn;                 // exact: multiples of 0.25
+            const double yT = -yo - 0.25 + 0.5 * (2 * H - 1 - mm);   // exact
+            const double xc = __dsub_rn(__dmul_rn(xT, cs), (double)rFirst);
+            const double ri = __dadd_rn(xc, __dmul_rn(yT, sn));
+            int rl = (int)ri;
+            const double pl = __dmul_rn(pix, __dadd_rn(__dsub_rn(1.0, ri), (double)rl));
+            atomicAdd(&pr[rl], pl);
+            atomicAdd(&pr[rl + 1], __dsub_rn(pix, pl));
+        }
+    }
+    __syncthreads();
+    double lo = 10E200, hi = -10E200;
+    for (int i = threadIdx.x; i < rSize; i += blockDim.x) {
+        lo = fmin(lo, pr[i]);
+        hi = fmax(hi, pr[i]);
+    }
+    lo = block_min(lo, sh);
+    hi = block_max(hi, sh);
+    __shared__ unsigned int bins[3];
+    if (threadIdx.x < 3) bins[threadIdx.x] = 0;
+    __syncthreads();
+    const double sc = hist_scale(lo, hi, 3);
+    for (int i = threadIdx.x; i < rSize; i += blockDim.x) atomicAdd(&bins[hist_bin(pr[i], lo, sc, 3)], 1u);
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        // raw index ang*3 + b, permuted by vd_RadonTextures: out = [0 1 2 9 10 11 3 4 5 6 7 8]
+        const int raw = ang * 3 + threadIdx.x;
+        const int dst = raw < 3 ? raw : (raw >= 9 ? raw - 6 : raw + 3);
+        feat[J.out + dst] = (double)bins[threadIdx.x];
+    }
+}
+
+void launch_radon(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw, int maxh,
+                  double *feat) {
+    if (njobs <= 0) return;
+    int rLast = (int)ceil(sqrt(pow((double)(maxw - 1 - (maxw - 1) / 2), 2) + pow((double)(maxh - 1 - (maxh - 1) / 2), 2))) + 1;
+    int rsize = 2 * rLast + 1;
+    WC_LAUNCH(c);
+    k_radon<<<dim3(4, njobs), 1024, rsize * sizeof(double), c.st>>>(arena, planes, jobs, feat, nullptr, rsize);
+}
+
+// ---------------------------------------------------------------- Chebyshev coefficients
+// ImageMatrix::ChebyshevStatistics2D (N = min(20, W, H), 32 bins),
+// src/cmatrix.cpp:1274-1281, with Chebyshev2D (src/transforms/chebyshev.cpp:118-165):
+// C[j][k] = sum_y B_k(y) * sum_x I(y,x) A_j(x), then a 32-bin histogram of the
+// N*N coefficients.  A/B tables (T_j(x)/W scaled, halved) come from the host.
+__global__ void k_chebcoef(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                           const double *__restrict__ tabs, const long long *__restrict__ tab_off,
+                           double *__restrict__ mid_ws, const long long *__restrict__ mid_off, double *__restrict__ feat) {
+    __shared__ double C[400];
+    __shared__ double sh[32];
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const int W = P.w, H = P.h;
+    int N = 20;
+    if (N > min(W, H)) N = min(W, H);
+    const double *TA = tabs + tab_off[2 * blockIdx.x], *TB = tabs + tab_off[2 * blockIdx.x + 1];
+    const double *p = arena + P.off;
+    double *mid = mid_ws + mid_off[blockIdx.x];  // H x N
+    for (int q = threadIdx.x; q < H * N; q += blockDim.x) {
+        const int y = q / N, j = q - y * N;
+        const double *row = p + (long long)y * W;
+        double s = 0;
+        for (int x = 0; x < W; x++) s = __dadd_rn(s, __dmul_rn(row[x], TA[(long long)x * N + j]));
+        mid[q] = s;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        const int j = q / N, k = q - j * N;
+        double s = 0;
+        for (int y = 0; y < H; y++) s = __dadd_rn(s, __dmul_rn(mid[(long long)y * N + j], TB[(long long)y * N + k]));
+        C[q] = s;
+    }
+    __syncthreads();
+    double lo = DBL_MAX, hi = -DBL_MAX;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        lo = fmin(lo, C[q]);
+        hi = fmax(hi, C[q]);
+    }
+    lo = block_min(lo, sh);
+    hi = block_max(hi, sh);
+    __shared__ unsigned int bins[32];
+    if (threadIdx.x < 32) bins[threadIdx.x] = 0;
+    __syncthreads();
+    const double sc = hist_scale(lo, hi, 32);
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) atomicAdd(&bins[hist_bin(C[q], lo, sc, 32)], 1u);
+    __syncthreads();
+    if (threadIdx.x < 32) feat[J.out + threadIdx.x] = (double)bins[threadIdx.x];
+}
+
+void launch_chebcoef(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, const double *tabs,
+                     const long long *tab_off, double *mid_ws, const long long *mid_off, double *feat) {
+    if (njobs <= 0) return;
+    WC_LAUNCH(c);
+    k_chebcoef<<<njobs, 512, 0, c.st>>>(arena, planes, jobs, tabs, tab_off, mid_ws, mid_off, feat);
+}
+
+}  // namespace wc

@@ -1,0 +1,98 @@
+// Chebyshev transform node: ImageMatrix::ChebyshevTransform(N = min(W,H))
+// with Chebyshev2D (src/cmatrix.cpp:1203-1222, src/transforms/chebyshev.cpp:118-165):
+//   Mid[y][j] = sum_x I[y][x] * TA[x][j]      (H x N, TA = T_j(x_x) * w_j / 2)
+//   Out[j][k] = sum_y Mid[y][j] * TB[y][k]    (N x N), output pixel (y=j, x=k).
+// Both products are FP64 register-tiled GEMMs whose threads accumulate every
+// output over k in ascending order with separate multiply and add, which is
+// the reference's order of operations (getChCoeff1D, chebyshev.cpp:82-102), so
+// on identical input the result is bit-identical to the CPU.
+#include "kcommon.cuh"
+#include "kernels.h"
+
+namespace wc {
+
+#define GT_M 64
+#define GT_N 64
+#define GT_K 16
+
+// C[i][j] = sum_k A(i,k) B(k,j); A(i,k) = A[i*sai + k*sak], B(k,j) = B[k*ldb + j],
+// C[i*ldc + j].  One CTA per 64x64 tile, 256 threads, 4x4 outputs each.
+__device__ void gemm_tile(const double *__restrict__ A, long long sai, long long sak, const double *__restrict__ B,
+                          long long ldb, double *__restrict__ C, long long ldc, int M, int N, int K, int ti, int tj) {
+    __shared__ double As[GT_K][GT_M + 1];
+    __shared__ double Bs[GT_K][GT_N + 1];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int i0 = ti * GT_M, j0 = tj * GT_N;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
+    for (int k0 = 0; k0 < K; k0 += GT_K) {
+        for (int q = threadIdx.x; q < GT_K * GT_M; q += blockDim.x) {
+            int kk = q / GT_M, ii = q - kk * GT_M;
+            int i = i0 + ii, k = k0 + kk;
+            As[kk][ii] = (i < M && k < K) ? A[(long long)i * sai + (long long)k * sak] : 0.0;
+        }
+        for (int q = threadIdx.x; q < GT_K * GT_N; q += blockDim.x) {
+            int kk = q / GT_N, jj = q - kk * GT_N;
+            int j = j0 + jj, k = k0 + kk;
+            Bs[kk][jj] = (j < N && k < K) ? B[(long long)k * ldb + j] : 0.0;
+        }
+        __syncthreads();
+        const int kend = min(GT_K, K - k0);
+        for (int kk = 0; kk < kend; kk++) {
+            double a[4], b[4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) a[r] = As[kk][ty + 16 * r];
+#pragma unroll
+            for (int s = 0; s < 4; s++) b[s] = Bs[kk][tx + 16 * s];
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int s = 0; s < 4; s++) acc[r][s] = __dadd_rn(acc[r][s], __dmul_rn(a[r], b[s]));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            int i = i0 + ty + 16 * r, j = j0 + tx + 16 * s;
+            if (i < M && j < N) C[(long long)i * ldc + j] = acc[r][s];
+        }
+}
+
+// stage 0: Mid = I * TA ; stage 1: Out = Mid^T * TB
+__global__ void __launch_bounds__(256) k_cheb_gemm(double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                   const TJob *__restrict__ jobs, const double *__restrict__ tabs,
+                                                   const long long *__restrict__ tab_off, double *__restrict__ mid,
+                                                   const long long *__restrict__ mid_off, int stage) {
+    const TJob J = jobs[blockIdx.z];
+    const Plane S = planes[J.src];
+    const int W = S.w, H = S.h, N = min(W, H);
+    double *Mid = mid + mid_off[blockIdx.z];
+    const double *TA = tabs + tab_off[2 * blockIdx.z], *TB = tabs + tab_off[2 * blockIdx.z + 1];
+    if (stage == 0) {
+        if (blockIdx.x * GT_N >= N || blockIdx.y * GT_M >= H) return;
+        gemm_tile(arena + S.off, W, 1, TA, N, Mid, N, H, N, W, blockIdx.y, blockIdx.x);
+    } else {
+        const Plane D = planes[J.dst];
+        if (blockIdx.x * GT_N >= N || blockIdx.y * GT_M >= N) return;
+        gemm_tile(Mid, 1, N, TB, N, arena + D.off, N, N, N, H, blockIdx.y, blockIdx.x);
+    }
+}
+
+void launch_chebyshev(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
+                      const double *tabs, const long long *tab_off, double *mid, const long long *mid_off) {
+    if (njobs <= 0) return;
+    const int N = maxw < maxh ? maxw : maxh;
+    WC_LAUNCH(c);
+    k_cheb_gemm<<<dim3((N + GT_N - 1) / GT_N, (maxh + GT_M - 1) / GT_M, njobs), 256, 0, c.st>>>(arena, planes, jobs, tabs,
+                                                                                            tab_off, mid, mid_off, 0);
+    WC_LAUNCH(c);
+    k_cheb_gemm<<<dim3((N + GT_N - 1) / GT_N, (N + GT_M - 1) / GT_M, njobs), 256, 0, c.st>>>(arena, planes, jobs, tabs,
+                                                                                         tab_off, mid, mid_off, 1);
+}
+
+}  // namespace wc

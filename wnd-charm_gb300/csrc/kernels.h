@@ -1,0 +1,45 @@
+// Host-side launchers of the CUDA kernels (one per family or transform).
+#pragma once
+#include "wc_internal.h"
+
+namespace wc {
+
+// k_basic.cu
+void launch_convert(Ctx &c, const void *src, int dtype, double *dst, long long n);
+void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int nplanes, PlaneStats *out);
+void launch_edge(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh);
+void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
+                    double *tmp, const long long *tmp_off);
+void launch_plane_sort(Ctx &c, const double *arena, const Plane *planes, const int *plane_ids, int n,
+                       unsigned long long *keys, unsigned long long *tmp, const long long *key_off,
+                       unsigned int *counts);
+void launch_pixstats(Ctx &c, const Plane *planes, const PlaneStats *stats, const FJob *jobs, int njobs,
+                     const int *sort_slot, const unsigned long long *keys, const long long *key_off, double *feat);
+void launch_gini(Ctx &c, const Plane *planes, const FJob *jobs, int njobs, const int *sort_slot,
+                 const unsigned long long *keys, const long long *key_off, double *feat);
+void launch_mshist(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
+                   int njobs, double *feat);
+void launch_fractal(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, double *feat);
+void launch_comb(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, double *feat);
+void set_radon_table(const double *cs8);
+void launch_radon(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw, int maxh,
+                  double *feat);
+void launch_chebcoef(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, const double *tabs,
+                     const long long *tab_off, double *mid_ws, const long long *mid_off, double *feat);
+
+// k_fft.cu: 1-D complex DFTs of any length <= kMaxFFT, batched, in shared memory
+const int kMaxFFT = 4096;
+struct FFTPlan {  // device description of one length
+    int n, nstages;
+    int radix[16];
+    long long tw_off;  // offset of exp(-2 pi i k / n), k < n, in the twiddle table (interleaved re, im)
+};
+void launch_fourier(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
+                    const FFTPlan *plans_d, const int *job_plan_y, const int *job_plan_x, const double *tw,
+                    double *cbuf, const long long *cbuf_off);
+
+// k_gemm.cu: the Chebyshev transform (two FP64 products with host-made tables)
+void launch_chebyshev(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
+                      const double *tabs, const long long *tab_off, double *mid, const long long *mid_off);
+
+}  // namespace wc

@@ -1,0 +1,45 @@
+// Feature-family preparation (host) and launch (device) for one batch.
+#pragma once
+#include <functional>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "wc_internal.h"
+
+namespace wc {
+
+struct FeatureSetup {
+    // inputs
+    const std::vector<Plane> *planes;
+    const std::vector<std::vector<FJob>> *fj;  // per algorithm
+    std::function<long long(const std::string &, const std::vector<double> &)> tabs_add;
+    std::function<FFTPlan(int)> fft_plan;
+    std::function<size_t(const void *, size_t)> put_copy;  // metadata blob, returns offset
+    std::function<size_t(size_t)> ws_take;                 // workspace bytes, returns offset
+    std::function<size_t(size_t)> meta_take;               // device-written metadata bytes
+    // per-family results of the preparation (offsets into meta / ws)
+    std::map<std::string, size_t> off;
+    std::map<std::string, long long> val;
+};
+
+struct FeatureRun {
+    Ctx *ctx;
+    double *arena;
+    const Plane *planes;
+    const PlaneStats *stats;
+    char *meta;
+    char *ws;
+    const double *tabs;
+    double *feat;
+};
+
+void features_init();
+int features_prepare(FeatureSetup &fs);
+int features_launch(FeatureSetup &fs, FeatureRun &fr);
+// reads and clears the device error word; *dev_err != 0 if a kernel flagged one
+int features_check(cudaStream_t st, int *dev_err);
+int set_err(int code, const char *fmt, ...);
+
+}  // namespace wc

@@ -1,0 +1,57 @@
+// Internal definitions shared by the host executor and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace wc {
+
+// Feature algorithms of the reference (src/FeatureAlgorithms.h): the 15
+// grayscale FeatureAlgorithm singletons, in this project's numbering.
+enum Alg {
+    A_CHEBFOURIER = 0, A_CHEB, A_ZERNIKE, A_HARALICK, A_MSHIST, A_TAMURA, A_COMB, A_RADON,
+    A_FRACTAL, A_PIXSTATS, A_EDGEF, A_OBJ, A_INVOBJ, A_GABOR, A_GINI, A_COUNT
+};
+// Image transforms (src/ImageTransforms.h): Fourier, Chebyshev, Wavelet, Edge.
+enum Xf { X_FOURIER = 0, X_CHEBYSHEV, X_WAVELET, X_EDGE, X_COUNT };
+
+extern const char *const kAlgName[A_COUNT];
+extern const int kAlgN[A_COUNT];
+extern const char *const kXfName[X_COUNT];
+
+// One image plane in the plane arena (row-major doubles).
+struct Plane {
+    long long off;  // element offset into the arena
+    int w, h;
+};
+
+// Per-plane statistics (ImageMatrix::stats, a Moments2): min, max, mean,
+// M2/(n-1) when n > 2 (0 otherwise), plus the plain sum.
+struct PlaneStats {
+    double mn, mx, mean, var, sum;
+    long long n;
+};
+
+// A feature job: compute one algorithm on one plane, write n values at `out`
+// (element offset into the feature matrix).
+struct FJob {
+    int plane;
+    int img;
+    long long out;
+};
+
+// A transform job: dst = T(src).
+struct TJob {
+    int src, dst;
+};
+
+// Launch context handed to every kernel launcher.
+struct Ctx {
+    cudaStream_t st;
+    long long *launches;  // incremented per kernel launch
+    int prec;             // WC_PREC_FP64 or WC_PREC_MIXED
+    int sms;              // multiprocessors on the device
+};
+
+}  // namespace wc

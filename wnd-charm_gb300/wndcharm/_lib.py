@@ -1,0 +1,68 @@
+"""ctypes binding of libwndcharm_gb300.so (the C ABI in include/wndcharm_gb300.h).
+
+The library is built in-tree by wnd-charm_gb300/build.py.  Loading fails loudly
+when it is missing: there is no CPU fallback behind this package.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(HERE, "build", "libwndcharm_gb300.so")
+
+WC_OK = 0
+WC_PLAN_SHORT, WC_PLAN_LONG = 0, 1
+WC_U8, WC_U16, WC_F32, WC_F64 = 0, 1, 2, 3
+WC_PREC_FP64, WC_PREC_MIXED = 0, 1
+
+D = ctypes.POINTER(ctypes.c_double)
+I = ctypes.POINTER(ctypes.c_int)
+
+
+class wc_image_desc(ctypes.Structure):
+    _fields_ = [("pixels", ctypes.c_void_p), ("dtype", ctypes.c_int), ("width", ctypes.c_int),
+                ("height", ctypes.c_int), ("bits", ctypes.c_int), ("on_device", ctypes.c_int)]
+
+
+class WndcharmError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise WndcharmError("CUDA library not built: %s (run wnd-charm_gb300/build.py)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        L.wc_last_error.restype = ctypes.c_char_p
+        L.wc_version.restype = ctypes.c_char_p
+        L.wc_plan_get.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+        L.wc_plan_from_names.argtypes = [ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.POINTER(vp)]
+        L.wc_plan_free.argtypes = [vp]
+        L.wc_plan_free.restype = None
+        L.wc_plan_n_features.argtypes = [vp]
+        L.wc_plan_feature_name.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+        L.wc_plan_n_groups.argtypes = [vp]
+        L.wc_plan_group.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, I, I]
+        L.wc_engine_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.wc_engine_destroy.argtypes = [vp]
+        L.wc_engine_destroy.restype = None
+        L.wc_engine_set_stream.argtypes = [vp, vp]
+        L.wc_engine_launch_count.argtypes = [vp]
+        L.wc_engine_launch_count.restype = ctypes.c_longlong
+        L.wc_extract.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
+        L.wc_extract_batch.argtypes = [vp, vp, ctypes.POINTER(wc_image_desc), ctypes.c_int, vp, ctypes.c_int]
+        L.wc_transform.argtypes = [vp, ctypes.c_char_p, D, ctypes.c_int, ctypes.c_int, D, ctypes.c_longlong, I, I]
+        L.wc_wnd_fit.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D, D, D]
+        L.wc_wnd_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D, I]
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc < 0:
+        raise WndcharmError(lib().wc_last_error().decode(errors="replace"))
+    return rc

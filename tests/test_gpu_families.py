@@ -13,7 +13,8 @@ GROUP_C = ["Comb Moments", "Haralick Textures", "Multiscale Histograms", "Tamura
            "Fractal Features", "Pixel Intensity Statistics", "Gini Coefficient"]
 GROUP_B = ["Chebyshev-Fourier Coefficients", "Chebyshev Coefficients", "Zernike Coefficients"]
 GROUP_A = ["Edge Features", "Otsu Object Features", "Inverse-Otsu Object Features", "Gabor Textures"]
-READY = {"Comb Moments", "Multiscale Histograms", "Radon Coefficients", "Fractal Features",
+READY = {"Comb Moments", "Multiscale Histograms", "Radon Coefficients", "Fractal Features", "Zernike Coefficients",
+         "Chebyshev-Fourier Coefficients",
          "Pixel Intensity Statistics", "Gini Coefficient", "Chebyshev Coefficients"}
 
 

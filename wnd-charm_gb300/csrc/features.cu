@@ -15,7 +15,15 @@ __device__ int g_dev_err = 0;
 
 std::vector<double> cheb_table(int len, int N);
 
-void features_init() {}
+void features_init() { set_zernike_tables(); }
+
+// positions of the reference's Downsample loop (x starts at 0, x += dx while
+// x < old): src/cmatrix.cpp:602-606
+static std::vector<double> ds_positions(int old, double dx) {
+    std::vector<double> v;
+    for (double x = 0; x < old; x += dx) v.push_back(x);
+    return v;
+}
 
 int features_check(cudaStream_t st, int *dev_err) {
     int v = 0;
@@ -93,6 +101,60 @@ int features_prepare(FeatureSetup &fs) {
         fs.off["cc_moff"] = fs.put_copy(moff.data(), moff.size() * sizeof(long long));
         fs.off["cc_mid"] = fs.ws_take(tot * sizeof(double));
     }
+    // Zernike: per-job centroid moments and per-chunk partials
+    if (!fj[A_ZERNIKE].empty()) {
+        long long maxpix = 0;
+        for (auto &j : fj[A_ZERNIKE]) maxpix = std::max(maxpix, (long long)P[j.plane].w * P[j.plane].h);
+        const long long nchunk = (maxpix + 2047) / 2048;
+        fs.val["zk_maxpix"] = maxpix;
+        fs.off["zk_mom"] = fs.ws_take(fj[A_ZERNIKE].size() * 3 * sizeof(double));
+        fs.off["zk_part"] = fs.ws_take(fj[A_ZERNIKE].size() * 2 * nchunk * 72 * sizeof(double));
+    }
+
+    // Chebyshev-Fourier: source image (downsampled above 300*300), chunk partials
+    if (!fj[A_CHEBFOURIER].empty()) {
+        std::vector<CFJob> cj;
+        int max_cnt_x = 0, max_w = 0, max_h = 0, nchunk_max = 1;
+        for (auto &j : fj[A_CHEBFOURIER]) {
+            const Plane &Q = P[j.plane];
+            CFJob c;
+            memset(&c, 0, sizeof c);
+            if ((long)Q.w * Q.h > 300L * 300) {
+                double r = std::min(300.0 / (double)Q.w, 300.0 / (double)Q.h);
+                double xr = r > 1 ? 1 : r, yr = r > 1 ? 1 : r;
+                c.dx = 1 / xr;
+                c.down = 1;
+                c.new_w = (unsigned)(xr * Q.w);
+                c.new_h = (unsigned)(yr * Q.h);
+                std::vector<double> xs = ds_positions(Q.w, c.dx), ys = ds_positions(Q.h, 1 / yr);
+                c.cnt_x = (int)xs.size();
+                c.cnt_y = (int)ys.size();
+                char key[96];
+                snprintf(key, sizeof key, "ds%d_%.17g", Q.w, c.dx);
+                c.xs_tab = fs.tabs_add(key, xs);
+                snprintf(key, sizeof key, "ds%d_%.17g", Q.h, 1 / yr);
+                c.ys_tab = fs.tabs_add(key, ys);
+                c.tmp_ws = (long long)(fs.ws_take((size_t)Q.h * c.cnt_x * sizeof(double)) / sizeof(double));
+            } else {
+                c.new_w = Q.w;
+                c.new_h = Q.h;
+                c.dx = 1;
+            }
+            c.src_ws = (long long)(fs.ws_take((size_t)c.new_w * c.new_h * sizeof(double)) / sizeof(double));
+            c.nchunk = (int)(((long long)c.new_w * c.new_h + 1023) / 1024);
+            nchunk_max = std::max(nchunk_max, c.nchunk);
+            max_cnt_x = std::max(max_cnt_x, c.cnt_x);
+            max_w = std::max(max_w, c.new_w);
+            max_h = std::max(max_h, c.new_h);
+            cj.push_back(c);
+        }
+        fs.off["cf_jobs"] = fs.put_copy(cj.data(), cj.size() * sizeof(CFJob));
+        fs.off["cf_part"] = fs.ws_take(cj.size() * (size_t)nchunk_max * 2 * 529 * sizeof(double));
+        fs.val["cf_nchunk"] = nchunk_max;
+        fs.val["cf_cntx"] = max_cnt_x;
+        fs.val["cf_w"] = max_w;
+        fs.val["cf_h"] = max_h;
+    }
     return WC_OK;
 }
 
@@ -128,6 +190,14 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
         launch_chebcoef(c, fr.arena, fr.planes, jobs(A_CHEB), nj(A_CHEB), fr.tabs,
                         (const long long *)(fr.meta + fs.off["cc_tab"]), (double *)(fr.ws + fs.off["cc_mid"]),
                         (const long long *)(fr.meta + fs.off["cc_moff"]), fr.feat);
+    if (nj(A_ZERNIKE))
+        launch_zernike(c, fr.arena, fr.planes, jobs(A_ZERNIKE), nj(A_ZERNIKE), fs.val["zk_maxpix"],
+                       (double *)(fr.ws + fs.off["zk_mom"]), (double *)(fr.ws + fs.off["zk_part"]), fr.feat);
+    if (nj(A_CHEBFOURIER))
+        launch_chebfourier(c, fr.arena, fr.planes, jobs(A_CHEBFOURIER), nj(A_CHEBFOURIER),
+                           maxw_of(P, fj[A_CHEBFOURIER]), maxh_of(P, fj[A_CHEBFOURIER]), (int)fs.val["cf_cntx"],
+                           (int)fs.val["cf_w"], (int)fs.val["cf_h"], (const CFJob *)(fr.meta + fs.off["cf_jobs"]), fr.tabs,
+                           (double *)fr.ws, (double *)(fr.ws + fs.off["cf_part"]), (int)fs.val["cf_nchunk"], fr.feat);
     return WC_OK;
 }
 

@@ -290,7 +290,7 @@ __global__ void k_pixstats(const Plane *__restrict__ planes, const PlaneStats *_
     o[4] = S.mx;
 }
 
-__global__ void k_gini(const Plane *__restrict__ planes, const FJob *__restrict__ jobs, const int *__restrict__ sort_slot,
+__global__ void __launch_bounds__(512) k_gini(const Plane *__restrict__ planes, const FJob *__restrict__ jobs, const int *__restrict__ sort_slot,
                        const unsigned long long *__restrict__ keys, const long long *__restrict__ key_off,
                        double *__restrict__ feat) {
     __shared__ double sh[32];
@@ -335,7 +335,7 @@ void launch_gini(Ctx &c, const Plane *planes, const FJob *jobs, int njobs, const
 
 // ---------------------------------------------------------------- multiscale histograms
 // ImageMatrix::MultiScaleHistogram, src/cmatrix.cpp:1743-1756.
-__global__ void k_mshist(const double *__restrict__ arena, const Plane *__restrict__ planes,
+__global__ void __launch_bounds__(512) k_mshist(const double *__restrict__ arena, const Plane *__restrict__ planes,
                          const PlaneStats *__restrict__ stats, const FJob *__restrict__ jobs, double *__restrict__ feat) {
     __shared__ unsigned int h[24];
     const FJob J = jobs[blockIdx.x];
@@ -366,13 +366,13 @@ void launch_mshist(Ctx &c, const double *arena, const Plane *planes, const Plane
                    int njobs, double *feat) {
     if (njobs <= 0) return;
     WC_LAUNCH(c);
-    k_mshist<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, jobs, feat);
+    k_mshist<<<njobs, 512, 0, c.st>>>(arena, planes, stats, jobs, feat);
 }
 
 // ---------------------------------------------------------------- fractal
 // FractalFeatures::execute, src/FeatureAlgorithms.cpp:232-267: for the k-th
 // lag (k = 1 + slot*step, k < K), mean absolute difference along y and x.
-__global__ void k_fractal(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+__global__ void __launch_bounds__(512) k_fractal(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                           double *__restrict__ feat) {
     __shared__ double sh[32];
     const FJob J = jobs[blockIdx.y];
@@ -419,7 +419,7 @@ __device__ __forceinline__ bool comb_pixel(int dir, long long j, long long ii, l
     y = m2 - 1 - ii; x = j; return y >= 0 && y < m;
 }
 
-__global__ void k_comb(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+__global__ void __launch_bounds__(512) k_comb(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                        double *__restrict__ feat) {
     __shared__ double M[4][4][20];  // dir, moment, sample
     __shared__ int nsamp;
@@ -522,7 +522,7 @@ void set_radon_table(const double *cs8) { cudaMemcpyToSymbol(c_radon_cs, cs8, 8 
 // linear split between two bins) + vd_RadonTextures, src/cmatrix.cpp:1463-1514,
 // src/transforms/radon.cpp:14-115.  One CTA per (plane, angle); projections in
 // shared memory, then a 3-bin histogram per angle.
-__global__ void k_radon(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+__global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                         double *__restrict__ feat, double *__restrict__ proj_ws, int rsize_max) {
     extern __shared__ double pr[];
     __shared__ double sh[32];
@@ -588,7 +588,7 @@ void launch_radon(Ctx &c, const double *arena, const Plane *planes, const FJob *
 // src/cmatrix.cpp:1274-1281, with Chebyshev2D (src/transforms/chebyshev.cpp:118-165):
 // C[j][k] = sum_y B_k(y) * sum_x I(y,x) A_j(x), then a 32-bin histogram of the
 // N*N coefficients.  A/B tables (T_j(x)/W scaled, halved) come from the host.
-__global__ void k_chebcoef(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+__global__ void __launch_bounds__(512) k_chebcoef(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                            const double *__restrict__ tabs, const long long *__restrict__ tab_off,
                            double *__restrict__ mid_ws, const long long *__restrict__ mid_off, double *__restrict__ feat) {
     __shared__ double C[400];

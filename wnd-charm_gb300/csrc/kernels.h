@@ -42,4 +42,21 @@ void launch_fourier(Ctx &c, double *arena, const Plane *planes, const TJob *jobs
 void launch_chebyshev(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
                       const double *tabs, const long long *tab_off, double *mid, const long long *mid_off);
 
+// k_groupb.cu: Zernike and Chebyshev-Fourier coefficients
+void set_zernike_tables();
+void launch_zernike(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, long long maxpix,
+                    double *mom, double *part, double *feat);
+struct CFJob {
+    long long src_ws;          // offset (doubles) of the m x n source image in the workspace
+    long long tmp_ws;          // offset of the x-pass buffer (old_h x cnt_x)
+    long long xs_tab, ys_tab;  // position tables (doubles) in the table buffer
+    int cnt_x, cnt_y, new_w, new_h;
+    int down;  // 1 if downsampled
+    int nchunk;
+    double dx;
+};
+void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw,
+                        int maxh, int max_cnt_x, int max_src_w, int max_src_h, const CFJob *cj, const double *tabs,
+                        double *ws, double *part, int nchunk_max, double *feat);
+
 }  // namespace wc

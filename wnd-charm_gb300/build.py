@@ -17,6 +17,9 @@ OUT = os.path.join(HERE, "build")
 LIB = os.path.join(OUT, "libwndcharm_gb300.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# files whose arithmetic restates a CPU order of operations bit for bit: no
+# multiply-add contraction anywhere in them
+EXTRA = {"k_haralick.cu": ["-fmad=false"]}
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + CSRC, "-I" + os.path.join(os.path.dirname(HERE), "include")]
 
@@ -34,7 +37,7 @@ def _compile(src, force):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     if not force and not _deps_newer(src, obj):
         return obj, None
-    cmd = [NVCC] + ARCH + FLAGS + ["-c", src, "-o", obj]
+    cmd = [NVCC] + ARCH + FLAGS + EXTRA.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
         return obj, p.stdout + p.stderr

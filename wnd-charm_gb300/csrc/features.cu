@@ -155,6 +155,40 @@ int features_prepare(FeatureSetup &fs) {
         fs.val["cf_w"] = max_w;
         fs.val["cf_h"] = max_h;
     }
+    // Tamura: normalised plane, running sums, best scale, phi; partials
+    if (!fj[A_TAMURA].empty()) {
+        std::vector<TamJob> tj;
+        long long maxpix = 0;
+        for (auto &j : fj[A_TAMURA]) {
+            const size_t n = (size_t)P[j.plane].w * P[j.plane].h;
+            maxpix = std::max(maxpix, (long long)n);
+            TamJob t;
+            t.norm_ws = (long long)(fs.ws_take(n * 8) / 8);
+            t.sum_ws = (long long)(fs.ws_take(n * 8) / 8);
+            t.sbest_ws = (long long)(fs.ws_take(n) / 8);
+            t.phi_ws = (long long)(fs.ws_take(n * 8) / 8);
+            tj.push_back(t);
+        }
+        fs.off["tam_jobs"] = fs.put_copy(tj.data(), tj.size() * sizeof(TamJob));
+        fs.off["tam_part"] = fs.ws_take(tj.size() * (size_t)((maxpix + 1023) / 1024) * 6 * 8);
+        fs.val["tam_maxpix"] = maxpix;
+    }
+
+    // Haralick: gray image, LUT, 4 matrices, 4 Q matrices, 4 x 14 results per job
+    if (!fj[A_HARALICK].empty()) {
+        std::vector<HarJob> hj;
+        for (auto &j : fj[A_HARALICK]) {
+            const size_t n = (size_t)P[j.plane].w * P[j.plane].h;
+            HarJob h;
+            h.gray_b = (long long)fs.ws_take(n);
+            h.lut_b = (long long)fs.ws_take(257 * 4);
+            h.glcm_b = (long long)fs.ws_take(4 * 256 * 256 * 8);
+            h.q_b = (long long)fs.ws_take(4 * 256 * 256 * 8);
+            h.res_b = (long long)fs.ws_take(4 * 14 * 8);
+            hj.push_back(h);
+        }
+        fs.off["har_jobs"] = fs.put_copy(hj.data(), hj.size() * sizeof(HarJob));
+    }
     return WC_OK;
 }
 
@@ -198,6 +232,13 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                            maxw_of(P, fj[A_CHEBFOURIER]), maxh_of(P, fj[A_CHEBFOURIER]), (int)fs.val["cf_cntx"],
                            (int)fs.val["cf_w"], (int)fs.val["cf_h"], (const CFJob *)(fr.meta + fs.off["cf_jobs"]), fr.tabs,
                            (double *)fr.ws, (double *)(fr.ws + fs.off["cf_part"]), (int)fs.val["cf_nchunk"], fr.feat);
+    if (nj(A_TAMURA))
+        launch_tamura(c, fr.planes, fr.stats, fr.arena, jobs(A_TAMURA), nj(A_TAMURA),
+                      (const TamJob *)(fr.meta + fs.off["tam_jobs"]), (double *)fr.ws,
+                      (double *)(fr.ws + fs.off["tam_part"]), fs.val["tam_maxpix"], fr.feat);
+    if (nj(A_HARALICK))
+        launch_haralick(c, fr.arena, fr.planes, fr.stats, jobs(A_HARALICK), nj(A_HARALICK),
+                        (const HarJob *)(fr.meta + fs.off["har_jobs"]), fr.ws, fr.feat);
     return WC_OK;
 }
 

@@ -87,8 +87,8 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
         const long long c1 = min(npix, c0 + ZCHUNK);
         for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
             const long long yy = i / P.w, xx = i - yy * P.w;
-            const double x = (xx + 1 - cx) / rad, y = (yy + 1 - cy) / rad;
-            const double r2 = x * x + y * y, r = sqrt(r2);
+            const double x = __dsub_rn((double)(xx + 1), cx) / rad, y = __dsub_rn((double)(yy + 1), cy) / rad;
+            const double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), r = sqrt(r2);
             if (r < DBL_EPSILON || r > 1.0) continue;
             double R[16], CO[16], SI[16];
             R[0] = 1;
@@ -254,11 +254,12 @@ __global__ void __launch_bounds__(256) k_cf_accum(const CFJob *__restrict__ cj, 
             double Ival = 0;
             if (ind < npix && ind < c0 + CF_CHUNK) {
                 const long long x = ind / m, y = ind - x * m;
-                const double xi = -1.0 + (double)x * tn, yi = -1.0 + (double)y * tm;
-                const double r = sqrt(xi * xi + yi * yi);
+                // exact reference rounding (no contraction): decides r < 1 on the circle
+                const double xi = __dadd_rn(-1.0, __dmul_rn((double)x, tn)), yi = __dadd_rn(-1.0, __dmul_rn((double)y, tm));
+                const double r = sqrt(__dadd_rn(__dmul_rn(xi, xi), __dmul_rn(yi, yi)));
                 if (r < 1) {
                     Ival = img[y * n + x];
-                    double xx = r * 2 - 1;
+                    double xx = __dsub_rn(__dmul_rn(r, 2.0), 1.0);
                     if (xx < -1) xx = -1;
                     if (xx > 1) xx = 1;
                     const double ac = acos(xx);

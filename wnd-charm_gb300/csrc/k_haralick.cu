@@ -1,0 +1,574 @@
+// Haralick textures (FP64 form): haralick2D + Extract_Texture_Features,
+// src/textures/haralick/haralick.cpp:12-144, src/textures/haralick/CVIPtexture.cpp:384-1108.
+//   * gray = (unsigned char)((p - min) * 255 / (max - min));
+//   * tone LUT over the tones present (tone 0 included), Ng tones;
+//   * per angle (0, 45, 90, 135) a symmetric co-occurrence matrix at distance 1
+//     over pairs whose two pixels are both nonzero, divided by the pair count;
+//   * f1..f13 from the matrix; f14 = sqrt(Re lambda_2) of Q in the order of
+//     the real Schur form (0 if lambda_2 is complex, or Ng < 3);
+//   * (mean, range) over the 4 angles, permuted into the reference's order.
+// Counts are integers, so the matrices are bit-identical to the CPU's for the
+// same gray image.  The eigen-solver is the same algorithm, loop orders and
+// rounding (no contraction) as the oracle's restatement of Eigen 3.1.2.
+#include <cfloat>
+#include <cmath>
+
+#include "kcommon.cuh"
+#include "kernels.h"
+
+namespace wc {
+
+// one CTA per job: gray image, tone LUT, Ng
+__global__ void __launch_bounds__(1024) k_har_quant(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                    const PlaneStats *__restrict__ stats, const FJob *__restrict__ jobs,
+                                                    const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    __shared__ int flag[256];
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const PlaneStats S = stats[J.plane];
+    const HarJob H = hj[blockIdx.x];
+    unsigned char *g = (unsigned char *)(wsb + H.gray_b);
+    int *lut = (int *)(wsb + H.lut_b);
+    if (threadIdx.x < 256) flag[threadIdx.x] = 0;
+    __syncthreads();
+    const double sc = 255.0 / (S.mx - S.mn);
+    const double *p = arena + P.off;
+    for (long long i = threadIdx.x; i < (long long)P.w * P.h; i += blockDim.x) {
+        const double q = (p[i] - S.mn) * sc;
+        unsigned char v = 0;
+        if (q >= 0 && q < 256) v = (unsigned char)q;  // constant plane (0/0): tone 0
+        g[i] = v;
+        flag[v] = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ng = 0;
+        for (int t = 0; t < 256; t++) lut[t] = flag[t] ? ng++ : -1;
+        lut[256] = ng;
+    }
+}
+
+// one CTA per (job, angle): symmetric GLCM in shared memory (upper triangle),
+// written out normalised as a full Ng x Ng matrix.
+__global__ void __launch_bounds__(1024) k_har_glcm(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                                                   const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    extern __shared__ unsigned int tri[];  // 256*257/2
+    __shared__ int lut_s[257];
+    __shared__ unsigned long long cnt_s;
+    const int ang = blockIdx.y;
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const HarJob H = hj[blockIdx.x];
+    const unsigned char *g = (const unsigned char *)(wsb + H.gray_b);
+    const int *lut = (const int *)(wsb + H.lut_b);
+    for (int t = threadIdx.x; t < 257; t += blockDim.x) lut_s[t] = lut[t];
+    for (int t = threadIdx.x; t < 256 * 257 / 2; t += blockDim.x) tri[t] = 0;
+    if (threadIdx.x == 0) cnt_s = 0;
+    __syncthreads();
+    const int Ng = lut_s[256];
+    const int dr = ang == 0 ? 0 : 1, dc = ang == 0 ? 1 : (ang == 1 ? -1 : (ang == 2 ? 0 : 1));
+    const int rows = P.h, cols = P.w;
+    unsigned long long cnt = 0;
+    for (long long i = threadIdx.x; i < (long long)rows * cols; i += blockDim.x) {
+        const int r = (int)(i / cols), c = (int)(i - (long long)r * cols);
+        const unsigned char a = g[i];
+        if (a == 0) continue;
+        const int r2 = r + dr, c2 = c + dc;
+        if (r2 >= rows || c2 < 0 || c2 >= cols) continue;
+        const unsigned char b = g[(long long)r2 * cols + c2];
+        if (!b) continue;
+        int x = lut_s[a], y = lut_s[b];
+        if (x > y) { int t = x; x = y; y = t; }
+        atomicAdd(&tri[x * 256 - x * (x - 1) / 2 + (y - x)], 1u);
+        cnt += 2;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&cnt_s, cnt);
+    __syncthreads();
+    const double count = (double)cnt_s;
+    double *Pm = (double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256;
+    for (long long q = threadIdx.x; q < (long long)Ng * Ng; q += blockDim.x) {
+        const int i = (int)(q / Ng), j = (int)(q - (long long)i * Ng);
+        const int x = min(i, j), y = max(i, j);
+        double c = (double)tri[x * 256 - x * (x - 1) / 2 + (y - x)];
+        if (i == j) c *= 2;
+        Pm[q] = (cnt_s == 0) ? 0.0 : c / count;
+    }
+}
+
+// f1..f13 for one (job, angle); marginals summed sequentially per entry.
+__global__ void __launch_bounds__(256) k_har_stats(const FJob *__restrict__ jobs, const HarJob *__restrict__ hj,
+                                                   char *__restrict__ wsb) {
+    __shared__ double px[256], py[256], pxpy[512], pxmy[256];
+    __shared__ double sh[32];
+    const int ang = blockIdx.y;
+    const HarJob H = hj[blockIdx.x];
+    const int Ng = ((const int *)(wsb + H.lut_b))[256];
+    const double *P = (const double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256;
+    double *res = (double *)(wsb + H.res_b) + ang * 14;
+    const double EPS = 0.000000001, l2 = log10(2.0);
+    for (int i = threadIdx.x; i < Ng; i += blockDim.x) {
+        double s = 0, t = 0;
+        for (int j = 0; j < Ng; j++) {
+            s += P[(long long)i * Ng + j];
+            t += P[(long long)j * Ng + i];
+        }
+        px[i] = s;
+        py[i] = t;
+    }
+    for (int k = threadIdx.x; k <= 2 * Ng - 2; k += blockDim.x) {
+        double s = 0;
+        for (int i = max(0, k - Ng + 1); i <= min(k, Ng - 1); i++) s += P[(long long)i * Ng + (k - i)];
+        pxpy[k] = s;
+    }
+    for (int k = threadIdx.x; k < Ng; k += blockDim.x) {
+        double s = 0;
+        for (int i = 0; i < Ng; i++) {
+            if (i + k < Ng) s += P[(long long)i * Ng + i + k];
+            if (k > 0 && i - k >= 0) s += P[(long long)i * Ng + i - k];
+        }
+        pxmy[k] = s;
+    }
+    __syncthreads();
+    double f1 = 0, tmp3 = 0, mean4 = 0, f5 = 0, e9 = 0, hxy1 = 0, hxy2 = 0;
+    for (long long q = threadIdx.x; q < (long long)Ng * Ng; q += blockDim.x) {
+        const int i = (int)(q / Ng), j = (int)(q - (long long)i * Ng);
+        const double p = P[q];
+        f1 += p * p;
+        tmp3 += i * j * p;
+        mean4 += i * p;
+        f5 += p / (1 + (i - j) * (i - j));
+        e9 += p * log10(p + EPS) / l2;
+        const double pp = px[i] * py[j];
+        hxy1 -= p * log10(pp + EPS) / l2;
+        hxy2 -= pp * log10(pp + EPS) / l2;
+    }
+    f1 = block_sum(f1, sh);
+    tmp3 = block_sum(tmp3, sh);
+    mean4 = block_sum(mean4, sh);
+    f5 = block_sum(f5, sh);
+    e9 = block_sum(e9, sh);
+    hxy1 = block_sum(hxy1, sh);
+    hxy2 = block_sum(hxy2, sh);
+    double var4 = 0;
+    for (long long q = threadIdx.x; q < (long long)Ng * Ng; q += blockDim.x) {
+        const int i = (int)(q / Ng);
+        var4 += (i - mean4) * (i - mean4) * P[q];
+    }
+    var4 = block_sum(var4, sh);
+    if (threadIdx.x == 0) {
+        double f2 = 0;
+        for (int n = 0; n < Ng; n++) f2 += n * n * pxmy[n];
+        double meanx = 0, sq = 0;
+        for (int i = 0; i < Ng; i++) {
+            meanx += px[i] * i;
+            sq += px[i] * i * i;
+        }
+        const double sd = sqrt(sq - meanx * meanx);
+        const double f3 = (sd * sd == 0) ? 1 : (tmp3 - meanx * meanx) / (sd * sd);
+        double f6 = 0, sent = 0;
+        for (int k = 0; k <= 2 * Ng - 2; k++) f6 += k * pxpy[k];
+        for (int k = 0; k <= 2 * Ng - 2; k++) sent -= pxpy[k] * log10(pxpy[k] + EPS) / l2;
+        double f7 = 0;
+        for (int k = 0; k <= 2 * Ng - 2; k++) f7 += (k - sent) * (k - sent) * pxpy[k];
+        double s10 = 0, s10sq = 0, e11 = 0;
+        for (int k = 0; k < Ng; k++) {
+            s10 += k * pxmy[k];
+            s10sq += k * k * pxmy[k];
+            e11 += pxmy[k] * log10(pxmy[k] + EPS) / l2;
+        }
+        double hx = 0, hy = 0;
+        for (int i = 0; i < Ng; i++) {
+            hx -= px[i] * log10(px[i] + EPS) / l2;
+            hy -= py[i] * log10(py[i] + EPS) / l2;
+        }
+        const double hxy = -e9, m = hx > hy ? hx : hy;
+        res[0] = f1;
+        res[1] = f2;
+        res[2] = f3;
+        res[3] = var4;
+        res[4] = f5;
+        res[5] = f6;
+        res[6] = f7;
+        res[7] = sent;
+        res[8] = -e9;
+        res[9] = s10sq - s10 * s10;
+        res[10] = -e11;
+        res[11] = (m == 0) ? 1 : (hxy - hxy1) / m;
+        res[12] = sqrt(fabs(1 - exp(-2.0 * (hxy2 - hxy))));
+    }
+}
+
+// ---------------------------------------------------------------- f14
+// Q(i,j) = sum_k P(i,k) P(j,k) / (px_i py_k + 1e-13) (_Q_calc_eigen,
+// CVIPtexture.cpp:961-987), then eigenvalue #2 of Q in real-Schur order.
+__device__ void hh_make(const double *v, int n, double *ess, double &tau, double &beta) {
+    double tail = 0;
+    for (int i = 1; i < n; i++) tail = __dadd_rn(tail, __dmul_rn(v[i], v[i]));
+    const double c0 = v[0];
+    if (n == 1 || tail == 0) {
+        tau = 0;
+        beta = c0;
+        for (int i = 1; i < n; i++) ess[i - 1] = 0;
+    } else {
+        beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
+        if (c0 >= 0) beta = -beta;
+        for (int i = 1; i < n; i++) ess[i - 1] = v[i] / __dsub_rn(c0, beta);
+        tau = __dsub_rn(beta, c0) / beta;
+    }
+}
+
+// B = H B on rows r0..r0+m-1, columns c0..c0+nc-1 (threads over columns)
+__device__ void hh_left_par(double *A, int ld, int r0, int m, int c0, int nc, const double *ess, double tau) {
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        double *col = A + (long long)r0 * ld + c0 + c;
+        if (m == 1) {
+            col[0] = __dmul_rn(col[0], __dsub_rn(1.0, tau));
+            continue;
+        }
+        double t = 0;
+        for (int r = 1; r < m; r++) t = __dadd_rn(t, __dmul_rn(ess[r - 1], col[(long long)r * ld]));
+        t = __dadd_rn(t, col[0]);
+        col[0] = __dsub_rn(col[0], __dmul_rn(tau, t));
+        for (int r = 1; r < m; r++)
+            col[(long long)r * ld] = __dsub_rn(col[(long long)r * ld], __dmul_rn(__dmul_rn(tau, ess[r - 1]), t));
+    }
+}
+
+// B = B H on rows r0..r0+m-1, columns c0..c0+nc-1 (threads over rows)
+__device__ void hh_right_par(double *A, int ld, int r0, int m, int c0, int nc, const double *ess, double tau) {
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        double *row = A + (long long)(r0 + r) * ld + c0;
+        if (nc == 1) {
+            row[0] = __dmul_rn(row[0], __dsub_rn(1.0, tau));
+            continue;
+        }
+        double t = 0;
+        for (int c = 1; c < nc; c++) t = __dadd_rn(t, __dmul_rn(row[c], ess[c - 1]));
+        t = __dadd_rn(t, row[0]);
+        row[0] = __dsub_rn(row[0], __dmul_rn(tau, t));
+        for (int c = 1; c < nc; c++) row[c] = __dsub_rn(row[c], __dmul_rn(__dmul_rn(tau, t), ess[c - 1]));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_har_f14(const FJob *__restrict__ jobs, const HarJob *__restrict__ hj,
+                                                 char *__restrict__ wsb) {
+    __shared__ double px[256], py[256], v[256], ess[256];
+    __shared__ double s_tau, s_beta;
+    __shared__ int s_cmd, s_il, s_im, s_iu;
+    __shared__ double s_sh[3], s_fv[3], s_exshift;
+    const int ang = blockIdx.y;
+    const HarJob H = hj[blockIdx.x];
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    double *res = (double *)(wsb + H.res_b) + ang * 14;
+    if (n < 3) {
+        if (threadIdx.x == 0) res[13] = 0.0;
+        return;
+    }
+    const double *P = (const double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256;
+    double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
+    // marginals as the oracle computes them (sequential sums)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = 0, t = 0;
+        for (int j = 0; j < n; j++) {
+            s += P[(long long)i * n + j];
+            t += P[(long long)j * n + i];
+        }
+        px[i] = s;
+        py[i] = t;
+    }
+    __syncthreads();
+    for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
+        const int i = (int)(q / n), j = (int)(q - (long long)i * n);
+        const double di = px[i];
+        double s = 0;
+        for (int k = 0; k < n; k++) {
+            const double a = P[(long long)i * n + k], b = P[(long long)j * n + k];
+            const double rp = __dmul_rn(a, b);
+            if (rp == 0.0) continue;  // adds +0: skipping is exact
+            s = __dadd_rn(s, rp / __dadd_rn(__dmul_rn(di, py[k]), 0.0000000000001));
+        }
+        A[q] = s;
+    }
+    __syncthreads();
+    // Hessenberg reduction
+    for (int i = 0; i < n - 1; i++) {
+        const int rem = n - i - 1;
+        for (int k = threadIdx.x; k < rem; k += blockDim.x) v[k] = A[(long long)(i + 1 + k) * n + i];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tau, beta;
+            hh_make(v, rem, ess, tau, beta);
+            s_tau = tau;
+            s_beta = beta;
+        }
+        __syncthreads();
+        const double tau = s_tau;
+        if (threadIdx.x == 0) A[(long long)(i + 1) * n + i] = s_beta;
+        for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) A[(long long)(i + 1 + k) * n + i] = ess[k - 1];
+        __syncthreads();
+        hh_left_par(A, n, i + 1, rem, i + 1, rem, ess, tau);
+        __syncthreads();
+        hh_right_par(A, n, 0, n, i + 1, rem, ess, tau);
+        __syncthreads();
+    }
+    for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
+        const int r = (int)(q / n), c = (int)(q - (long long)r * n);
+        if (c < r - 1) A[q] = 0;
+    }
+    __syncthreads();
+#define T_(r, c) A[(long long)(r) * n + (c)]
+    // norm of T (computeNormOfT)
+    if (threadIdx.x == 0) {
+        double norm = 0;
+        for (int j = 0; j < n; j++) {
+            const int s0 = j - 1 > 0 ? j - 1 : 0;
+            double s = 0;
+            for (int c = s0; c < n; c++) s += fabs(T_(j, c));
+            norm += s;
+        }
+        s_sh[0] = norm;
+        s_exshift = 0;
+    }
+    __syncthreads();
+    const double norm = s_sh[0];
+    const double eps = DBL_EPSILON;
+    const int maxIter = 40 * n;
+    int iu = n - 1, iter = 0, totalIter = 0;
+    bool failed = false;
+    if (norm != 0) {
+        while (iu >= 0) {
+            // thread 0 decides; others follow the broadcast command
+            if (threadIdx.x == 0) {
+                int il = iu;
+                while (il > 0) {
+                    double s = fabs(T_(il - 1, il - 1)) + fabs(T_(il, il));
+                    if (s == 0.0) s = norm;
+                    if (fabs(T_(il, il - 1)) < eps * s) break;
+                    il--;
+                }
+                s_il = il;
+                if (il == iu) {
+                    T_(iu, iu) = T_(iu, iu) + s_exshift;
+                    if (iu > 0) T_(iu, iu - 1) = 0;
+                    s_cmd = 0;
+                } else if (il == iu - 1) {
+                    const double p = 0.5 * (T_(iu - 1, iu - 1) - T_(iu, iu));
+                    const double q = p * p + T_(iu, iu - 1) * T_(iu - 1, iu);
+                    T_(iu, iu) += s_exshift;
+                    T_(iu - 1, iu - 1) += s_exshift;
+                    if (q >= 0) {
+                        const double z = sqrt(fabs(q));
+                        const double gp = (p >= 0) ? p + z : p - z, gq = T_(iu, iu - 1);
+                        double c, s;
+                        if (gq == 0) { c = gp < 0 ? -1 : 1; s = 0; }
+                        else if (gp == 0) { c = 0; s = gq < 0 ? 1 : -1; }
+                        else if (fabs(gp) > fabs(gq)) {
+                            const double t = gq / gp;
+                            double u = sqrt(1 + t * t);
+                            if (gp < 0) u = -u;
+                            c = 1 / u;
+                            s = -t * c;
+                        } else {
+                            const double t = gp / gq;
+                            double u = sqrt(1 + t * t);
+                            if (gq < 0) u = -u;
+                            s = -1 / u;
+                            c = -t * s;
+                        }
+                        s_sh[0] = c;
+                        s_sh[1] = s;
+                        s_cmd = 1;
+                    } else {
+                        s_cmd = 2;
+                    }
+                } else {
+                    double sh0 = T_(iu, iu), sh1 = T_(iu - 1, iu - 1), sh2 = T_(iu, iu - 1) * T_(iu - 1, iu);
+                    if (iter == 10) {
+                        s_exshift += sh0;
+                        for (int i = 0; i <= iu; i++) T_(i, i) -= sh0;
+                        const double s = fabs(T_(iu, iu - 1)) + fabs(T_(iu - 1, iu - 2));
+                        sh0 = 0.75 * s;
+                        sh1 = 0.75 * s;
+                        sh2 = -0.4375 * s * s;
+                    }
+                    if (iter == 30) {
+                        double s = (sh1 - sh0) / 2.0;
+                        s = s * s + sh2;
+                        if (s > 0) {
+                            s = sqrt(s);
+                            if (sh1 < sh0) s = -s;
+                            s = s + (sh1 - sh0) / 2.0;
+                            s = sh0 - sh2 / s;
+                            s_exshift += s;
+                            for (int i = 0; i <= iu; i++) T_(i, i) -= s;
+                            sh0 = sh1 = sh2 = 0.964;
+                        }
+                    }
+                    double fv0 = 0, fv1 = 0, fv2 = 0;
+                    int im;
+                    for (im = iu - 2; im >= il; --im) {
+                        const double Tmm = T_(im, im), r = sh0 - Tmm, s = sh1 - Tmm;
+                        fv0 = (r * s - sh2) / T_(im + 1, im) + T_(im, im + 1);
+                        fv1 = T_(im + 1, im + 1) - Tmm - r - s;
+                        fv2 = T_(im + 2, im + 1);
+                        if (im == il) break;
+                        const double lhs = T_(im, im - 1) * (fabs(fv1) + fabs(fv2));
+                        const double rhs = fv0 * (fabs(T_(im - 1, im - 1)) + fabs(Tmm) + fabs(T_(im + 1, im + 1)));
+                        if (fabs(lhs) < eps * rhs) break;
+                    }
+                    s_im = im;
+                    s_fv[0] = fv0;
+                    s_fv[1] = fv1;
+                    s_fv[2] = fv2;
+                    s_cmd = 3;
+                }
+            }
+            __syncthreads();
+            const int cmd = s_cmd;
+            if (cmd == 0) {
+                iu--;
+                iter = 0;
+            } else if (cmd == 1 || cmd == 2) {
+                if (cmd == 1) {
+                    const double c = s_sh[0], s = s_sh[1];
+                    for (int col = iu - 1 + threadIdx.x; col < n; col += blockDim.x) {
+                        const double xi = T_(iu - 1, col), yi = T_(iu, col);
+                        T_(iu - 1, col) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
+                        T_(iu, col) = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
+                    }
+                    __syncthreads();
+                    for (int row = threadIdx.x; row <= iu; row += blockDim.x) {
+                        const double xi = T_(row, iu - 1), yi = T_(row, iu);
+                        T_(row, iu - 1) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
+                        T_(row, iu) = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
+                    }
+                    __syncthreads();
+                    if (threadIdx.x == 0) T_(iu, iu - 1) = 0;
+                }
+                if (threadIdx.x == 0 && iu > 1) T_(iu - 1, iu - 2) = 0;
+                __syncthreads();
+                iu -= 2;
+                iter = 0;
+            } else {
+                iter++;
+                totalIter++;
+                if (totalIter > maxIter) {
+                    failed = true;
+                    break;
+                }
+                const int il = s_il, im = s_im;
+                for (int k = im; k <= iu - 2; ++k) {
+                    const bool first = (k == im);
+                    if (threadIdx.x == 0) {
+                        double vv[3];
+                        if (first) { vv[0] = s_fv[0]; vv[1] = s_fv[1]; vv[2] = s_fv[2]; }
+                        else { vv[0] = T_(k, k - 1); vv[1] = T_(k + 1, k - 1); vv[2] = T_(k + 2, k - 1); }
+                        double tau, beta;
+                        hh_make(vv, 3, ess, tau, beta);
+                        s_tau = tau;
+                        s_beta = beta;
+                        if (beta != 0) {
+                            if (first && k > il) T_(k, k - 1) = -T_(k, k - 1);
+                            else if (!first) T_(k, k - 1) = beta;
+                        }
+                    }
+                    __syncthreads();
+                    if (s_beta != 0) {
+                        hh_left_par(A, n, k, 3, k, n - k, ess, s_tau);
+                        __syncthreads();
+                        hh_right_par(A, n, 0, min(iu, k + 3) + 1, k, 3, ess, s_tau);
+                    }
+                    __syncthreads();
+                }
+                if (threadIdx.x == 0) {
+                    double vv[2] = {T_(iu - 1, iu - 2), T_(iu, iu - 2)};
+                    double tau, beta;
+                    hh_make(vv, 2, ess, tau, beta);
+                    s_tau = tau;
+                    s_beta = beta;
+                    if (beta != 0) T_(iu - 1, iu - 2) = beta;
+                }
+                __syncthreads();
+                if (s_beta != 0) {
+                    hh_left_par(A, n, iu - 1, 2, iu - 1, n - iu + 1, ess, s_tau);
+                    __syncthreads();
+                    hh_right_par(A, n, 0, iu + 1, iu - 1, 2, ess, s_tau);
+                }
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    for (int i = im + 2; i <= iu; ++i) {
+                        T_(i, i - 2) = 0;
+                        if (i > im + 2) T_(i, i - 3) = 0;
+                    }
+                __syncthreads();
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        double f = 0;
+        if (!failed) {
+            // eigenvalue #2 in Schur order (EigenSolver::compute, EigenSolver.h:363-381)
+            int i = 0;
+            double re2 = 0, im2 = 1;
+            while (i < n && i <= 2) {
+                if (i == n - 1 || T_(i + 1, i) == 0) {
+                    if (i == 2) { re2 = T_(i, i); im2 = 0; }
+                    ++i;
+                } else {
+                    const double p = 0.5 * (T_(i, i) - T_(i + 1, i + 1));
+                    const double z = sqrt(fabs(p * p + T_(i + 1, i) * T_(i, i + 1)));
+                    if (i == 2 || i + 1 == 2) { re2 = T_(i + 1, i + 1) + p; im2 = (i == 2) ? z : -z; }
+                    i += 2;
+                }
+            }
+            if (im2 == 0) f = sqrt(re2);
+        }
+        res[13] = f;  // no convergence: 0, as the oracle
+    }
+#undef T_
+}
+
+// mean and range over the angles, permuted into the output order
+__global__ void k_har_final(const FJob *__restrict__ jobs, const HarJob *__restrict__ hj, const char *__restrict__ wsb,
+                            double *__restrict__ feat) {
+    const FJob J = jobs[blockIdx.x];
+    const HarJob H = hj[blockIdx.x];
+    const double *res = (const double *)(wsb + H.res_b);
+    if (threadIdx.x != 0) return;
+    double mn[14], mx[14], sm[14], tmp[28];
+    for (int a = 0; a < 14; a++) { mn[a] = 10E200; mx[a] = -10E200; sm[a] = 0; }
+    for (int ang = 0; ang < 4; ang++)
+        for (int a = 0; a < 14; a++) {
+            const double v = res[ang * 14 + a];
+            sm[a] += v;
+            if (v < mn[a]) mn[a] = v;
+            if (v > mx[a]) mx[a] = v;
+        }
+    for (int a = 0; a < 14; a++) { tmp[a] = sm[a] / 4; tmp[a + 14] = mx[a] - mn[a]; }
+    const int perm[28] = {0, 14, 1, 15, 2, 16, 9, 23, 10, 24, 8, 22, 11, 25, 4, 18, 13, 27, 12, 26, 5, 19, 7, 21, 6, 20, 3, 17};
+    for (int k = 0; k < 28; k++) feat[J.out + k] = tmp[perm[k]];
+}
+
+void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
+                     int njobs, const HarJob *hj, char *wsb, double *feat) {
+    if (njobs <= 0) return;
+    const int sm = 256 * 257 / 2 * sizeof(unsigned int);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_har_glcm, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        attr = true;
+    }
+    WC_LAUNCH(c);
+    k_har_quant<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, jobs, hj, wsb);
+    WC_LAUNCH(c);
+    k_har_glcm<<<dim3(njobs, 4), 1024, sm, c.st>>>(planes, jobs, hj, wsb);
+    WC_LAUNCH(c);
+    k_har_stats<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
+    WC_LAUNCH(c);
+    k_har_f14<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
+    WC_LAUNCH(c);
+    k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);
+}
+
+}  // namespace wc

@@ -1,0 +1,226 @@
+// Tamura textures (FP64 form): Tamura3Sigs2D, src/textures/tamura.cpp:10-299.
+//   normImg = (p - min) / max
+//   coarseness: running sums S(y,x) = I + S(y,x-1) + S(y-1,x) - S(y-1,x-1) with
+//     the reference's exact recurrence (an anti-diagonal wavefront, so every
+//     entry is rounded exactly as on the CPU), local means over 2^k windows via
+//     efficientLocalMean (:106-139), best scale per pixel, mean and a 3-bin
+//     histogram normalised by its largest bin;
+//   directionality: 3x3 zero-padded correlations with the kernels as the
+//     reference's assignments leave them (:45-57), phi = atan(dV/dH)+pi/2+0.001
+//     where dH >= 1e-4, 125-bin histogram;
+//   contrast: std / (kurtosis / std^4)^(1/4) from Moments4 (no -3).
+// Output order: hist0, hist1, hist2, contrast, directionality, coarseness.
+#include <cfloat>
+#include <cmath>
+
+#include "kcommon.cuh"
+#include "kernels.h"
+
+namespace wc {
+
+// S table by anti-diagonals; one CTA per job.  norm written on the fly.
+__global__ void __launch_bounds__(1024) k_tam_prefix(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                     const PlaneStats *__restrict__ stats, const FJob *__restrict__ jobs,
+                                                     const TamJob *__restrict__ tj, double *__restrict__ ws) {
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const PlaneStats St = stats[J.plane];
+    const TamJob T = tj[blockIdx.x];
+    const int W = P.w, H = P.h;
+    const double *p = arena + P.off;
+    double *nrm = ws + T.norm_ws, *S = ws + T.sum_ws;
+    for (long long i = threadIdx.x; i < (long long)W * H; i += blockDim.x) nrm[i] = (p[i] - St.mn) / St.mx;
+    __syncthreads();
+    for (int d = 0; d < W + H - 1; d++) {
+        const int y0 = max(0, d - (W - 1)), y1 = min(d, H - 1);
+        for (int y = y0 + threadIdx.x; y <= y1; y += blockDim.x) {
+            const int x = d - y;
+            const double l = (x < 1) ? 0 : S[(long long)y * W + x - 1];
+            const double o = (y < 1) ? 0 : S[(long long)(y - 1) * W + x];
+            const double ol = (y < 1 || x < 1) ? 0 : S[(long long)(y - 1) * W + x - 1];
+            S[(long long)y * W + x] = __dsub_rn(__dadd_rn(__dadd_rn(nrm[(long long)y * W + x], l), o), ol);
+        }
+        __syncthreads();
+    }
+}
+
+// efficientLocalMean (tamura.cpp:106-139)
+__device__ __forceinline__ double local_mean(const double *__restrict__ S, int W, int H, long long x, long long y, long long k) {
+    const long long k2 = k / 2;
+    long long sy = y - k2, sx = x - k2, ey = y + k2 - 1, ex = x + k2 - 1;
+    if (sy < 0) sy = 0;
+    if (sx < 0) sx = 0;
+    if (ex > W - 1) ex = W - 1;
+    if (ey > H - 1) ey = H - 1;
+    const double links = (sx - 1 < 0) ? 0 : S[ey * W + sx - 1];
+    const double oben = (sy - 1 < 0) ? 0 : S[(ey - 1) * W + sx];
+    const double ol = ((sy - 1 < 0) || (sx - 1 < 0)) ? 0 : S[(ey - 1) * W + sx - 1];
+    const double unten = S[ey * W + sx];
+    const long long cnt = (ey - sy + 1) * (ex - sx + 1);
+    return __dadd_rn(__dsub_rn(__dsub_rn(unten, links), oben), ol) / (double)cnt;
+}
+
+#define TAM_TILE 1024
+// per pixel: best coarseness scale, direction angle; per-CTA partials
+__global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                                                   const TamJob *__restrict__ tj, double *__restrict__ ws,
+                                                   double *__restrict__ part, int nchunk) {
+    __shared__ double sh[32];
+    __shared__ long long shl[32];
+    const FJob J = jobs[blockIdx.y];
+    const Plane P = planes[J.plane];
+    const TamJob T = tj[blockIdx.y];
+    const int W = P.w, H = P.h;
+    const long long n = (long long)W * H;
+    const double *nrm = ws + T.norm_ws, *S = ws + T.sum_ws;
+    unsigned char *sb = (unsigned char *)(ws + T.sbest_ws);
+    double *phi = ws + T.phi_ws;
+    long long ksum = 0;
+    int kmin = 1 << 30, kmax = -1;
+    double pmn = DBL_MAX, pmx = -DBL_MAX, sr = 0;
+    const long long i0 = (long long)blockIdx.x * TAM_TILE, i1 = min(n, i0 + TAM_TILE);
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int y = (int)(i / W), x = (int)(i - (long long)y * W);
+        // coarseness: first strict maximum over k = 1..7, horizontal before vertical
+        double maxE = 0;
+        int maxk = 0, k2 = 1;
+        for (int k = 1; k <= 7; k++, k2 *= 2) {
+            const long long len = 2 * k2;
+            double eh = 0, ev = 0;
+            if (x + k2 < W && x - k2 >= 0)
+                eh = fabs(__dsub_rn(local_mean(S, W, H, x + k2, y, len), local_mean(S, W, H, x - k2, y, len)));
+            if (y + k2 < H && y - k2 >= 0)
+                ev = fabs(__dsub_rn(local_mean(S, W, H, x, y + k2, len), local_mean(S, W, H, x, y - k2, len)));
+            if (eh > maxE) { maxE = eh; maxk = k; }
+            if (ev > maxE) { maxE = ev; maxk = k; }
+        }
+        sb[i] = (unsigned char)maxk;
+        ksum += maxk;
+        kmin = min(kmin, maxk);
+        kmax = max(kmax, maxk);
+        // directionality: H = [[-1,2,1],[-2,0,2],[-1,-2,-1]], V = [[1,0,0],[0,0,0],[-1,0,0]],
+        // accumulated x offset outer, y offset inner, zero outside the image
+        const double fH[3][3] = {{-1, 2, 1}, {-2, 0, 2}, {-1, -2, -1}};
+        const double fV[3][3] = {{1, 0, 0}, {0, 0, 0}, {-1, 0, 0}};
+        double dH = 0, dV = 0;
+        for (int a = -1; a <= 1; a++) {
+            const int xx = x + a;
+            if (xx < 0 || xx >= W) continue;
+            for (int b = -1; b <= 1; b++) {
+                const int yy = y + b;
+                if (yy < 0 || yy >= H) continue;
+                const double v = nrm[(long long)yy * W + xx];
+                dH = __dadd_rn(dH, __dmul_rn(fH[b + 1][a + 1], v));
+                dV = __dadd_rn(dV, __dmul_rn(fV[b + 1][a + 1], v));
+            }
+        }
+        double ph = 0.0;
+        if (dH >= 0.0001) {
+            ph = atan(dV / dH) + (M_PI / 2.0 + 0.001);
+            sr += __dadd_rn(__dadd_rn(__dmul_rn(dH, dH), __dmul_rn(dV, dV)), __dmul_rn(ph, ph));
+        }
+        phi[i] = ph;
+        pmn = fmin(pmn, ph);
+        pmx = fmax(pmx, ph);
+    }
+    ksum = block_sum_ll(ksum, shl);
+    const double dkmin = block_min((double)kmin, sh), dkmax = block_max((double)kmax, sh);
+    pmn = block_min(pmn, sh);
+    pmx = block_max(pmx, sh);
+    sr = block_sum(sr, sh);
+    if (threadIdx.x == 0) {
+        double *o = part + ((long long)blockIdx.y * nchunk + blockIdx.x) * 6;
+        o[0] = (double)ksum;
+        o[1] = dkmin;
+        o[2] = dkmax;
+        o[3] = pmn;
+        o[4] = pmx;
+        o[5] = sr;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_tam_final(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                                                    const TamJob *__restrict__ tj, const double *__restrict__ ws,
+                                                    const double *__restrict__ part, int nchunk_max,
+                                                    double *__restrict__ feat) {
+    __shared__ double sh[32];
+    __shared__ unsigned int hs[3], hp[125];
+    const FJob J = jobs[blockIdx.x];
+    const Plane P = planes[J.plane];
+    const TamJob T = tj[blockIdx.x];
+    const long long n = (long long)P.w * P.h;
+    const int nch = (int)((n + TAM_TILE - 1) / TAM_TILE);
+    double ksum = 0, kmin = DBL_MAX, kmax = -DBL_MAX, pmn = DBL_MAX, pmx = -DBL_MAX, sr = 0;
+    for (int c = 0; c < nch; c++) {  // every thread reduces the partials in the same order
+        const double *o = part + ((long long)blockIdx.x * nchunk_max + c) * 6;
+        ksum += o[0];
+        kmin = fmin(kmin, o[1]);
+        kmax = fmax(kmax, o[2]);
+        pmn = fmin(pmn, o[3]);
+        pmx = fmax(pmx, o[4]);
+        sr += o[5];
+    }
+    if (threadIdx.x < 3) hs[threadIdx.x] = 0;
+    if (threadIdx.x < 125) hp[threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned char *sb = (const unsigned char *)(ws + T.sbest_ws);
+    const double *phi = ws + T.phi_ws, *nrm = ws + T.norm_ws;
+    const double ssc = hist_scale(kmin, kmax, 3), psc = hist_scale(pmn, pmx, 125);
+    double s1 = 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        atomicAdd(&hs[hist_bin((double)sb[i], kmin, ssc, 3)], 1u);
+        atomicAdd(&hp[hist_bin(phi[i], pmn, psc, 125)], 1u);
+        s1 += nrm[i];
+    }
+    s1 = block_sum(s1, sh);
+    const double mean = s1 / (double)n;
+    double m2 = 0, m4 = 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double d = nrm[i] - mean, d2 = d * d;
+        m2 += d2;
+        m4 += d2 * d2;
+    }
+    m2 = block_sum(m2, sh);
+    m4 = block_sum(m4, sh);
+    if (threadIdx.x == 0) {
+        // coarseness mean: unsigned 32-bit denominator as in tamura.cpp:246-248
+        const unsigned yD = P.h, xD = P.w;
+        double coarse = ksum;
+        if (yD == 32 || xD == 32) coarse /= (double)((unsigned)((xD + 1 - 32) * (yD + 1 - 32)));
+        else coarse /= (double)((unsigned)((yD - 32) * (xD - 32)));
+        double hm = 0;
+        for (int k = 0; k < 3; k++) hm = fmax(hm, (double)hs[k]);
+        double mx = 0;
+        long fmx = 0;
+        for (int a = 0; a < 125; a++)
+            if ((double)hp[a] > mx) { mx = hp[a]; fmx = a; }
+        double sum = 0;
+        for (int a = 0; a < 125; a++) sum += (double)hp[a] * pow((double)(a + 1 - fmx), 2);
+        const double dir = fabs(log(sum / sr + 0.0000001));
+        const double nn = (double)n;
+        const double sd = n > 2 ? sqrt(m2 / (nn - 1)) : 0.0;
+        const double kurt = n > 4 ? (nn * m4) / (m2 * m2) : 0.0;
+        const double con = (sd < DBL_EPSILON) ? 0 : sd / pow(kurt / pow(sd, 4), 0.25);
+        double *o = feat + J.out;
+        o[0] = hs[0] / hm;
+        o[1] = hs[1] / hm;
+        o[2] = hs[2] / hm;
+        o[3] = con;
+        o[4] = dir;
+        o[5] = coarse;
+    }
+}
+
+void launch_tamura(Ctx &c, const Plane *planes, const PlaneStats *stats, const double *arena, const FJob *jobs, int njobs,
+                   const TamJob *tj, double *ws, double *part, long long maxpix, double *feat) {
+    if (njobs <= 0) return;
+    const int nchunk = (int)((maxpix + TAM_TILE - 1) / TAM_TILE);
+    WC_LAUNCH(c);
+    k_tam_prefix<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, jobs, tj, ws);
+    WC_LAUNCH(c);
+    k_tam_pixel<<<dim3(nchunk, njobs), 256, 0, c.st>>>(planes, jobs, tj, ws, part, nchunk);
+    WC_LAUNCH(c);
+    k_tam_final<<<njobs, 1024, 0, c.st>>>(planes, jobs, tj, ws, part, nchunk, feat);
+}
+
+}  // namespace wc

@@ -59,4 +59,18 @@ void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const 
                         int maxh, int max_cnt_x, int max_src_w, int max_src_h, const CFJob *cj, const double *tabs,
                         double *ws, double *part, int nchunk_max, double *feat);
 
+// k_tamura.cu
+struct TamJob {
+    long long norm_ws, sum_ws, sbest_ws, phi_ws;  // offsets in doubles into the workspace
+};
+void launch_tamura(Ctx &c, const Plane *planes, const PlaneStats *stats, const double *arena, const FJob *jobs, int njobs,
+                   const TamJob *tj, double *ws, double *part, long long maxpix, double *feat);
+
+// k_haralick.cu
+struct HarJob {
+    long long gray_b, lut_b, glcm_b, q_b, res_b;  // byte offsets into the workspace
+};
+void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
+                     int njobs, const HarJob *hj, char *wsb, double *feat);
+
 }  // namespace wc

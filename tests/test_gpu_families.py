@@ -14,7 +14,8 @@ GROUP_C = ["Comb Moments", "Haralick Textures", "Multiscale Histograms", "Tamura
 GROUP_B = ["Chebyshev-Fourier Coefficients", "Chebyshev Coefficients", "Zernike Coefficients"]
 GROUP_A = ["Edge Features", "Otsu Object Features", "Inverse-Otsu Object Features", "Gabor Textures"]
 READY = {"Comb Moments", "Multiscale Histograms", "Radon Coefficients", "Fractal Features", "Zernike Coefficients",
-         "Chebyshev-Fourier Coefficients", "Tamura Textures", "Haralick Textures",
+         "Chebyshev-Fourier Coefficients", "Tamura Textures", "Haralick Textures", "Edge Features", "Otsu Object Features",
+         "Inverse-Otsu Object Features", "Gabor Textures",
          "Pixel Intensity Statistics", "Gini Coefficient", "Chebyshev Coefficients"}
 
 

@@ -17,6 +17,42 @@ std::vector<double> cheb_table(int len, int N);
 
 void features_init() { set_zernike_tables(); }
 
+// Gabor kernel (function Gabor, src/textures/gabor.cpp:103-162): n = 38,
+// sig2lam = 0.56, gamma = 0.5, theta = 3.14159265/2, fi = 0, normalised by the
+// sum of magnitudes; interleaved (re, im), row-major 38 x 38.
+static std::vector<double> gabor_kernel(double f0) {
+    const int n = 38;
+    const double sig2lam = 0.56, gamma = 0.5, theta = 3.14159265 / 2, fi = 0;
+    const double lambda = 2 * M_PI / f0, ct = cos(theta), st = sin(theta), sig = sig2lam * lambda;
+    std::vector<double> tx(n + 1), ty(n + 1), G((size_t)n * n * 2);
+    tx[0] = -(n / 2);
+    for (int x = 1; x <= n; x++) tx[x] = tx[x - 1] + 1;
+    ty[0] = -(n / 2);
+    for (int y = 1; y <= n; y++) ty[y] = ty[y - 1] + 1;
+    double sum = 0;
+    for (int y = 0; y < n; y++)
+        for (int x = 0; x < n; x++) {
+            const double xte = tx[x] * ct + ty[y] * st, yte = ty[y] * ct - tx[x] * st;
+            const double rte = xte * xte + gamma * gamma * yte * yte;
+            const double ge = exp(-1 * rte / (2 * sig * sig));
+            const double argm = xte * f0 + fi;
+            G[(size_t)y * n * 2 + x * 2] = ge * cos(argm);
+            G[(size_t)y * n * 2 + x * 2 + 1] = ge * sin(argm);
+            sum += sqrt(pow(G[(size_t)y * n * 2 + x * 2], 2) + pow(G[(size_t)y * n * 2 + x * 2 + 1], 2));
+        }
+    for (auto &g : G) g = g / sum;
+    return G;
+}
+
+static int smooth_size(int n) {  // smallest m >= n with prime factors in {2, 3, 5, 7}
+    for (int m = n;; m++) {
+        int r = m;
+        for (int p : {2, 3, 5, 7})
+            while (r % p == 0) r /= p;
+        if (r == 1) return m;
+    }
+}
+
 // positions of the reference's Downsample loop (x starts at 0, x += dx while
 // x < old): src/cmatrix.cpp:602-606
 static std::vector<double> ds_positions(int old, double dx) {
@@ -189,6 +225,136 @@ int features_prepare(FeatureSetup &fs) {
         }
         fs.off["har_jobs"] = fs.put_copy(hj.data(), hj.size() * sizeof(HarJob));
     }
+    // Edge features: magnitude / direction planes in the workspace, sorted copies
+    if (!fj[A_EDGEF].empty()) {
+        std::vector<EFJob> ej;
+        std::vector<Plane> aux;
+        std::vector<int> ids;
+        std::vector<long long> koff;
+        size_t ktot = 0;
+        for (auto &j : fj[A_EDGEF]) {
+            const Plane &Q = P[j.plane];
+            const size_t n = (size_t)Q.w * Q.h;
+            EFJob e;
+            e.mag_ws = (long long)(fs.ws_take(n * 8) / 8);
+            e.dir_ws = (long long)(fs.ws_take(n * 8) / 8);
+            ej.push_back(e);
+            for (long long o : {e.mag_ws, e.dir_ws}) {
+                ids.push_back((int)aux.size());
+                aux.push_back({o, Q.w, Q.h});
+                koff.push_back((long long)ktot);
+                ktot += (n + 31) & ~(size_t)31;
+            }
+        }
+        fs.off["ef_jobs"] = fs.put_copy(ej.data(), ej.size() * sizeof(EFJob));
+        fs.off["ef_aux"] = fs.put_copy(aux.data(), aux.size() * sizeof(Plane));
+        fs.off["ef_ids"] = fs.put_copy(ids.data(), ids.size() * sizeof(int));
+        fs.off["ef_koff"] = fs.put_copy(koff.data(), koff.size() * sizeof(long long));
+        fs.off["ef_stats"] = fs.meta_take(aux.size() * sizeof(PlaneStats));
+        fs.off["ef_keys"] = fs.ws_take(ktot * 8);
+        fs.off["ef_tmp"] = fs.ws_take(ktot * 8);
+        fs.off["ef_cnt"] = fs.ws_take(aux.size() * 256 * 512 * sizeof(unsigned int));
+    }
+
+    // Otsu / Inverse-Otsu object features (one job list for both)
+    if (!fj[A_OBJ].empty() || !fj[A_INVOBJ].empty()) {
+        std::vector<FJob> all;
+        std::vector<OBJob> oj;
+        std::vector<Plane> inv;
+        long long maxpix = 0;
+        for (int a : {A_OBJ, A_INVOBJ})
+            for (auto &j : fj[a]) all.push_back(j);
+        size_t zero_begin = fs.ws_take(0), zero_bytes = 0;
+        (void)zero_bytes;
+        // zeroed block first: area (u32), xm, ym (u64) per job, accumulators
+        std::vector<size_t> zoff;
+        for (auto &j : all) {
+            const size_t n = (size_t)P[j.plane].w * P[j.plane].h;
+            zoff.push_back(fs.ws_take(n * 4));
+            zoff.push_back(fs.ws_take(n * 8));
+            zoff.push_back(fs.ws_take(n * 8));
+        }
+        const size_t acc_off = fs.ws_take(all.size() * 8 * 8);
+        const size_t zero_end = fs.ws_take(0);
+        fs.val["ob_zero_begin"] = (long long)zero_begin;
+        fs.val["ob_zero_bytes"] = (long long)(zero_end - zero_begin);
+        fs.off["ob_acc"] = acc_off;
+        for (size_t k = 0; k < all.size(); k++) {
+            const Plane &Q = P[all[k].plane];
+            const size_t n = (size_t)Q.w * Q.h;
+            maxpix = std::max(maxpix, (long long)n);
+            OBJob o;
+            memset(&o, 0, sizeof o);
+            o.inverse = k >= fj[A_OBJ].size();
+            o.src_ws = (long long)(fs.ws_take(o.inverse ? n * 8 : 8) / 8);
+            o.lab_ws = (long long)(fs.ws_take(n * 4) / 8);
+            o.area_ws = (long long)(zoff[3 * k] / 8);
+            o.xm_ws = (long long)(zoff[3 * k + 1] / 8);
+            o.ym_ws = (long long)(zoff[3 * k + 2] / 8);
+            o.roots_ws = (long long)(fs.ws_take(n * 4) / 8);
+            o.keys_ws = (long long)(fs.ws_take(2 * n * 8) / 8);
+            o.tmp_ws = (long long)(fs.ws_take(n * 8) / 8);
+            o.dist_ws = (long long)(fs.ws_take(n * 8) / 8);
+            o.cnt_ws = (long long)(fs.ws_take(256 * 512 * 4) / 8);
+            oj.push_back(o);
+            inv.push_back({o.src_ws, Q.w, Q.h});
+        }
+        fs.off["ob_fjobs"] = fs.put_copy(all.data(), all.size() * sizeof(FJob));
+        fs.off["ob_jobs"] = fs.put_copy(oj.data(), oj.size() * sizeof(OBJob));
+        fs.off["ob_inv"] = fs.put_copy(inv.data(), inv.size() * sizeof(Plane));
+        fs.off["ob_invstats"] = fs.meta_take(inv.size() * sizeof(PlaneStats));
+        fs.off["ob_thr"] = fs.ws_take(all.size() * 8);
+        fs.val["ob_n"] = (long long)all.size();
+        fs.val["ob_maxpix"] = maxpix;
+    }
+
+    // Gabor: padded spectra, 8 energy maps per job, kernel spectra per size
+    if (!fj[A_GABOR].empty()) {
+        std::vector<GabJob> gj;
+        std::vector<GabSize> sizes;
+        std::vector<FFTPlan> plans;
+        std::map<int, int> pidx;
+        auto plan_of = [&](int n) {
+            if (!pidx.count(n)) { pidx[n] = (int)plans.size(); plans.push_back(fs.fft_plan(n)); }
+            return pidx[n];
+        };
+        std::vector<double> kt;
+        for (double f0 : {0.1, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0}) {
+            std::vector<double> g = gabor_kernel(f0);
+            kt.insert(kt.end(), g.begin(), g.end());
+        }
+        fs.val["gab_kern"] = fs.tabs_add("gabor38", kt);
+        for (auto &j : fj[A_GABOR]) {
+            const Plane &Q = P[j.plane];
+            GabJob g;
+            g.fh = smooth_size(Q.h + 37);
+            g.fw = smooth_size(Q.w + 37);
+            if (g.fh > kMaxFFT || g.fw > kMaxFFT) return set_err(WC_ERR_UNSUPPORTED, "Gabor: image too large");
+            g.plan_h = plan_of(g.fh);
+            g.plan_w = plan_of(g.fw);
+            int si = -1;
+            for (size_t k = 0; k < sizes.size(); k++)
+                if (sizes[k].fh == g.fh && sizes[k].fw == g.fw) si = (int)k;
+            if (si < 0) {
+                GabSize S{g.fh, g.fw, g.plan_h, g.plan_w, (long long)(fs.ws_take((size_t)8 * g.fh * g.fw * 16) / 8)};
+                sizes.push_back(S);
+                si = (int)sizes.size() - 1;
+            }
+            g.g_ws = sizes[si].g_ws;
+            gj.push_back(g);
+        }
+        for (auto &g : gj) g.a_ws = (long long)(fs.ws_take((size_t)g.fh * g.fw * 16) / 8);
+        for (auto &g : gj) g.c_ws = (long long)(fs.ws_take((size_t)g.fh * g.fw * 16) / 8);
+        for (size_t k = 0; k < gj.size(); k++) {
+            const Plane &Q = P[fj[A_GABOR][k].plane];
+            gj[k].e_ws = (long long)(fs.ws_take((size_t)8 * Q.w * Q.h * 8) / 8);
+        }
+        fs.off["gab_jobs"] = fs.put_copy(gj.data(), gj.size() * sizeof(GabJob));
+        fs.off["gab_plans"] = fs.put_copy(plans.data(), plans.size() * sizeof(FFTPlan));
+        fs.off["gab_counts"] = fs.ws_take(gj.size() * 8 * 8);
+        fs.gab_jobs = gj;
+        fs.gab_sizes = sizes;
+    }
     return WC_OK;
 }
 
@@ -239,6 +405,25 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
     if (nj(A_HARALICK))
         launch_haralick(c, fr.arena, fr.planes, fr.stats, jobs(A_HARALICK), nj(A_HARALICK),
                         (const HarJob *)(fr.meta + fs.off["har_jobs"]), fr.ws, fr.feat);
+    if (nj(A_EDGEF))
+        launch_edgefeat(c, fr.arena, fr.planes, jobs(A_EDGEF), nj(A_EDGEF), maxw_of(P, fj[A_EDGEF]),
+                        maxh_of(P, fj[A_EDGEF]), (const EFJob *)(fr.meta + fs.off["ef_jobs"]), (double *)fr.ws,
+                        (const Plane *)(fr.meta + fs.off["ef_aux"]), (const int *)(fr.meta + fs.off["ef_ids"]),
+                        (PlaneStats *)(fr.meta + fs.off["ef_stats"]), (unsigned long long *)(fr.ws + fs.off["ef_keys"]),
+                        (unsigned long long *)(fr.ws + fs.off["ef_tmp"]), (const long long *)(fr.meta + fs.off["ef_koff"]),
+                        (unsigned int *)(fr.ws + fs.off["ef_cnt"]), fr.feat);
+    if (fs.val.count("ob_n")) {
+        if (cudaMemsetAsync(fr.ws + fs.val["ob_zero_begin"], 0, (size_t)fs.val["ob_zero_bytes"], c.st) != cudaSuccess)
+            return set_err(WC_ERR_CUDA, "memset failed");
+        launch_objects(c, fr.arena, fr.planes, fr.stats, (const FJob *)(fr.meta + fs.off["ob_fjobs"]), (int)fs.val["ob_n"],
+                       fs.val["ob_maxpix"], (const OBJob *)(fr.meta + fs.off["ob_jobs"]), (double *)fr.ws,
+                       (const Plane *)(fr.meta + fs.off["ob_inv"]), (PlaneStats *)(fr.meta + fs.off["ob_invstats"]),
+                       (double *)(fr.ws + fs.off["ob_thr"]), (unsigned long long *)(fr.ws + fs.off["ob_acc"]), fr.feat);
+    }
+    if (nj(A_GABOR))
+        launch_gabor(c, fr.arena, fr.planes, jobs(A_GABOR), nj(A_GABOR), (const GabJob *)(fr.meta + fs.off["gab_jobs"]),
+                     fs.gab_jobs, fs.gab_sizes, (const FFTPlan *)(fr.meta + fs.off["gab_plans"]), fr.tabs,
+                     fs.val["gab_kern"], (double *)fr.ws, (double *)(fr.ws + fs.off["gab_counts"]), fr.feat);
     return WC_OK;
 }
 

@@ -7,6 +7,7 @@
 
 #include "kcommon.cuh"
 #include "kernels.h"
+#include "ksort.cuh"
 
 namespace wc {
 
@@ -185,11 +186,7 @@ void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs
 }
 
 // ---------------------------------------------------------------- radix sort
-// LSD radix sort of each plane's values (64-bit orderable keys, 8-bit digits),
-// one CTA per plane.  Each thread owns a contiguous segment, so the scatter is
-// stable without in-tile ranking: position = base[d] + count of digit d in
-// earlier segments + count earlier in the own segment.  Passes whose digit is
-// the same for every key are skipped.  `cnt` holds 256 x blockDim counters.
+// Each plane's values as orderable 64-bit keys, sorted by one CTA (ksort.cuh).
 #define SORT_THREADS 512
 __global__ void __launch_bounds__(SORT_THREADS) k_plane_sort(const double *__restrict__ arena, const Plane *__restrict__ planes,
                                                              const int *__restrict__ plane_ids,
@@ -200,61 +197,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_plane_sort(const double *__res
     const Plane P = planes[plane_ids[blockIdx.x]];
     const long long n = (long long)P.w * P.h;
     unsigned long long *A = keys + key_off[blockIdx.x], *B = tmp + key_off[blockIdx.x];
-    unsigned int *cnt = counts + (size_t)blockIdx.x * 256 * SORT_THREADS;
-    const int T = blockDim.x, t = threadIdx.x;
-    const long long seg = (n + T - 1) / T, s0 = t * seg, s1 = min(n, s0 + seg);
     const double *src = arena + P.off;
-    for (long long i = t; i < n; i += T) A[i] = dkey(src[i]);
-    __shared__ unsigned int base[256];
-    __shared__ int skip;
-    __syncthreads();
-    for (int pass = 0; pass < 8; pass++) {
-        const int sh = pass * 8;
-        unsigned int local[256];
-        // count digits of the own segment (registers spill to local memory; fine)
-        for (int d = 0; d < 256; d++) local[d] = 0;
-        for (long long i = s0; i < s1; i++) local[(A[i] >> sh) & 255]++;
-        for (int d = 0; d < 256; d++) cnt[(size_t)d * T + t] = local[d];
-        __syncthreads();
-        // per digit: exclusive scan over threads, digit totals
-        if (t < 256) {
-            unsigned int run = 0;
-            for (int u = 0; u < T; u++) {
-                unsigned int v = cnt[(size_t)t * T + u];
-                cnt[(size_t)t * T + u] = run;
-                run += v;
-            }
-            base[t] = run;
-        }
-        if (t == 0) skip = 0;
-        __syncthreads();
-        if (t == 0) {
-            unsigned int run = 0;
-            for (int d = 0; d < 256; d++) {
-                unsigned int v = base[d];
-                if (v == (unsigned int)n) skip = 1;
-                base[d] = run;
-                run += v;
-            }
-        }
-        __syncthreads();
-        if (!skip) {
-            for (int d = 0; d < 256; d++) local[d] = base[d] + cnt[(size_t)d * T + t];
-            for (long long i = s0; i < s1; i++) {
-                unsigned long long k = A[i];
-                B[local[(k >> sh) & 255]++] = k;
-            }
-            __syncthreads();
-            unsigned long long *x = A;
-            A = B;
-            B = x;
-        }
-        __syncthreads();
-    }
-    // result must end in `keys`
-    if (A != keys + key_off[blockIdx.x]) {
-        for (long long i = t; i < n; i += T) B[i] = A[i];
-    }
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) A[i] = dkey(src[i]);
+    cta_radix_sort_u64(A, B, n, counts + (size_t)blockIdx.x * 256 * SORT_THREADS);
 }
 
 void launch_plane_sort(Ctx &c, const double *arena, const Plane *planes, const int *plane_ids, int n,

@@ -1,5 +1,7 @@
 // Host-side launchers of the CUDA kernels (one per family or transform).
 #pragma once
+#include <vector>
+
 #include "wc_internal.h"
 
 namespace wc {
@@ -72,5 +74,35 @@ struct HarJob {
 };
 void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
                      int njobs, const HarJob *hj, char *wsb, double *feat);
+
+// k_groupa.cu
+struct EFJob {
+    long long mag_ws, dir_ws;  // Prewitt magnitude / direction planes (doubles offsets)
+};
+void launch_edgefeat(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw, int maxh,
+                     const EFJob *ej, double *ws, const Plane *aux_planes, const int *aux_ids, PlaneStats *aux_stats,
+                     unsigned long long *keys, unsigned long long *tmp, const long long *koff, unsigned int *counts,
+                     double *feat);
+struct OBJob {
+    int inverse;  // 1: Inverse-Otsu (source = inverted plane at src_ws)
+    int pad_;
+    long long src_ws, lab_ws, area_ws, xm_ws, ym_ws, roots_ws, keys_ws, tmp_ws, dist_ws, cnt_ws;  // doubles offsets
+};
+void launch_objects(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs, int njobs,
+                    long long maxpix, const OBJob *oj, double *ws, const Plane *inv_planes, PlaneStats *inv_stats,
+                    double *thr, unsigned long long *acc, double *feat);
+
+// k_gabor.cu
+struct GabJob {
+    long long a_ws, c_ws, e_ws, g_ws;  // doubles offsets: image spectrum, product, 8 energy maps, kernel spectra
+    int fh, fw, plan_h, plan_w;
+};
+struct GabSize {
+    int fh, fw, plan_h, plan_w;
+    long long g_ws;
+};
+void launch_gabor(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, const GabJob *gj_d,
+                  const std::vector<GabJob> &gj, const std::vector<GabSize> &sizes, const FFTPlan *plans_d,
+                  const double *tabs, long long kern_tab, double *ws, double *counts, double *feat);
 
 }  // namespace wc

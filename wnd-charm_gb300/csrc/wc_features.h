@@ -22,6 +22,8 @@ struct FeatureSetup {
     // per-family results of the preparation (offsets into meta / ws)
     std::map<std::string, size_t> off;
     std::map<std::string, long long> val;
+    std::vector<GabJob> gab_jobs;
+    std::vector<GabSize> gab_sizes;
 };
 
 struct FeatureRun {

@@ -1,0 +1,281 @@
+#!/usr/bin/env python
+"""Benchmark: images/s of the 2919-feature (long) WND-CHARM plan on 512 x 512
+uint16 (12-bit) images, the blob + grating workload with 4 classes (seed 1).
+
+One step = one batch of B images through the whole plan.
+  value : device-resident form (inputs already in HBM, features left in HBM),
+          CUDA events on the engine's stream around each step, L2 flushed
+          between steps (outside the timed region);
+  e2e   : the public API with host buffers (pinned input images in, host
+          feature rows out), host<->device copies inside the timed region.
+--impl reference times the reference algorithm on the host CPU cores (the
+oracle port, one image per thread) on the same workload.
+
+Multi-GPU (torchrun): independent replicas, one per rank (the path shards by
+image); the slowest rank's time defines the step.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "wnd-charm_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "images/sec, 2919-feature set, 512^2 uint16 (long plan)"
+IMG = 512
+
+
+def clocks_sampler(stop, out):
+    cmd = ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits", "-i", os.environ.get("LOCAL_RANK", "0")]
+    while not stop.is_set():
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=5)
+            if r.returncode == 0 and r.stdout.strip():
+                out.append([x.strip() for x in r.stdout.strip().split(",")])
+        except Exception:
+            pass
+        stop.wait(0.2)
+
+
+def summarize_clocks(samples):
+    if not samples:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+    sm = [float(s[0]) for s in samples if s[0].replace(".", "").isdigit()]
+    mx = [float(s[1]) for s in samples if s[1].replace(".", "").isdigit()]
+    reasons = set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for s in samples:
+        for k, n in enumerate(names):
+            if len(s) > 4 + k and s[4 + k].lower().startswith("active"):
+                reasons.add(n)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons)}
+
+
+def make_images(n, seed=1):
+    from wndcharm import synth
+    per = (n + 3) // 4
+    imgs, _ = synth.config2(n_per_class=per, size=IMG, seed=seed)
+    order = [c * per + i for i in range(per) for c in range(4)][:n]  # interleave the classes
+    return [imgs[k] for k in order]
+
+
+def cpu_baseline(images, nthreads):
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+    ora = ctypes.CDLL(os.path.join(REPO, "oracle", "build", "libwc_oracle.so"))
+    n = len(images)
+    pix = np.concatenate([np.ascontiguousarray(a, dtype=np.float64).ravel() for a in images])
+    offs = np.cumsum([0] + [a.size for a in images[:-1]]).astype(np.int64)
+    ws = np.array([a.shape[1] for a in images], dtype=np.int32)
+    hs = np.array([a.shape[0] for a in images], dtype=np.int32)
+    out = np.zeros((n, 2919))
+    D = ctypes.POINTER(ctypes.c_double)
+    t0 = time.perf_counter()
+    ora.wco_extract_std_batch(1, pix.ctypes.data_as(D), offs.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                              ws.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                              hs.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n, 16, out.ctypes.data_as(D), nthreads)
+    dt = time.perf_counter() - t0
+    return n / dt, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    # each timed step: one image per host thread, bounded so the run stays within minutes
+    per_step = max(1, min(nthreads, int(nthreads * 150.0 / (max(1, args.steps) * 14.0))))
+    warm = make_images(1, seed=99)
+    for _ in range(args.warmup):
+        cpu_baseline([w[:64, :64] for w in warm], 1)
+    imgs = make_images(per_step)
+    tot_imgs, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        _, dt = cpu_baseline(imgs, min(nthreads, per_step))
+        tot_imgs += len(imgs)
+        tot_t += dt
+    v = tot_imgs / tot_t
+    line = {"metric": METRIC, "value": v, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "long plan (2919 features), %dx%d uint16 12-bit blob+grating, seed 1" % (IMG, IMG),
+                       "images_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": "images/s", "cores": min(nthreads, per_step), "kind": "port",
+                             "sample": "%d images of %dx%d per step, one per host thread" % (per_step, IMG, IMG)},
+            "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def stage_work(name, B):
+    """Algorithmic work per step of a stage on the long plan at 512^2, for the
+    roofline of the dominant stage: (kind, amount) with kind 'bytes' (HBM) or
+    'flops'."""
+    px = IMG * IMG
+    planes_c = 12  # group C runs on 12 planes per image
+    table = {
+        # read each plane once (8 B/px) for every pass the family needs
+        "Haralick Textures": ("bytes", B * planes_c * px * (8 + 1 + 1)),
+        "Tamura Textures": ("bytes", B * planes_c * px * 8 * 4),
+        "Gabor Textures": ("bytes", B * px * 8 * 2),
+        "Chebyshev": ("flops", B * 3 * 2 * 2 * IMG ** 3),
+        "Zernike Coefficients": ("flops", B * 8 * px * 460),
+        "Chebyshev-Fourier Coefficients": ("flops", B * 8 * int(0.785 * 300 * 300) * 529 * 4),
+        "Comb Moments": ("bytes", B * planes_c * px * 8),
+        "Radon Coefficients": ("bytes", B * planes_c * px * 8),
+        "Fractal Features": ("bytes", B * planes_c * px * 8),
+        "PixStats+Gini (sort)": ("bytes", B * planes_c * px * 8 * 16),
+    }
+    return table.get(name)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import wndcharm
+    B = args.batch
+    plan = wndcharm.StdFeatureComputationPlans.getFeatureSetLong()
+    nf = plan.n_features
+    eng = wndcharm.Engine(local, args.precision)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    imgs = make_images(B, seed=1 + rank)
+    host = torch.from_numpy(np.stack(imgs).view(np.int16)).pin_memory()
+    dev = host.to(f"cuda:{local}")
+    feat_dev = torch.empty((B, nf), dtype=torch.float64, device=f"cuda:{local}")
+    out_host = torch.empty((B, nf), dtype=torch.float64).pin_memory()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    descs_dev = (wndcharm._lib.wc_image_desc * B)()
+    descs_host = (wndcharm._lib.wc_image_desc * B)()
+    for i in range(B):
+        descs_dev[i] = wndcharm._lib.wc_image_desc(dev[i].data_ptr(), wndcharm._lib.WC_U16, IMG, IMG, 16, 1)
+        descs_host[i] = wndcharm._lib.wc_image_desc(host[i].data_ptr(), wndcharm._lib.WC_U16, IMG, IMG, 16, 0)
+    L = wndcharm.lib()
+
+    def step_dev():
+        wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_dev, B, ctypes.c_void_p(feat_dev.data_ptr()), 1))
+
+    def step_e2e():
+        wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_host, B, ctypes.c_void_p(out_host.data_ptr()), 0))
+
+    def timed(fn, k):
+        tot = 0.0
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            stream.synchronize()
+            if dist:
+                dist.barrier()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            tot += a.elapsed_time(b) / 1000.0
+        if dist:
+            t = torch.tensor([tot], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot
+
+    for _ in range(max(3, args.warmup)):
+        step_dev()
+    stream.synchronize()
+    stop, samples = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    l0 = eng.launches
+    t_dev = timed(step_dev, args.steps)
+    launches = eng.launches - l0
+    for _ in range(2):
+        step_e2e()
+    t_e2e = timed(step_e2e, args.steps)
+    stop.set()
+    th.join(timeout=10)
+    clocks = summarize_clocks(samples)
+
+    # per-stage profile (one extra step, outside the timed regions)
+    eng.profile(True)
+    step_dev()
+    stream.synchronize()
+    prof = eng.profile_report()
+    eng.profile(False)
+    tot_prof = sum(ms for _, ms, _ in prof) or 1.0
+    dom = max(prof, key=lambda r: r[1]) if prof else ("none", 0.0, 1)
+    peaks = {}
+    pk_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tfl = peaks.get("bf16_tflops", 1900.0)
+    work = stage_work(dom[0], B)
+    roof = {"stage": dom[0], "stage_ms_per_step": dom[1], "stage_share": dom[1] / tot_prof,
+            "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
+            "peak_source": "measured" if peaks else "fallback"}
+    if work:
+        kind, amt = work
+        sec = dom[1] / 1000.0
+        if kind == "bytes":
+            roof.update({"bound": "hbm", "achieved": amt / sec / 1e9, "peak": hbm, "unit": "GB/s"})
+        else:
+            roof.update({"bound": "tensor", "achieved": amt / sec / 1e12, "peak": tfl, "unit": "TFLOP/s"})
+        roof["frac"] = roof["achieved"] / roof["peak"]
+
+    value = world * B * args.steps / t_dev
+    e2e = world * B * args.steps / t_e2e
+    line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "mixed",
+            "data": "synthetic",
+            "config": {"workload": "long plan (2919 features), %dx%d uint16 12-bit blob+grating, 4 classes, seed 1"
+                       % (IMG, IMG), "images_per_step": B, "precision_form": args.precision,
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"},
+            "e2e": {"value": e2e, "unit": "images/s", "h2d_bytes_per_step": B * IMG * IMG * 2,
+                    "d2h_bytes_per_step": B * nf * 8},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "roofline": roof,
+            "stages_ms": {n: round(ms, 3) for n, ms, _ in prof}}
+    if rank == 0 and not args.no_cpu_baseline:
+        nth = os.cpu_count() or 1
+        v, dt = cpu_baseline(make_images(nth, seed=7), nth)
+        line["cpu_baseline"] = {"value": v, "unit": "images/s", "cores": nth, "kind": "port",
+                                "sample": "%d images of %dx%d, one per host thread, %.1f s" % (nth, IMG, IMG, dt)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

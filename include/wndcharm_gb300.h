@@ -88,6 +88,13 @@ void wc_engine_destroy(wc_engine *engine);
 int wc_engine_set_stream(wc_engine *engine, void *stream);
 /* kernels launched by this engine since creation (counts every launch) */
 long long wc_engine_launch_count(const wc_engine *engine);
+/* Per-stage timing (no reference counterpart; the reference prints a per-node
+ * TIME line at verbosity > 4, src/Tasks.cpp:208-253): while on, every
+ * transform and feature-family stage is bracketed by CUDA events on the
+ * engine's stream (this serialises nothing but adds events); the report lists
+ * "stage<TAB>milliseconds<TAB>calls" lines accumulated since the last switch. */
+int wc_engine_profile(wc_engine *engine, int on);
+int wc_engine_profile_report(wc_engine *engine, char *buf, int buflen);
 
 /* ---- feature extraction ----
  * FeatureComputationPlanExecutor::run for one image: writes plan->n_features

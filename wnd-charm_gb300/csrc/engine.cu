@@ -147,6 +147,7 @@ struct wc_engine {
     Tables tabs;
     std::vector<char> hmeta;
     std::mutex mu;
+    Prof prof;
 };
 
 namespace wc {
@@ -184,7 +185,7 @@ static int out_shape(int xf, int w, int h, int &ow, int &oh) {
 // Runs `plan` over `n` images; `dfeat` receives n x n_features on the device.
 int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, double *dfeat,
               std::vector<Plane> *planes_out = nullptr) {
-    Ctx ctx{E->st, &E->launches, E->prec, E->sms};
+    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof};
     // ---- nodes: every prefix of every group's transform chain
     std::vector<Node> nodes(1);
     nodes[0] = {-1, -1, 0, {}};
@@ -365,6 +366,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
                                cudaMemcpyHostToDevice, E->st));
             src = (char *)E->stage.p + in_off[b];
         }
+        ProfScope ps(ctx, "convert");
         launch_convert(ctx, src, I.dtype, arena + planes[(size_t)b * NN].off, (long long)I.width * I.height);
     }
     const Plane *dplanes = (const Plane *)(dm + m_planes);
@@ -378,6 +380,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
             TL &L = tl[d][x];
             const TJob *dj = (const TJob *)(dm + L.jobs);
             const int nj = (int)G.jobs.size();
+            ProfScope ps(ctx, kXfName[x]);
             if (x == X_EDGE) launch_edge(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh);
             else if (x == X_WAVELET)
                 launch_wavelet(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh, (double *)(dw + L.ws),
@@ -391,7 +394,10 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
                                  (const long long *)(dm + L.aux2), (double *)(dw + L.ws),
                                  (const long long *)(dm + L.aux1));
         }
-    launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats);
+    {
+        ProfScope ps(ctx, "plane stats");
+        launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats);
+    }
 
     FeatureRun fr;
     fr.ctx = &ctx;
@@ -508,6 +514,28 @@ int wc_engine_set_stream(wc_engine *E, void *stream) {
 
 long long wc_engine_launch_count(const wc_engine *E) { return E ? E->launches : 0; }
 
+int wc_engine_profile(wc_engine *E, int on) {
+    if (!E) return set_err(WC_ERR_ARG, "null engine");
+    E->prof.on = on != 0;
+    E->prof.order.clear();
+    E->prof.ms.clear();
+    E->prof.calls.clear();
+    return WC_OK;
+}
+
+int wc_engine_profile_report(wc_engine *E, char *buf, int buflen) {
+    if (!E || !buf || buflen < 1) return set_err(WC_ERR_ARG, "bad arguments");
+    std::string s;
+    char line[256];
+    for (size_t k = 0; k < E->prof.order.size(); k++) {
+        snprintf(line, sizeof line, "%s\t%.6f\t%lld\n", E->prof.order[k].c_str(), E->prof.ms[k], E->prof.calls[k]);
+        s += line;
+    }
+    strncpy(buf, s.c_str(), (size_t)buflen - 1);
+    buf[buflen - 1] = 0;
+    return (int)s.size();
+}
+
 int wc_extract_batch(wc_engine *E, const wc_plan *plan, const wc_image_desc *images, int n, double *out,
                      int out_on_device) {
     if (!E || !plan || !images || n < 1 || !out) return set_err(WC_ERR_ARG, "wc_extract_batch: bad arguments");
@@ -526,6 +554,10 @@ int wc_extract_batch(wc_engine *E, const wc_plan *plan, const wc_image_desc *ima
     if (!out_on_device) {
         CK(cudaMemcpyAsync(out, dfeat, fbytes, cudaMemcpyDeviceToHost, E->st));
         CK(cudaStreamSynchronize(E->st));
+    }
+    if (E->prof.on) {
+        CK(cudaStreamSynchronize(E->st));
+        E->prof.collect();
     }
     int dev_err = 0;
     if ((r = features_check(E->st, &dev_err))) return r;

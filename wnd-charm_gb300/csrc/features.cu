@@ -366,6 +366,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
     auto nj = [&](int a) { return (int)fj[a].size(); };
 
     if (fs.val.count("sort_n")) {
+        ProfScope ps(c, "PixStats+Gini (sort)");
         launch_plane_sort(c, fr.arena, fr.planes, (const int *)(fr.meta + fs.off["sort_ids"]), (int)fs.val["sort_n"],
                           (unsigned long long *)(fr.ws + fs.off["sort_keys"]),
                           (unsigned long long *)(fr.ws + fs.off["sort_tmp"]),
@@ -380,39 +381,70 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
             launch_gini(c, fr.planes, jobs(A_GINI), nj(A_GINI),
                         (const int *)(fr.meta + fs.off["slots" + std::to_string(A_GINI)]), keys, koff, fr.feat);
     }
-    if (nj(A_MSHIST)) launch_mshist(c, fr.arena, fr.planes, fr.stats, jobs(A_MSHIST), nj(A_MSHIST), fr.feat);
-    if (nj(A_FRACTAL)) launch_fractal(c, fr.arena, fr.planes, jobs(A_FRACTAL), nj(A_FRACTAL), fr.feat);
-    if (nj(A_COMB)) launch_comb(c, fr.arena, fr.planes, jobs(A_COMB), nj(A_COMB), fr.feat);
-    if (nj(A_RADON))
+    {
+        ProfScope ps(c, "Multiscale Histograms");
+        if (nj(A_MSHIST)) launch_mshist(c, fr.arena, fr.planes, fr.stats, jobs(A_MSHIST), nj(A_MSHIST), fr.feat);
+    }
+    {
+        ProfScope ps(c, "Fractal Features");
+        if (nj(A_FRACTAL)) launch_fractal(c, fr.arena, fr.planes, jobs(A_FRACTAL), nj(A_FRACTAL), fr.feat);
+    }
+    {
+        ProfScope ps(c, "Comb Moments");
+        if (nj(A_COMB)) launch_comb(c, fr.arena, fr.planes, jobs(A_COMB), nj(A_COMB), fr.feat);
+    }
+    {
+        ProfScope ps(c, "Radon Coefficients");
+        if (nj(A_RADON))
         launch_radon(c, fr.arena, fr.planes, jobs(A_RADON), nj(A_RADON), maxw_of(P, fj[A_RADON]), maxh_of(P, fj[A_RADON]),
                      fr.feat);
-    if (nj(A_CHEB))
+    }
+    {
+        ProfScope ps(c, "Chebyshev Coefficients");
+        if (nj(A_CHEB))
         launch_chebcoef(c, fr.arena, fr.planes, jobs(A_CHEB), nj(A_CHEB), fr.tabs,
                         (const long long *)(fr.meta + fs.off["cc_tab"]), (double *)(fr.ws + fs.off["cc_mid"]),
                         (const long long *)(fr.meta + fs.off["cc_moff"]), fr.feat);
-    if (nj(A_ZERNIKE))
+    }
+    {
+        ProfScope ps(c, "Zernike Coefficients");
+        if (nj(A_ZERNIKE))
         launch_zernike(c, fr.arena, fr.planes, jobs(A_ZERNIKE), nj(A_ZERNIKE), fs.val["zk_maxpix"],
                        (double *)(fr.ws + fs.off["zk_mom"]), (double *)(fr.ws + fs.off["zk_part"]), fr.feat);
-    if (nj(A_CHEBFOURIER))
+    }
+    {
+        ProfScope ps(c, "Chebyshev-Fourier Coefficients");
+        if (nj(A_CHEBFOURIER))
         launch_chebfourier(c, fr.arena, fr.planes, jobs(A_CHEBFOURIER), nj(A_CHEBFOURIER),
                            maxw_of(P, fj[A_CHEBFOURIER]), maxh_of(P, fj[A_CHEBFOURIER]), (int)fs.val["cf_cntx"],
                            (int)fs.val["cf_w"], (int)fs.val["cf_h"], (const CFJob *)(fr.meta + fs.off["cf_jobs"]), fr.tabs,
                            (double *)fr.ws, (double *)(fr.ws + fs.off["cf_part"]), (int)fs.val["cf_nchunk"], fr.feat);
-    if (nj(A_TAMURA))
+    }
+    {
+        ProfScope ps(c, "Tamura Textures");
+        if (nj(A_TAMURA))
         launch_tamura(c, fr.planes, fr.stats, fr.arena, jobs(A_TAMURA), nj(A_TAMURA),
                       (const TamJob *)(fr.meta + fs.off["tam_jobs"]), (double *)fr.ws,
                       (double *)(fr.ws + fs.off["tam_part"]), fs.val["tam_maxpix"], fr.feat);
-    if (nj(A_HARALICK))
+    }
+    {
+        ProfScope ps(c, "Haralick Textures");
+        if (nj(A_HARALICK))
         launch_haralick(c, fr.arena, fr.planes, fr.stats, jobs(A_HARALICK), nj(A_HARALICK),
                         (const HarJob *)(fr.meta + fs.off["har_jobs"]), fr.ws, fr.feat);
-    if (nj(A_EDGEF))
+    }
+    {
+        ProfScope ps(c, "Edge Features");
+        if (nj(A_EDGEF))
         launch_edgefeat(c, fr.arena, fr.planes, jobs(A_EDGEF), nj(A_EDGEF), maxw_of(P, fj[A_EDGEF]),
                         maxh_of(P, fj[A_EDGEF]), (const EFJob *)(fr.meta + fs.off["ef_jobs"]), (double *)fr.ws,
                         (const Plane *)(fr.meta + fs.off["ef_aux"]), (const int *)(fr.meta + fs.off["ef_ids"]),
                         (PlaneStats *)(fr.meta + fs.off["ef_stats"]), (unsigned long long *)(fr.ws + fs.off["ef_keys"]),
                         (unsigned long long *)(fr.ws + fs.off["ef_tmp"]), (const long long *)(fr.meta + fs.off["ef_koff"]),
                         (unsigned int *)(fr.ws + fs.off["ef_cnt"]), fr.feat);
+    }
     if (fs.val.count("ob_n")) {
+        ProfScope ps(c, "Object Features (Otsu + Inverse)");
         if (cudaMemsetAsync(fr.ws + fs.val["ob_zero_begin"], 0, (size_t)fs.val["ob_zero_bytes"], c.st) != cudaSuccess)
             return set_err(WC_ERR_CUDA, "memset failed");
         launch_objects(c, fr.arena, fr.planes, fr.stats, (const FJob *)(fr.meta + fs.off["ob_fjobs"]), (int)fs.val["ob_n"],
@@ -420,10 +452,13 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                        (const Plane *)(fr.meta + fs.off["ob_inv"]), (PlaneStats *)(fr.meta + fs.off["ob_invstats"]),
                        (double *)(fr.ws + fs.off["ob_thr"]), (unsigned long long *)(fr.ws + fs.off["ob_acc"]), fr.feat);
     }
-    if (nj(A_GABOR))
+    {
+        ProfScope ps(c, "Gabor Textures");
+        if (nj(A_GABOR))
         launch_gabor(c, fr.arena, fr.planes, jobs(A_GABOR), nj(A_GABOR), (const GabJob *)(fr.meta + fs.off["gab_jobs"]),
                      fs.gab_jobs, fs.gab_sizes, (const FFTPlan *)(fr.meta + fs.off["gab_plans"]), fr.tabs,
                      fs.val["gab_kern"], (double *)fr.ws, (double *)(fr.ws + fs.off["gab_counts"]), fr.feat);
+    }
     return WC_OK;
 }
 

@@ -46,12 +46,57 @@ struct TJob {
     int src, dst;
 };
 
+// Optional per-stage timing with CUDA events on the engine's stream.
+struct Prof {
+    bool on = false;
+    struct Mark {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> pending;
+    std::vector<std::string> order;
+    std::vector<double> ms;
+    std::vector<long long> calls;
+    void begin(const std::string &name, cudaStream_t st) {
+        if (!on) return;
+        Mark m{name, nullptr, nullptr};
+        cudaEventCreate(&m.a);
+        cudaEventCreate(&m.b);
+        cudaEventRecord(m.a, st);
+        pending.push_back(m);
+    }
+    void end(cudaStream_t st) {
+        if (!on || pending.empty() || !pending.back().b) return;
+        cudaEventRecord(pending.back().b, st);
+    }
+    void collect() {  // after the stream has been synchronised
+        for (auto &m : pending) {
+            float t = 0;
+            cudaEventElapsedTime(&t, m.a, m.b);
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+            size_t k = 0;
+            while (k < order.size() && order[k] != m.name) k++;
+            if (k == order.size()) { order.push_back(m.name); ms.push_back(0); calls.push_back(0); }
+            ms[k] += t;
+            calls[k] += 1;
+        }
+        pending.clear();
+    }
+};
+
 // Launch context handed to every kernel launcher.
 struct Ctx {
     cudaStream_t st;
     long long *launches;  // incremented per kernel launch
     int prec;             // WC_PREC_FP64 or WC_PREC_MIXED
     int sms;              // multiprocessors on the device
+    Prof *prof;
+};
+struct ProfScope {
+    Ctx &c;
+    ProfScope(Ctx &c_, const char *name) : c(c_) { if (c.prof) c.prof->begin(name, c.st); }
+    ~ProfScope() { if (c.prof) c.prof->end(c.st); }
 };
 
 }  // namespace wc

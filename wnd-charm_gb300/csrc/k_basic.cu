@@ -481,20 +481,48 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
     __syncthreads();
     const double cs = c_radon_cs[2 * ang], sn = c_radon_cs[2 * ang + 1];
     const double *p = arena + P.off;
-    const long long nsub = 4LL * W * H;
-    for (long long q = threadIdx.x; q < nsub; q += blockDim.x) {
-        const int nn = (int)(q / (2 * H)), mm = (int)(q - (long long)nn * 2 * H);
-        double pix = p[(long long)(mm / 2) * W + nn / 2];
-        if (pix != 0.0) {
+    // Sub-pixel lines along which the bin index is constant up to rounding:
+    // columns (0 deg), rows (90 deg), diagonals (45 deg), anti-diagonals (135 deg).
+    // Each sub-pixel's split is computed exactly as the reference does; a
+    // thread adds its run to shared memory only when the bin changes.
+    const int NX = 2 * W, NY = 2 * H;
+    int nlines, dn, dm;
+    if (ang == 0) { nlines = NX; dn = 0; dm = 1; }
+    else if (ang == 2) { nlines = NY; dn = 1; dm = 0; }
+    else if (ang == 1) { nlines = NX + NY - 1; dn = 1; dm = 1; }
+    else { nlines = NX + NY - 1; dn = 1; dm = -1; }
+    for (int line = threadIdx.x; line < nlines; line += blockDim.x) {
+        int n, m;
+        if (ang == 0) { n = line; m = 0; }
+        else if (ang == 2) { n = 0; m = line; }
+        else if (ang == 1) { if (line < NX) { n = line; m = 0; } else { n = 0; m = line - NX + 1; } }
+        else { if (line < NY) { n = 0; m = line; } else { n = line - NY + 1; m = NY - 1; } }
+        int cur = -1;
+        double lo = 0, hi = 0;
+        for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
+            double pix = p[(long long)(m / 2) * W + n / 2];
+            if (pix == 0.0) continue;
             pix *= 0.25;
-            const double xT = -xo - 0.25 + 0.5 * nn;                 // exact: multiples of 0.25
-            const double yT = -yo - 0.25 + 0.5 * (2 * H - 1 - mm);   // exact
-            const double xc = __dsub_rn(__dmul_rn(xT, cs), (double)rFirst);
-            const double ri = __dadd_rn(xc, __dmul_rn(yT, sn));
-            int rl = (int)ri;
+            const double xT = -xo - 0.25 + 0.5 * n;              // exact: multiples of 0.25
+            const double yT = -yo - 0.25 + 0.5 * (NY - 1 - m);   // exact
+            const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
+            const int rl = (int)ri;
             const double pl = __dmul_rn(pix, __dadd_rn(__dsub_rn(1.0, ri), (double)rl));
-            atomicAdd(&pr[rl], pl);
-            atomicAdd(&pr[rl + 1], __dsub_rn(pix, pl));
+            if (rl != cur) {
+                if (cur >= 0) {
+                    atomicAdd(&pr[cur], lo);
+                    atomicAdd(&pr[cur + 1], hi);
+                }
+                cur = rl;
+                lo = 0;
+                hi = 0;
+            }
+            lo += pl;
+            hi += __dsub_rn(pix, pl);
+        }
+        if (cur >= 0) {
+            atomicAdd(&pr[cur], lo);
+            atomicAdd(&pr[cur + 1], hi);
         }
     }
     __syncthreads();

@@ -251,20 +251,14 @@ __device__ void hh_right_par(double *A, int ld, int r0, int m, int c0, int nc, c
     }
 }
 
-__global__ void __launch_bounds__(256) k_har_f14(const FJob *__restrict__ jobs, const HarJob *__restrict__ hj,
+__global__ void __launch_bounds__(256) k_har_qhess(const FJob *__restrict__ jobs, const HarJob *__restrict__ hj,
                                                  char *__restrict__ wsb) {
     __shared__ double px[256], py[256], v[256], ess[256];
     __shared__ double s_tau, s_beta;
-    __shared__ int s_cmd, s_il, s_im, s_iu;
-    __shared__ double s_sh[3], s_fv[3], s_exshift;
     const int ang = blockIdx.y;
     const HarJob H = hj[blockIdx.x];
     const int n = ((const int *)(wsb + H.lut_b))[256];
-    double *res = (double *)(wsb + H.res_b) + ang * 14;
-    if (n < 3) {
-        if (threadIdx.x == 0) res[13] = 0.0;
-        return;
-    }
+    if (n < 3) return;
     const double *P = (const double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256;
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
     // marginals as the oracle computes them (sequential sums)
@@ -317,195 +311,239 @@ __global__ void __launch_bounds__(256) k_har_f14(const FJob *__restrict__ jobs, 
         if (c < r - 1) A[q] = 0;
     }
     __syncthreads();
-#define T_(r, c) A[(long long)(r) * n + (c)]
-    // norm of T (computeNormOfT)
-    if (threadIdx.x == 0) {
-        double norm = 0;
-        for (int j = 0; j < n; j++) {
-            const int s0 = j - 1 > 0 ? j - 1 : 0;
-            double s = 0;
-            for (int c = s0; c < n; c++) s += fabs(T_(j, c));
-            norm += s;
-        }
-        s_sh[0] = norm;
-        s_exshift = 0;
+}
+
+// Real-Schur QR iteration of one Hessenberg matrix per warp (RealSchur::compute,
+// src/Eigen/src/Eigenvalues/RealSchur.h:204-463), then eigenvalue #2.
+// Every update is restricted to the active window [il, iu]: the reflectors act
+// on rows/columns independently, so the window's entries get exactly the
+// operations they get from the full-width updates, and entries outside the
+// window are never read again (columns > iu are deflated, the block above il
+// is decoupled).  All lanes take the same decisions from the same (broadcast)
+// values; lane-parallel loops run over the columns/rows of a reflector.
+#define QR_WARPS 4
+__global__ void __launch_bounds__(32 * QR_WARPS) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb, int nmat) {
+    __shared__ double rowsum[QR_WARPS][256];
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    const int m = blockIdx.x * QR_WARPS + wq;
+    if (m >= nmat) return;
+    const int job = m >> 2, ang = m & 3;
+    const HarJob H = hj[job];
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    double *res = (double *)(wsb + H.res_b) + ang * 14;
+    if (n < 3) {
+        if (lane == 0) res[13] = 0.0;
+        return;
     }
-    __syncthreads();
-    const double norm = s_sh[0];
+    double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
+#define T_(r, c) A[(long long)(r) * n + (c)]
+    // computeNormOfT: row sums (sequential within a row), then rows in order
+    for (int j = lane; j < n; j += 32) {
+        const int s0 = j - 1 > 0 ? j - 1 : 0;
+        double s = 0;
+        for (int c = s0; c < n; c++) s = __dadd_rn(s, fabs(T_(j, c)));
+        rowsum[wq][j] = s;
+    }
+    __syncwarp();
+    double norm = 0;
+    for (int j = 0; j < n; j++) norm = __dadd_rn(norm, rowsum[wq][j]);
     const double eps = DBL_EPSILON;
     const int maxIter = 40 * n;
     int iu = n - 1, iter = 0, totalIter = 0;
+    double exshift = 0;
     bool failed = false;
     if (norm != 0) {
         while (iu >= 0) {
-            // thread 0 decides; others follow the broadcast command
-            if (threadIdx.x == 0) {
-                int il = iu;
-                while (il > 0) {
-                    double s = fabs(T_(il - 1, il - 1)) + fabs(T_(il, il));
-                    if (s == 0.0) s = norm;
-                    if (fabs(T_(il, il - 1)) < eps * s) break;
-                    il--;
+            // findSmallSubdiagEntry: first il (downwards from iu) with a negligible T(il, il-1)
+            int il = 0;
+            for (int base = iu; base > 0; base -= 32) {
+                const int r = base - lane;
+                bool hit = false;
+                if (r > 0) {
+                    double sm = __dadd_rn(fabs(T_(r - 1, r - 1)), fabs(T_(r, r)));
+                    if (sm == 0.0) sm = norm;
+                    hit = fabs(T_(r, r - 1)) < __dmul_rn(eps, sm);
                 }
-                s_il = il;
-                if (il == iu) {
-                    T_(iu, iu) = T_(iu, iu) + s_exshift;
-                    if (iu > 0) T_(iu, iu - 1) = 0;
-                    s_cmd = 0;
-                } else if (il == iu - 1) {
-                    const double p = 0.5 * (T_(iu - 1, iu - 1) - T_(iu, iu));
-                    const double q = p * p + T_(iu, iu - 1) * T_(iu - 1, iu);
-                    T_(iu, iu) += s_exshift;
-                    T_(iu - 1, iu - 1) += s_exshift;
-                    if (q >= 0) {
-                        const double z = sqrt(fabs(q));
-                        const double gp = (p >= 0) ? p + z : p - z, gq = T_(iu, iu - 1);
-                        double c, s;
-                        if (gq == 0) { c = gp < 0 ? -1 : 1; s = 0; }
-                        else if (gp == 0) { c = 0; s = gq < 0 ? 1 : -1; }
-                        else if (fabs(gp) > fabs(gq)) {
-                            const double t = gq / gp;
-                            double u = sqrt(1 + t * t);
-                            if (gp < 0) u = -u;
-                            c = 1 / u;
-                            s = -t * c;
-                        } else {
-                            const double t = gp / gq;
-                            double u = sqrt(1 + t * t);
-                            if (gq < 0) u = -u;
-                            s = -1 / u;
-                            c = -t * s;
-                        }
-                        s_sh[0] = c;
-                        s_sh[1] = s;
-                        s_cmd = 1;
-                    } else {
-                        s_cmd = 2;
-                    }
-                } else {
-                    double sh0 = T_(iu, iu), sh1 = T_(iu - 1, iu - 1), sh2 = T_(iu, iu - 1) * T_(iu - 1, iu);
-                    if (iter == 10) {
-                        s_exshift += sh0;
-                        for (int i = 0; i <= iu; i++) T_(i, i) -= sh0;
-                        const double s = fabs(T_(iu, iu - 1)) + fabs(T_(iu - 1, iu - 2));
-                        sh0 = 0.75 * s;
-                        sh1 = 0.75 * s;
-                        sh2 = -0.4375 * s * s;
-                    }
-                    if (iter == 30) {
-                        double s = (sh1 - sh0) / 2.0;
-                        s = s * s + sh2;
-                        if (s > 0) {
-                            s = sqrt(s);
-                            if (sh1 < sh0) s = -s;
-                            s = s + (sh1 - sh0) / 2.0;
-                            s = sh0 - sh2 / s;
-                            s_exshift += s;
-                            for (int i = 0; i <= iu; i++) T_(i, i) -= s;
-                            sh0 = sh1 = sh2 = 0.964;
-                        }
-                    }
-                    double fv0 = 0, fv1 = 0, fv2 = 0;
-                    int im;
-                    for (im = iu - 2; im >= il; --im) {
-                        const double Tmm = T_(im, im), r = sh0 - Tmm, s = sh1 - Tmm;
-                        fv0 = (r * s - sh2) / T_(im + 1, im) + T_(im, im + 1);
-                        fv1 = T_(im + 1, im + 1) - Tmm - r - s;
-                        fv2 = T_(im + 2, im + 1);
-                        if (im == il) break;
-                        const double lhs = T_(im, im - 1) * (fabs(fv1) + fabs(fv2));
-                        const double rhs = fv0 * (fabs(T_(im - 1, im - 1)) + fabs(Tmm) + fabs(T_(im + 1, im + 1)));
-                        if (fabs(lhs) < eps * rhs) break;
-                    }
-                    s_im = im;
-                    s_fv[0] = fv0;
-                    s_fv[1] = fv1;
-                    s_fv[2] = fv2;
-                    s_cmd = 3;
+                const unsigned b = __ballot_sync(0xffffffffu, hit);
+                if (b) {
+                    il = base - (__ffs(b) - 1);
+                    break;
                 }
             }
-            __syncthreads();
-            const int cmd = s_cmd;
-            if (cmd == 0) {
+            if (il == iu) {
+                __syncwarp();
+                if (lane == 0) {
+                    T_(iu, iu) = __dadd_rn(T_(iu, iu), exshift);
+                    if (iu > 0) T_(iu, iu - 1) = 0;
+                }
+                __syncwarp();
                 iu--;
                 iter = 0;
-            } else if (cmd == 1 || cmd == 2) {
-                if (cmd == 1) {
-                    const double c = s_sh[0], s = s_sh[1];
-                    for (int col = iu - 1 + threadIdx.x; col < n; col += blockDim.x) {
-                        const double xi = T_(iu - 1, col), yi = T_(iu, col);
-                        T_(iu - 1, col) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
-                        T_(iu, col) = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
-                    }
-                    __syncthreads();
-                    for (int row = threadIdx.x; row <= iu; row += blockDim.x) {
-                        const double xi = T_(row, iu - 1), yi = T_(row, iu);
-                        T_(row, iu - 1) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
-                        T_(row, iu) = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
-                    }
-                    __syncthreads();
-                    if (threadIdx.x == 0) T_(iu, iu - 1) = 0;
+            } else if (il == iu - 1) {
+                const double p = __dmul_rn(0.5, __dsub_rn(T_(iu - 1, iu - 1), T_(iu, iu)));
+                const double q = __dadd_rn(__dmul_rn(p, p), __dmul_rn(T_(iu, iu - 1), T_(iu - 1, iu)));
+                __syncwarp();
+                if (lane == 0) {
+                    T_(iu, iu) = __dadd_rn(T_(iu, iu), exshift);
+                    T_(iu - 1, iu - 1) = __dadd_rn(T_(iu - 1, iu - 1), exshift);
                 }
-                if (threadIdx.x == 0 && iu > 1) T_(iu - 1, iu - 2) = 0;
-                __syncthreads();
+                __syncwarp();
+                if (q >= 0) {
+                    const double z = sqrt(fabs(q));
+                    const double gp = (p >= 0) ? __dadd_rn(p, z) : __dsub_rn(p, z), gq = T_(iu, iu - 1);
+                    double c, s;
+                    if (gq == 0) { c = gp < 0 ? -1 : 1; s = 0; }
+                    else if (gp == 0) { c = 0; s = gq < 0 ? 1 : -1; }
+                    else if (fabs(gp) > fabs(gq)) {
+                        const double t = gq / gp;
+                        double u = sqrt(__dadd_rn(1.0, __dmul_rn(t, t)));
+                        if (gp < 0) u = -u;
+                        c = 1 / u;
+                        s = __dmul_rn(-t, c);
+                    } else {
+                        const double t = gp / gq;
+                        double u = sqrt(__dadd_rn(1.0, __dmul_rn(t, t)));
+                        if (gq < 0) u = -u;
+                        s = -1 / u;
+                        c = __dmul_rn(-t, s);
+                    }
+                    // the 2x2 block: left (rows iu-1, iu), then right (cols iu-1, iu)
+                    if (lane == 0) {
+                        for (int col = iu - 1; col <= iu; col++) {
+                            const double xi = T_(iu - 1, col), yi = T_(iu, col);
+                            T_(iu - 1, col) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
+                            T_(iu, col) = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
+                        }
+                        for (int row = iu - 1; row <= iu; row++) {
+                            const double xi = T_(row, iu - 1), yi = T_(row, iu);
+                            T_(row, iu - 1) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
+                            T_(row, iu) = __dadd_rn(__dmul_rn(s, xi), __dmul_rn(c, yi));
+                        }
+                        T_(iu, iu - 1) = 0;
+                    }
+                }
+                if (lane == 0 && iu > 1) T_(iu - 1, iu - 2) = 0;
+                __syncwarp();
                 iu -= 2;
                 iter = 0;
             } else {
+                double sh0 = T_(iu, iu), sh1 = T_(iu - 1, iu - 1), sh2 = __dmul_rn(T_(iu, iu - 1), T_(iu - 1, iu));
+                if (iter == 10) {
+                    exshift = __dadd_rn(exshift, sh0);
+                    __syncwarp();
+                    for (int i = lane; i <= iu; i += 32) T_(i, i) = __dsub_rn(T_(i, i), sh0);
+                    __syncwarp();
+                    const double s = __dadd_rn(fabs(T_(iu, iu - 1)), fabs(T_(iu - 1, iu - 2)));
+                    sh0 = __dmul_rn(0.75, s);
+                    sh1 = __dmul_rn(0.75, s);
+                    sh2 = __dmul_rn(__dmul_rn(-0.4375, s), s);
+                }
+                if (iter == 30) {
+                    double s = __dsub_rn(sh1, sh0) / 2.0;
+                    s = __dadd_rn(__dmul_rn(s, s), sh2);
+                    if (s > 0) {
+                        s = sqrt(s);
+                        if (sh1 < sh0) s = -s;
+                        s = __dadd_rn(s, __dsub_rn(sh1, sh0) / 2.0);
+                        s = __dsub_rn(sh0, sh2 / s);
+                        exshift = __dadd_rn(exshift, s);
+                        __syncwarp();
+                        for (int i = lane; i <= iu; i += 32) T_(i, i) = __dsub_rn(T_(i, i), s);
+                        __syncwarp();
+                        sh0 = sh1 = sh2 = 0.964;
+                    }
+                }
                 iter++;
                 totalIter++;
                 if (totalIter > maxIter) {
                     failed = true;
                     break;
                 }
-                const int il = s_il, im = s_im;
+                // initFrancisQRStep
+                double fv0 = 0, fv1 = 0, fv2 = 0;
+                int im;
+                for (im = iu - 2; im >= il; --im) {
+                    const double Tmm = T_(im, im), r = __dsub_rn(sh0, Tmm), s = __dsub_rn(sh1, Tmm);
+                    fv0 = __dadd_rn(__dsub_rn(__dmul_rn(r, s), sh2) / T_(im + 1, im), T_(im, im + 1));
+                    fv1 = __dsub_rn(__dsub_rn(__dsub_rn(T_(im + 1, im + 1), Tmm), r), s);
+                    fv2 = T_(im + 2, im + 1);
+                    if (im == il) break;
+                    const double lhs = __dmul_rn(T_(im, im - 1), __dadd_rn(fabs(fv1), fabs(fv2)));
+                    const double rhs = __dmul_rn(fv0, __dadd_rn(__dadd_rn(fabs(T_(im - 1, im - 1)), fabs(Tmm)),
+                                                                fabs(T_(im + 1, im + 1))));
+                    if (fabs(lhs) < __dmul_rn(eps, rhs)) break;
+                }
+                // performFrancisQRStep, restricted to the window
                 for (int k = im; k <= iu - 2; ++k) {
                     const bool first = (k == im);
-                    if (threadIdx.x == 0) {
-                        double vv[3];
-                        if (first) { vv[0] = s_fv[0]; vv[1] = s_fv[1]; vv[2] = s_fv[2]; }
-                        else { vv[0] = T_(k, k - 1); vv[1] = T_(k + 1, k - 1); vv[2] = T_(k + 2, k - 1); }
-                        double tau, beta;
-                        hh_make(vv, 3, ess, tau, beta);
-                        s_tau = tau;
-                        s_beta = beta;
-                        if (beta != 0) {
+                    double vv[3], ess[2], tau, beta;
+                    if (first) { vv[0] = fv0; vv[1] = fv1; vv[2] = fv2; }
+                    else { vv[0] = T_(k, k - 1); vv[1] = T_(k + 1, k - 1); vv[2] = T_(k + 2, k - 1); }
+                    hh_make(vv, 3, ess, tau, beta);
+                    __syncwarp();
+                    if (beta != 0) {
+                        if (lane == 0) {
                             if (first && k > il) T_(k, k - 1) = -T_(k, k - 1);
                             else if (!first) T_(k, k - 1) = beta;
                         }
+                        for (int cc = k + lane; cc <= iu; cc += 32) {  // left: rows k..k+2
+                            const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
+                            double t = __dadd_rn(__dmul_rn(ess[0], a1), 0.0);
+                            t = __dadd_rn(t, __dmul_rn(ess[1], a2));
+                            t = __dadd_rn(t, a0);
+                            T_(k, cc) = __dsub_rn(a0, __dmul_rn(tau, t));
+                            T_(k + 1, cc) = __dsub_rn(a1, __dmul_rn(__dmul_rn(tau, ess[0]), t));
+                            T_(k + 2, cc) = __dsub_rn(a2, __dmul_rn(__dmul_rn(tau, ess[1]), t));
+                        }
+                        __syncwarp();
+                        const int rend = min(iu, k + 3);
+                        for (int rr = il + lane; rr <= rend; rr += 32) {  // right: cols k..k+2
+                            const double b0 = T_(rr, k), b1 = T_(rr, k + 1), b2 = T_(rr, k + 2);
+                            double t = __dadd_rn(__dmul_rn(b1, ess[0]), 0.0);
+                            t = __dadd_rn(t, __dmul_rn(b2, ess[1]));
+                            t = __dadd_rn(t, b0);
+                            const double tt = __dmul_rn(tau, t);
+                            T_(rr, k) = __dsub_rn(b0, tt);
+                            T_(rr, k + 1) = __dsub_rn(b1, __dmul_rn(tt, ess[0]));
+                            T_(rr, k + 2) = __dsub_rn(b2, __dmul_rn(tt, ess[1]));
+                        }
                     }
-                    __syncthreads();
-                    if (s_beta != 0) {
-                        hh_left_par(A, n, k, 3, k, n - k, ess, s_tau);
-                        __syncthreads();
-                        hh_right_par(A, n, 0, min(iu, k + 3) + 1, k, 3, ess, s_tau);
-                    }
-                    __syncthreads();
+                    __syncwarp();
                 }
-                if (threadIdx.x == 0) {
-                    double vv[2] = {T_(iu - 1, iu - 2), T_(iu, iu - 2)};
-                    double tau, beta;
+                {
+                    double vv[2] = {T_(iu - 1, iu - 2), T_(iu, iu - 2)}, ess[1], tau, beta;
                     hh_make(vv, 2, ess, tau, beta);
-                    s_tau = tau;
-                    s_beta = beta;
-                    if (beta != 0) T_(iu - 1, iu - 2) = beta;
-                }
-                __syncthreads();
-                if (s_beta != 0) {
-                    hh_left_par(A, n, iu - 1, 2, iu - 1, n - iu + 1, ess, s_tau);
-                    __syncthreads();
-                    hh_right_par(A, n, 0, iu + 1, iu - 1, 2, ess, s_tau);
-                }
-                __syncthreads();
-                if (threadIdx.x == 0)
-                    for (int i = im + 2; i <= iu; ++i) {
-                        T_(i, i - 2) = 0;
-                        if (i > im + 2) T_(i, i - 3) = 0;
+                    __syncwarp();
+                    if (beta != 0) {
+                        if (lane == 0) T_(iu - 1, iu - 2) = beta;
+                        for (int cc = iu - 1 + lane; cc <= iu; cc += 32) {
+                            const double a0 = T_(iu - 1, cc), a1 = T_(iu, cc);
+                            double t = __dadd_rn(__dmul_rn(ess[0], a1), 0.0);
+                            t = __dadd_rn(t, a0);
+                            T_(iu - 1, cc) = __dsub_rn(a0, __dmul_rn(tau, t));
+                            T_(iu, cc) = __dsub_rn(a1, __dmul_rn(__dmul_rn(tau, ess[0]), t));
+                        }
+                        __syncwarp();
+                        for (int rr = il + lane; rr <= iu; rr += 32) {
+                            const double b0 = T_(rr, iu - 1), b1 = T_(rr, iu);
+                            double t = __dadd_rn(__dmul_rn(b1, ess[0]), 0.0);
+                            t = __dadd_rn(t, b0);
+                            const double tt = __dmul_rn(tau, t);
+                            T_(rr, iu - 1) = __dsub_rn(b0, tt);
+                            T_(rr, iu) = __dsub_rn(b1, __dmul_rn(tt, ess[0]));
+                        }
                     }
-                __syncthreads();
+                    __syncwarp();
+                }
+                for (int i = im + 2 + lane; i <= iu; i += 32) {
+                    T_(i, i - 2) = 0;
+                    if (i > im + 2) T_(i, i - 3) = 0;
+                }
+                __syncwarp();
             }
         }
     }
-    if (threadIdx.x == 0) {
+    if (lane == 0) {
         double f = 0;
         if (!failed) {
             // eigenvalue #2 in Schur order (EigenSolver::compute, EigenSolver.h:363-381)
@@ -516,9 +554,9 @@ __global__ void __launch_bounds__(256) k_har_f14(const FJob *__restrict__ jobs, 
                     if (i == 2) { re2 = T_(i, i); im2 = 0; }
                     ++i;
                 } else {
-                    const double p = 0.5 * (T_(i, i) - T_(i + 1, i + 1));
-                    const double z = sqrt(fabs(p * p + T_(i + 1, i) * T_(i, i + 1)));
-                    if (i == 2 || i + 1 == 2) { re2 = T_(i + 1, i + 1) + p; im2 = (i == 2) ? z : -z; }
+                    const double p = __dmul_rn(0.5, __dsub_rn(T_(i, i), T_(i + 1, i + 1)));
+                    const double z = sqrt(fabs(__dadd_rn(__dmul_rn(p, p), __dmul_rn(T_(i + 1, i), T_(i, i + 1)))));
+                    if (i == 2 || i + 1 == 2) { re2 = __dadd_rn(T_(i + 1, i + 1), p); im2 = (i == 2) ? z : -z; }
                     i += 2;
                 }
             }
@@ -566,7 +604,9 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     WC_LAUNCH(c);
     k_har_stats<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
     WC_LAUNCH(c);
-    k_har_f14<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
+    k_har_qhess<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
+    WC_LAUNCH(c);
+    k_har_qr<<<(4 * njobs + QR_WARPS - 1) / QR_WARPS, 32 * QR_WARPS, 0, c.st>>>(hj, wsb, 4 * njobs);
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);
 }

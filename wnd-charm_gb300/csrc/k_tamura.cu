@@ -166,17 +166,26 @@ __global__ void __launch_bounds__(1024) k_tam_final(const Plane *__restrict__ pl
     const unsigned char *sb = (const unsigned char *)(ws + T.sbest_ws);
     const double *phi = ws + T.phi_ws, *nrm = ws + T.norm_ws;
     const double ssc = hist_scale(kmin, kmax, 3), psc = hist_scale(pmn, pmx, 125);
+    // contrast moments skip NaN and |v| > FLT_MAX, as Moments4::add does
     double s1 = 0;
+    long long cnt = 0;
     for (long long i = threadIdx.x; i < n; i += blockDim.x) {
         atomicAdd(&hs[hist_bin((double)sb[i], kmin, ssc, 3)], 1u);
         atomicAdd(&hp[hist_bin(phi[i], pmn, psc, 125)], 1u);
-        s1 += nrm[i];
+        const double v = nrm[i];
+        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;
+        s1 += v;
+        cnt++;
     }
     s1 = block_sum(s1, sh);
-    const double mean = s1 / (double)n;
+    __shared__ long long shl[32];
+    cnt = block_sum_ll(cnt, shl);
+    const double mean = cnt ? s1 / (double)cnt : 0.0;
     double m2 = 0, m4 = 0;
     for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-        const double d = nrm[i] - mean, d2 = d * d;
+        const double v = nrm[i];
+        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;
+        const double d = v - mean, d2 = d * d;
         m2 += d2;
         m4 += d2 * d2;
     }
@@ -197,9 +206,9 @@ __global__ void __launch_bounds__(1024) k_tam_final(const Plane *__restrict__ pl
         double sum = 0;
         for (int a = 0; a < 125; a++) sum += (double)hp[a] * pow((double)(a + 1 - fmx), 2);
         const double dir = fabs(log(sum / sr + 0.0000001));
-        const double nn = (double)n;
-        const double sd = n > 2 ? sqrt(m2 / (nn - 1)) : 0.0;
-        const double kurt = n > 4 ? (nn * m4) / (m2 * m2) : 0.0;
+        const double nn = (double)cnt;
+        const double sd = cnt > 2 ? sqrt(m2 / (nn - 1)) : 0.0;
+        const double kurt = cnt > 4 ? (nn * m4) / (m2 * m2) : 0.0;
         const double con = (sd < DBL_EPSILON) ? 0 : sd / pow(kurt / pow(sd, 4), 0.25);
         double *o = feat + J.out;
         o[0] = hs[0] / hm;

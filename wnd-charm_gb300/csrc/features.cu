@@ -108,12 +108,21 @@ int features_prepare(FeatureSetup &fs) {
             koff.push_back((long long)tot);
             tot += ((size_t)P[p].w * P[p].h + 31) & ~(size_t)31;
         }
+        std::vector<SortSeg> seg;
+        long long maxn = 0;
+        for (size_t k = 0; k < sort_planes.size(); k++) {
+            const long long n = (long long)P[sort_planes[k]].w * P[sort_planes[k]].h;
+            seg.push_back({koff[k], n});
+            maxn = std::max(maxn, n);
+        }
         fs.off["sort_ids"] = fs.put_copy(sort_planes.data(), sort_planes.size() * sizeof(int));
         fs.off["sort_koff"] = fs.put_copy(koff.data(), koff.size() * sizeof(long long));
+        fs.off["sort_seg"] = fs.put_copy(seg.data(), seg.size() * sizeof(SortSeg));
         fs.off["sort_keys"] = fs.ws_take(tot * 8);
         fs.off["sort_tmp"] = fs.ws_take(tot * 8);
-        fs.off["sort_cnt"] = fs.ws_take(sort_planes.size() * 256 * 512 * sizeof(unsigned int));
+        fs.off["sort_cnt"] = fs.ws_take(sort_scratch_bytes((int)sort_planes.size(), maxn));
         fs.val["sort_n"] = (long long)sort_planes.size();
+        fs.val["sort_maxn"] = maxn;
         for (int a : {A_PIXSTATS, A_GINI}) {
             std::vector<int> slots;
             for (auto &j : fj[a]) slots.push_back(slot_of[j.plane]);
@@ -249,11 +258,19 @@ int features_prepare(FeatureSetup &fs) {
         fs.off["ef_jobs"] = fs.put_copy(ej.data(), ej.size() * sizeof(EFJob));
         fs.off["ef_aux"] = fs.put_copy(aux.data(), aux.size() * sizeof(Plane));
         fs.off["ef_ids"] = fs.put_copy(ids.data(), ids.size() * sizeof(int));
+        std::vector<SortSeg> seg;
+        long long maxn = 0;
+        for (size_t k = 0; k < aux.size(); k++) {
+            seg.push_back({koff[k], (long long)aux[k].w * aux[k].h});
+            maxn = std::max(maxn, (long long)aux[k].w * aux[k].h);
+        }
         fs.off["ef_koff"] = fs.put_copy(koff.data(), koff.size() * sizeof(long long));
+        fs.off["ef_seg"] = fs.put_copy(seg.data(), seg.size() * sizeof(SortSeg));
         fs.off["ef_stats"] = fs.meta_take(aux.size() * sizeof(PlaneStats));
         fs.off["ef_keys"] = fs.ws_take(ktot * 8);
         fs.off["ef_tmp"] = fs.ws_take(ktot * 8);
-        fs.off["ef_cnt"] = fs.ws_take(aux.size() * 256 * 512 * sizeof(unsigned int));
+        fs.off["ef_cnt"] = fs.ws_take(sort_scratch_bytes((int)aux.size(), maxn));
+        fs.val["ef_maxn"] = maxn;
     }
 
     // Otsu / Inverse-Otsu object features (one job list for both)
@@ -367,11 +384,10 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
 
     if (fs.val.count("sort_n")) {
         ProfScope ps(c, "PixStats+Gini (sort)");
-        launch_plane_sort(c, fr.arena, fr.planes, (const int *)(fr.meta + fs.off["sort_ids"]), (int)fs.val["sort_n"],
-                          (unsigned long long *)(fr.ws + fs.off["sort_keys"]),
-                          (unsigned long long *)(fr.ws + fs.off["sort_tmp"]),
-                          (const long long *)(fr.meta + fs.off["sort_koff"]),
-                          (unsigned int *)(fr.ws + fs.off["sort_cnt"]));
+        launch_sort_planes(c, fr.arena, fr.planes, (const int *)(fr.meta + fs.off["sort_ids"]),
+                           (const SortSeg *)(fr.meta + fs.off["sort_seg"]), (int)fs.val["sort_n"], fs.val["sort_maxn"],
+                           (unsigned long long *)(fr.ws + fs.off["sort_keys"]),
+                           (unsigned long long *)(fr.ws + fs.off["sort_tmp"]), fr.ws + fs.off["sort_cnt"]);
         const unsigned long long *keys = (const unsigned long long *)(fr.ws + fs.off["sort_keys"]);
         const long long *koff = (const long long *)(fr.meta + fs.off["sort_koff"]);
         if (nj(A_PIXSTATS))
@@ -441,7 +457,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                         (const Plane *)(fr.meta + fs.off["ef_aux"]), (const int *)(fr.meta + fs.off["ef_ids"]),
                         (PlaneStats *)(fr.meta + fs.off["ef_stats"]), (unsigned long long *)(fr.ws + fs.off["ef_keys"]),
                         (unsigned long long *)(fr.ws + fs.off["ef_tmp"]), (const long long *)(fr.meta + fs.off["ef_koff"]),
-                        (unsigned int *)(fr.ws + fs.off["ef_cnt"]), fr.feat);
+                        (const SortSeg *)(fr.meta + fs.off["ef_seg"]), fs.val["ef_maxn"], fr.ws + fs.off["ef_cnt"], fr.feat);
     }
     if (fs.val.count("ob_n")) {
         ProfScope ps(c, "Object Features (Otsu + Inverse)");

@@ -105,13 +105,13 @@ __global__ void __launch_bounds__(512) k_ef_final(const Plane *__restrict__ plan
 
 void launch_edgefeat(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw, int maxh,
                      const EFJob *ej, double *ws, const Plane *aux_planes, const int *aux_ids, PlaneStats *aux_stats,
-                     unsigned long long *keys, unsigned long long *tmp, const long long *koff, unsigned int *counts,
-                     double *feat) {
+                     unsigned long long *keys, unsigned long long *tmp, const long long *koff, const SortSeg *seg,
+                     long long maxn, void *scratch, double *feat) {
     if (njobs <= 0) return;
     WC_LAUNCH(c);
     k_ef_prewitt<<<dim3((maxw + 31) / 32, (maxh + 7) / 8, njobs), dim3(32, 8), 0, c.st>>>(arena, planes, jobs, ej, ws);
     launch_plane_stats(c, ws, aux_planes, 2 * njobs, aux_stats);
-    launch_plane_sort(c, ws, aux_planes, aux_ids, 2 * njobs, keys, tmp, koff, counts);
+    launch_sort_planes(c, ws, aux_planes, aux_ids, seg, 2 * njobs, maxn, keys, tmp, scratch);
     WC_LAUNCH(c);
     k_ef_final<<<njobs, 512, 0, c.st>>>(planes, jobs, ej, ws, aux_stats, keys, koff, feat);
 }

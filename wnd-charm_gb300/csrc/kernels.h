@@ -29,6 +29,14 @@ void launch_radon(Ctx &c, const double *arena, const Plane *planes, const FJob *
 void launch_chebcoef(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, const double *tabs,
                      const long long *tab_off, double *mid_ws, const long long *mid_off, double *feat);
 
+// k_sort.cu: multi-CTA radix sort of many arrays of 64-bit keys
+struct SortSeg {
+    long long off, n;  // offset and length of the array in the key buffers
+};
+size_t sort_scratch_bytes(int nseg, long long max_n);
+void launch_sort_planes(Ctx &c, const double *arena, const Plane *planes, const int *ids, const SortSeg *seg, int nseg,
+                        long long max_n, unsigned long long *keys, unsigned long long *tmp, void *scratch);
+
 // k_fft.cu: 1-D complex DFTs of any length <= kMaxFFT, batched, in shared memory
 const int kMaxFFT = 4096;
 struct FFTPlan {  // device description of one length
@@ -81,8 +89,8 @@ struct EFJob {
 };
 void launch_edgefeat(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw, int maxh,
                      const EFJob *ej, double *ws, const Plane *aux_planes, const int *aux_ids, PlaneStats *aux_stats,
-                     unsigned long long *keys, unsigned long long *tmp, const long long *koff, unsigned int *counts,
-                     double *feat);
+                     unsigned long long *keys, unsigned long long *tmp, const long long *koff, const SortSeg *seg,
+                     long long maxn, void *scratch, double *feat);
 struct OBJob {
     int inverse;  // 1: Inverse-Otsu (source = inverted plane at src_ws)
     int pad_;

@@ -1,13 +1,19 @@
 #!/usr/bin/env python
 """Benchmark: images/s of the 2919-feature (long) WND-CHARM plan on 512 x 512
-uint16 (12-bit) images, the blob + grating workload with 4 classes (seed 1).
+uint16 (12-bit) images, the blob + grating workload with 4 classes (seed 1):
+the batched mixed-precision form against the plain per-image FP64 form.
 
 One step = one batch of B images through the whole plan.
-  value : device-resident form (inputs already in HBM, features left in HBM),
-          CUDA events on the engine's stream around each step, L2 flushed
-          between steps (outside the timed region);
-  e2e   : the public API with host buffers (pinned input images in, host
-          feature rows out), host<->device copies inside the timed region.
+  value : batched mixed-precision form, device-resident (inputs already in HBM,
+          features left in HBM), CUDA events on the engine's stream around each
+          step, L2 flushed between steps (outside the timed region);
+  e2e   : the same form through the public API with host buffers (pinned input
+          images in, host feature rows out), host<->device copies inside the
+          timed region;
+  forms : the FP64 form batched, and per image (one image per call, the
+          plain per-image FP64 GPU form), on the same images.
+The cpu_baseline leg runs the oracle on the first images of the batch and
+reports the mixed form's per-family error against it.
 --impl reference times the reference algorithm on the host CPU cores (the
 oracle port, one image per thread) on the same workload.
 
@@ -29,7 +35,7 @@ sys.path.insert(0, os.path.join(REPO, "wnd-charm_gb300"))
 
 import numpy as np  # noqa: E402
 
-METRIC = "images/sec, 2919-feature set, 512^2 uint16 (long plan)"
+METRIC = "images/sec, 2919-feature set, 512^2 uint16: mixed vs FP64 GPU form at stated tol"
 IMG = 512
 
 
@@ -87,7 +93,7 @@ def cpu_baseline(images, nthreads):
                               ws.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                               hs.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n, 16, out.ctypes.data_as(D), nthreads)
     dt = time.perf_counter() - t0
-    return n / dt, dt
+    return n / dt, dt, out
 
 
 def run_reference(args, rank, world):
@@ -102,7 +108,7 @@ def run_reference(args, rank, world):
     imgs = make_images(per_step)
     tot_imgs, tot_t = 0, 0.0
     for _ in range(args.steps):
-        _, dt = cpu_baseline(imgs, min(nthreads, per_step))
+        _, dt, _ = cpu_baseline(imgs, min(nthreads, per_step))
         tot_imgs += len(imgs)
         tot_t += dt
     v = tot_imgs / tot_t
@@ -126,7 +132,11 @@ def stage_work(name, B):
     planes_c = 12  # group C runs on 12 planes per image
     table = {
         # read each plane once (8 B/px) for every pass the family needs
-        "Haralick Textures": ("bytes", B * planes_c * px * (8 + 1 + 1)),
+        # FP64 operations of Q, the Hessenberg reduction and the real-Schur QR for
+        # f14, counted by an instrumented run of the oracle on this workload
+        # (about 1.3 G per 512^2 image: 10/3 Ng^3 + 9 per touched element per
+        # Francis step + 3 per nonzero Q term, summed over the 48 matrices)
+        "Haralick Textures": ("fp64", B * 1.3e9),
         "Tamura Textures": ("bytes", B * planes_c * px * 8 * 4),
         "Gabor Textures": ("bytes", B * px * 8 * 2),
         "Chebyshev": ("flops", B * 3 * 2 * 2 * IMG ** 3),
@@ -140,6 +150,25 @@ def stage_work(name, B):
     return table.get(name)
 
 
+def fp64_peak_tflops(dev):
+    """FP64 roof for the FP64-pipe stages, measured live: cuBLAS DGEMM 4096^3,
+    best of 5 (CUDA events)."""
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1000.0
+        best = t if best is None else min(best, t)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -147,8 +176,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=32)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--per-image", type=int, default=8, help="images timed one per call in the FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the FP64 comparison forms")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -158,6 +189,7 @@ def main():
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -166,24 +198,25 @@ def main():
     B = args.batch
     plan = wndcharm.StdFeatureComputationPlans.getFeatureSetLong()
     nf = plan.n_features
-    eng = wndcharm.Engine(local, args.precision)
     stream = torch.cuda.Stream()
+    eng = wndcharm.Engine(local, args.precision)
     eng.set_stream(stream.cuda_stream)
     imgs = make_images(B, seed=1 + rank)
     host = torch.from_numpy(np.stack(imgs).view(np.int16)).pin_memory()
-    dev = host.to(f"cuda:{local}")
-    feat_dev = torch.empty((B, nf), dtype=torch.float64, device=f"cuda:{local}")
+    dev_imgs = host.to(dev)
+    feat_dev = torch.empty((B, nf), dtype=torch.float64, device=dev)
     out_host = torch.empty((B, nf), dtype=torch.float64).pin_memory()
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
-    descs_dev = (wndcharm._lib.wc_image_desc * B)()
-    descs_host = (wndcharm._lib.wc_image_desc * B)()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    W = wndcharm._lib
+    descs_dev = (W.wc_image_desc * B)()
+    descs_host = (W.wc_image_desc * B)()
     for i in range(B):
-        descs_dev[i] = wndcharm._lib.wc_image_desc(dev[i].data_ptr(), wndcharm._lib.WC_U16, IMG, IMG, 16, 1)
-        descs_host[i] = wndcharm._lib.wc_image_desc(host[i].data_ptr(), wndcharm._lib.WC_U16, IMG, IMG, 16, 0)
+        descs_dev[i] = W.wc_image_desc(dev_imgs[i].data_ptr(), W.WC_U16, IMG, IMG, 16, 1)
+        descs_host[i] = W.wc_image_desc(host[i].data_ptr(), W.WC_U16, IMG, IMG, 16, 0)
     L = wndcharm.lib()
 
-    def step_dev():
-        wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_dev, B, ctypes.c_void_p(feat_dev.data_ptr()), 1))
+    def step_dev(e=eng, n=B, descs=descs_dev):
+        wndcharm.check(L.wc_extract_batch(e._h, plan.handle, descs, n, ctypes.c_void_p(feat_dev.data_ptr()), 1))
 
     def step_e2e():
         wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_host, B, ctypes.c_void_p(out_host.data_ptr()), 0))
@@ -203,7 +236,7 @@ def main():
             b.synchronize()
             tot += a.elapsed_time(b) / 1000.0
         if dist:
-            t = torch.tensor([tot], device=f"cuda:{local}")
+            t = torch.tensor([tot], device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tot = float(t.item())
         return tot
@@ -223,6 +256,32 @@ def main():
     stop.set()
     th.join(timeout=10)
     clocks = summarize_clocks(samples)
+    mixed_rows = out_host.numpy().copy()
+
+    # the FP64 form on the same images: batched, and one image per call
+    forms = None
+    if not args.no_forms:
+        e64 = wndcharm.Engine(local, "fp64")
+        e64.set_stream(stream.cuda_stream)
+        step64 = lambda: step_dev(e64, B, descs_dev)  # noqa: E731
+        step64()
+        ks = max(1, min(args.steps, 2))
+        t64 = timed(step64, ks)
+        npi = max(1, min(args.per_image, B))
+        one = (W.wc_image_desc * 1)()
+        one[0] = descs_dev[0]
+        step_dev(e64, 1, one)
+        tpi = 0.0
+        for i in range(npi):
+            one[0] = descs_dev[i]
+            tpi += timed(lambda: step_dev(e64, 1, one), 1)
+        v_mixed = world * B * args.steps / t_dev
+        forms = {"mixed_batched": v_mixed, "fp64_batched": world * B * ks / t64,
+                 "fp64_per_image": world * npi / tpi,
+                 "mixed_vs_fp64_per_image": v_mixed / (world * npi / tpi),
+                 "mixed_vs_fp64_batched": v_mixed / (world * B * ks / t64),
+                 "fp64_per_image_sample": "%d images, one wc_extract_batch call each" % npi}
+        del e64
 
     # per-stage profile (one extra step, outside the timed regions)
     eng.profile(True)
@@ -247,6 +306,10 @@ def main():
         sec = dom[1] / 1000.0
         if kind == "bytes":
             roof.update({"bound": "hbm", "achieved": amt / sec / 1e9, "peak": hbm, "unit": "GB/s"})
+        elif kind == "fp64":
+            p64 = fp64_peak_tflops(dev)
+            roof.update({"bound": "fp64", "achieved": amt / sec / 1e12, "peak": p64, "unit": "TFLOP/s",
+                         "peak_source": "measured live: cuBLAS DGEMM 4096^3"})
         else:
             roof.update({"bound": "tensor", "achieved": amt / sec / 1e12, "peak": tfl, "unit": "TFLOP/s"})
         roof["frac"] = roof["achieved"] / roof["peak"]
@@ -255,7 +318,7 @@ def main():
     e2e = world * B * args.steps / t_e2e
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "mixed",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic",
             "config": {"workload": "long plan (2919 features), %dx%d uint16 12-bit blob+grating, 4 classes, seed 1"
                        % (IMG, IMG), "images_per_step": B, "precision_form": args.precision,
@@ -265,12 +328,31 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clocks,
             "roofline": roof,
+            "forms": forms,
             "stages_ms": {n: round(ms, 3) for n, ms, _ in prof}}
     if rank == 0 and not args.no_cpu_baseline:
         nth = os.cpu_count() or 1
-        v, dt = cpu_baseline(make_images(nth, seed=7), nth)
+        ncpu = min(nth, B)
+        v, dt, ref = cpu_baseline(imgs[:ncpu], nth)
         line["cpu_baseline"] = {"value": v, "unit": "images/s", "cores": nth, "kind": "port",
-                                "sample": "%d images of %dx%d, one per host thread, %.1f s" % (nth, IMG, IMG, dt)}
+                                "sample": "%d images of %dx%d (the first of the batch), one per host thread, %.1f s"
+                                % (ncpu, IMG, IMG, dt)}
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        from parity import compare_mixed, family_errors, compare
+        names = open(os.path.join(REPO, "tests", "golden", "names_long.txt")).read().splitlines()
+        errs, ok = {}, True
+        for i in range(ncpu):
+            fam = family_errors(mixed_rows[i], ref[i], names)
+            for k, (r, g, w) in fam.items():
+                r0, g0, w0 = errs.get(k, (0.0, 0.0, ""))
+                errs[k] = (max(r0, r), max(g0, g), w if g >= g0 else w0)
+            cmp = compare_mixed if args.precision == "mixed" else compare
+            if cmp(mixed_rows[i], ref[i], names):
+                ok = False
+        line["error_vs_oracle"] = {"images": ncpu, "tolerances_met": ok,
+                                   "max_rel": {k: float("%.3g" % v[0]) for k, v in sorted(errs.items())},
+                                   "max_rel_to_group_max": {k: float("%.3g" % v[1]) for k, v in sorted(errs.items())},
+                                   "worst": {k: v[2] for k, v in sorted(errs.items()) if v[1] > 0}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

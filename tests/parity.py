@@ -63,3 +63,70 @@ def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=2, skip=()):
             j = np.nonzero(bad)[0]
             fails[g] = ("float", j[:8].tolist(), va[j[:4]].tolist(), vb[j[:4]].tolist())
     return fails
+
+
+# Mixed-precision form: families whose kernels compute in FP32 carry their own
+# stated tolerance; every other family keeps the FP64 rules above.
+#   ("float", rtol, gtol): |a-b| <= rtol*|b| + gtol*max|group|
+#   ("counts", moves):     at most `moves` single-count moves per group
+MIXED_RULES = {
+    "Chebyshev-Fourier Coefficients": ("counts", 3),
+}
+
+
+def compare_mixed(a, b, names, rtol=1e-7, atol=1e-9, count_moves=2, skip=()):
+    """compare() with the mixed form's per-family tolerances."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    fails = compare(a, b, names, rtol, atol, count_moves, skip=tuple(skip) + tuple(MIXED_RULES))
+    groups = {}
+    for i, n in enumerate(names):
+        groups.setdefault(group_of(n), []).append(i)
+    for g, idx in groups.items():
+        alg = g.split(" (")[0]
+        if alg not in MIXED_RULES or any(g.startswith(s) for s in skip):
+            continue
+        rule = MIXED_RULES[alg]
+        va, vb = a[idx], b[idx]
+        if rule[0] == "counts":
+            d = np.abs(va - vb)
+            if not ((np.abs(np.round(d) - d) < 1e-9).all() and d.sum() <= 2 * rule[1]):
+                fails[g] = ("counts", d.sum(), np.nonzero(d)[0][:8])
+        else:
+            scale = np.max(np.abs(vb)) if len(vb) else 0.0
+            bad = np.abs(va - vb) > rule[1] * np.abs(vb) + rule[2] * scale
+            if bad.any():
+                j = np.nonzero(bad)[0]
+                fails[g] = ("float", j[:8].tolist(), va[j[:4]].tolist(), vb[j[:4]].tolist())
+    return fails
+
+
+def family_errors(a, b, names):
+    """Per family (algorithm name): max |a-b| / max(|b|, 1e-300) over entries
+    and max |a-b| / max|group|, for reporting."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    out = {}
+    groups = {}
+    for i, n in enumerate(names):
+        groups.setdefault(group_of(n), []).append(i)
+    for g, idx in groups.items():
+        alg = g.split(" (")[0]
+        va, vb = a[idx], b[idx]
+        if alg == "Haralick Textures":
+            keep = np.array([index_of(names[i]) not in F14 for i in idx])
+            va, vb = va[keep], vb[keep]
+        fin = np.isfinite(va) & np.isfinite(vb)
+        va, vb = va[fin], vb[fin]
+        if not len(va):
+            continue
+        d = np.abs(va - vb)
+        relv = d / np.maximum(np.abs(vb), 1e-300)
+        rel = float(np.max(relv))
+        grel = float(np.max(d) / max(np.max(np.abs(vb)), 1e-300))
+        r0, g0, w0 = out.get(alg, (0.0, 0.0, ""))
+        if grel > g0:
+            k = int(np.argmax(d))
+            w0 = "%s (%.6g vs %.6g)" % (g, va[k], vb[k])
+        out[alg] = (max(r0, rel), max(g0, grel), w0)
+    return out

@@ -148,6 +148,8 @@ struct wc_engine {
     std::vector<char> hmeta;
     std::mutex mu;
     Prof prof;
+    cudaStream_t lanes[WC_LANES] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[WC_LANES] = {};
 };
 
 namespace wc {
@@ -408,7 +410,21 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     fr.ws = dw;
     fr.tabs = E->tabs.d();
     fr.feat = dfeat;
+    // the feature families are independent given the planes: fork them onto the
+    // engine's lane streams and join back before the caller's next operation
+    Ctx lc[WC_LANES];
+    CK(cudaEventRecord(E->fork_ev, ctx.st));
+    for (int k = 0; k < WC_LANES; k++) {
+        lc[k] = ctx;
+        lc[k].st = E->lanes[k];
+        CK(cudaStreamWaitEvent(E->lanes[k], E->fork_ev, 0));
+    }
+    fr.lanes = lc;
     r = features_launch(fs, fr);
+    for (int k = 0; k < WC_LANES; k++) {
+        CK(cudaEventRecord(E->join_ev[k], E->lanes[k]));
+        CK(cudaStreamWaitEvent(ctx.st, E->join_ev[k], 0));
+    }
     if (r) return r;
     CK(cudaGetLastError());
     if (planes_out) *planes_out = planes;
@@ -495,6 +511,11 @@ int wc_engine_create(int device, int precision, wc_engine **out) {
     }
     set_radon_table(cs);
     features_init();
+    for (int k = 0; k < WC_LANES; k++) {
+        CK(cudaStreamCreateWithFlags(&E->lanes[k], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&E->join_ev[k], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&E->fork_ev, cudaEventDisableTiming));
     *out = E;
     return WC_OK;
 }
@@ -503,6 +524,11 @@ void wc_engine_destroy(wc_engine *E) {
     if (!E) return;
     cudaSetDevice(E->dev);
     cudaStreamSynchronize(E->st);
+    for (int k = 0; k < WC_LANES; k++) {
+        if (E->lanes[k]) cudaStreamDestroy(E->lanes[k]);
+        if (E->join_ev[k]) cudaEventDestroy(E->join_ev[k]);
+    }
+    if (E->fork_ev) cudaEventDestroy(E->fork_ev);
     delete E;
 }
 

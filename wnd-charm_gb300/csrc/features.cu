@@ -230,9 +230,11 @@ int features_prepare(FeatureSetup &fs) {
             h.glcm_b = (long long)fs.ws_take(4 * 256 * 256 * 8);
             h.q_b = (long long)fs.ws_take(4 * 256 * 256 * 8);
             h.res_b = (long long)fs.ws_take(4 * 14 * 8);
+            h.mar_b = (long long)fs.ws_take(4 * HAR_MAR_BYTES);
             hj.push_back(h);
         }
         fs.off["har_jobs"] = fs.put_copy(hj.data(), hj.size() * sizeof(HarJob));
+        fs.off["har_perm"] = fs.ws_take(4 * hj.size() * sizeof(int));
     }
     // Edge features: magnitude / direction planes in the workspace, sorted copies
     if (!fj[A_EDGEF].empty()) {
@@ -353,15 +355,27 @@ int features_prepare(FeatureSetup &fs) {
             for (size_t k = 0; k < sizes.size(); k++)
                 if (sizes[k].fh == g.fh && sizes[k].fw == g.fw) si = (int)k;
             if (si < 0) {
-                GabSize S{g.fh, g.fw, g.plan_h, g.plan_w, (long long)(fs.ws_take((size_t)8 * g.fh * g.fw * 16) / 8)};
+                GabSize S{g.fh, g.fw, g.plan_h, g.plan_w, (long long)(fs.ws_take((size_t)8 * g.fh * g.fw * 16) / 8), 0, 0, 0};
                 sizes.push_back(S);
                 si = (int)sizes.size() - 1;
             }
             g.g_ws = sizes[si].g_ws;
+            sizes[si].count++;
             gj.push_back(g);
         }
-        for (auto &g : gj) g.a_ws = (long long)(fs.ws_take((size_t)g.fh * g.fw * 16) / 8);
-        for (auto &g : gj) g.c_ws = (long long)(fs.ws_take((size_t)g.fh * g.fw * 16) / 8);
+        // per padded size, the jobs' spectra and 8 products in contiguous blocks
+        for (auto &S : sizes) {
+            const long long arr = (long long)S.fh * S.fw * 2;  // doubles per complex array
+            S.a_ws = (long long)(fs.ws_take((size_t)S.count * arr * 8) / 8);
+            S.c_ws = (long long)(fs.ws_take((size_t)S.count * 8 * arr * 8) / 8);
+            int k = 0;
+            for (auto &g : gj)
+                if (g.fh == S.fh && g.fw == S.fw) {
+                    g.a_ws = S.a_ws + k * arr;
+                    g.c_ws = S.c_ws + (long long)k * 8 * arr;
+                    k++;
+                }
+        }
         for (size_t k = 0; k < gj.size(); k++) {
             const Plane &Q = P[fj[A_GABOR][k].plane];
             gj[k].e_ws = (long long)(fs.ws_take((size_t)8 * Q.w * Q.h * 8) / 8);
@@ -378,9 +392,20 @@ int features_prepare(FeatureSetup &fs) {
 int features_launch(FeatureSetup &fs, FeatureRun &fr) {
     const auto &P = *fs.planes;
     const auto &fj = *fs.fj;
-    Ctx &c = *fr.ctx;
+    // lanes: 0 Haralick; 1 Zernike, Chebyshev-Fourier; 2 Tamura, Chebyshev coefficients;
+    // 3 Gabor; 4 objects, edge features; 5 sorts and the plane scans
+    Ctx &c = fr.lanes[5];
     auto jobs = [&](int a) { return (const FJob *)(fr.meta + fs.off["jobs" + std::to_string(a)]); };
     auto nj = [&](int a) { return (int)fj[a].size(); };
+    // the longest dependent chain (Haralick f14) is issued first
+    {
+        Ctx &c = fr.lanes[0];
+        ProfScope ps(c, "Haralick Textures");
+        if (nj(A_HARALICK))
+        launch_haralick(c, fr.arena, fr.planes, fr.stats, jobs(A_HARALICK), nj(A_HARALICK),
+                        (const HarJob *)(fr.meta + fs.off["har_jobs"]), fr.ws, (int *)(fr.ws + fs.off["har_perm"]),
+                        fr.feat);
+    }
 
     if (fs.val.count("sort_n")) {
         ProfScope ps(c, "PixStats+Gini (sort)");
@@ -416,6 +441,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                      fr.feat);
     }
     {
+        Ctx &c = fr.lanes[2];
         ProfScope ps(c, "Chebyshev Coefficients");
         if (nj(A_CHEB))
         launch_chebcoef(c, fr.arena, fr.planes, jobs(A_CHEB), nj(A_CHEB), fr.tabs,
@@ -423,12 +449,14 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                         (const long long *)(fr.meta + fs.off["cc_moff"]), fr.feat);
     }
     {
+        Ctx &c = fr.lanes[1];
         ProfScope ps(c, "Zernike Coefficients");
         if (nj(A_ZERNIKE))
         launch_zernike(c, fr.arena, fr.planes, jobs(A_ZERNIKE), nj(A_ZERNIKE), fs.val["zk_maxpix"],
                        (double *)(fr.ws + fs.off["zk_mom"]), (double *)(fr.ws + fs.off["zk_part"]), fr.feat);
     }
     {
+        Ctx &c = fr.lanes[1];
         ProfScope ps(c, "Chebyshev-Fourier Coefficients");
         if (nj(A_CHEBFOURIER))
         launch_chebfourier(c, fr.arena, fr.planes, jobs(A_CHEBFOURIER), nj(A_CHEBFOURIER),
@@ -437,6 +465,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                            (double *)fr.ws, (double *)(fr.ws + fs.off["cf_part"]), (int)fs.val["cf_nchunk"], fr.feat);
     }
     {
+        Ctx &c = fr.lanes[2];
         ProfScope ps(c, "Tamura Textures");
         if (nj(A_TAMURA))
         launch_tamura(c, fr.planes, fr.stats, fr.arena, jobs(A_TAMURA), nj(A_TAMURA),
@@ -444,12 +473,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                       (double *)(fr.ws + fs.off["tam_part"]), fs.val["tam_maxpix"], fr.feat);
     }
     {
-        ProfScope ps(c, "Haralick Textures");
-        if (nj(A_HARALICK))
-        launch_haralick(c, fr.arena, fr.planes, fr.stats, jobs(A_HARALICK), nj(A_HARALICK),
-                        (const HarJob *)(fr.meta + fs.off["har_jobs"]), fr.ws, fr.feat);
-    }
-    {
+        Ctx &c = fr.lanes[4];
         ProfScope ps(c, "Edge Features");
         if (nj(A_EDGEF))
         launch_edgefeat(c, fr.arena, fr.planes, jobs(A_EDGEF), nj(A_EDGEF), maxw_of(P, fj[A_EDGEF]),
@@ -460,6 +484,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                         (const SortSeg *)(fr.meta + fs.off["ef_seg"]), fs.val["ef_maxn"], fr.ws + fs.off["ef_cnt"], fr.feat);
     }
     if (fs.val.count("ob_n")) {
+        Ctx &c = fr.lanes[4];
         ProfScope ps(c, "Object Features (Otsu + Inverse)");
         if (cudaMemsetAsync(fr.ws + fs.val["ob_zero_begin"], 0, (size_t)fs.val["ob_zero_bytes"], c.st) != cudaSuccess)
             return set_err(WC_ERR_CUDA, "memset failed");
@@ -469,6 +494,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
                        (double *)(fr.ws + fs.off["ob_thr"]), (unsigned long long *)(fr.ws + fs.off["ob_acc"]), fr.feat);
     }
     {
+        Ctx &c = fr.lanes[3];
         ProfScope ps(c, "Gabor Textures");
         if (nj(A_GABOR))
         launch_gabor(c, fr.arena, fr.planes, jobs(A_GABOR), nj(A_GABOR), (const GabJob *)(fr.meta + fs.off["gab_jobs"]),

@@ -18,17 +18,19 @@
 namespace wc {
 
 // batched 1-D complex DFTs: arrays blockIdx.y, line groups blockIdx.x; element
-// k of line l at data + arr*js + l*ls + k*es.  conj_in/conj_out conjugate on
-// load/store; scale multiplies on store.
-__global__ void k_cfft_lines(double *__restrict__ data, long long js, int nl, int n, long long ls, long long es,
+// k of line l at data + arr*js + l*ls + k*es (units of complex elements).
+// R = double is the FP64 form, R = float the mixed form.
+template <typename R>
+__global__ void k_cfft_lines(R *__restrict__ data, long long js, int nl, int n, long long ls, long long es,
                              const FFTPlan *__restrict__ plan, const double *__restrict__ twd, int lpc) {
-    extern __shared__ double smem[];
+    typedef cpx<R> C;
+    extern __shared__ __align__(16) unsigned char fsm[];
     const FFTPlan P = *plan;
     const int l0 = blockIdx.x * lpc;
     if (l0 >= nl) return;
     const int lines = min(lpc, nl - l0);
-    cplx *base = (cplx *)data + (long long)blockIdx.y * js;
-    cplx *b0 = (cplx *)smem, *b1 = b0 + (long long)lpc * n;
+    C *base = (C *)data + (long long)blockIdx.y * js;
+    C *b0 = (C *)fsm, *b1 = b0 + (long long)lpc * n;
     const cplx *tw = (const cplx *)(twd + P.tw_off);
     if (es == 1) {
         for (int i = threadIdx.x; i < lines * n; i += blockDim.x) {
@@ -42,7 +44,7 @@ __global__ void k_cfft_lines(double *__restrict__ data, long long js, int nl, in
         }
     }
     __syncthreads();
-    const cplx *r = stockham(b0, b1, lines, P, tw) ? b1 : b0;
+    const C *r = stockham<R>(b0, b1, lines, P, tw) ? b1 : b0;
     if (es == 1) {
         for (int i = threadIdx.x; i < lines * n; i += blockDim.x) {
             const int l = i / n, k = i - l * n;
@@ -56,79 +58,95 @@ __global__ void k_cfft_lines(double *__restrict__ data, long long js, int nl, in
     }
 }
 
-// forward 2-D DFT of `na` arrays of fh x fw complex values (row-major), in place
-void cfft2(Ctx &c, double *data, int na, int fh, int fw, const FFTPlan *plan_w, const FFTPlan *plan_h, const double *tw) {
+// forward 2-D DFT, in place, of `na` arrays of fh x fw complex values (row-major)
+// spaced fh * fw * 16 bytes apart (the workspace is laid out for the FP64 form)
+template <typename R>
+static void cfft2(Ctx &c, double *data, int na, int fh, int fw, const FFTPlan *plan_w, const FFTPlan *plan_h,
+                  const double *tw) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_cfft_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_cfft_lines<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
-    const long long js = (long long)fh * fw;
-    int lpc = 96 * 1024 / (32 * fw);
+    const int es = 2 * sizeof(R);
+    const long long js = (long long)fh * fw * 16 / es;
+    int lpc = 96 * 1024 / (2 * es * fw);
     lpc = lpc < 1 ? 1 : (lpc > 8 ? 8 : lpc);
     WC_LAUNCH(c);
-    k_cfft_lines<<<dim3((fh + lpc - 1) / lpc, na), 256, (size_t)lpc * fw * 32, c.st>>>(data, js, fh, fw, fw, 1, plan_w, tw, lpc);
-    int lpc2 = 96 * 1024 / (32 * fh);
+    k_cfft_lines<R><<<dim3((fh + lpc - 1) / lpc, na), 256, (size_t)lpc * fw * 2 * es, c.st>>>((R *)data, js, fh, fw, fw, 1,
+                                                                                            plan_w, tw, lpc);
+    int lpc2 = 96 * 1024 / (2 * es * fh);
     lpc2 = lpc2 < 1 ? 1 : (lpc2 > 8 ? 8 : lpc2);
     WC_LAUNCH(c);
-    k_cfft_lines<<<dim3((fw + lpc2 - 1) / lpc2, na), 256, (size_t)lpc2 * fh * 32, c.st>>>(data, js, fw, fh, 1, fw, plan_h, tw,
-                                                                                        lpc2);
+    k_cfft_lines<R><<<dim3((fw + lpc2 - 1) / lpc2, na), 256, (size_t)lpc2 * fh * 2 * es, c.st>>>((R *)data, js, fw, fh, 1, fw,
+                                                                                               plan_h, tw, lpc2);
 }
 
 // zero-padded image (job) into a fh x fw complex array
+template <typename R>
 __global__ void k_gab_pad(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                           const GabJob *__restrict__ gj, double *__restrict__ ws) {
     const FJob J = jobs[blockIdx.y];
     const GabJob G = gj[blockIdx.y];
     const Plane P = planes[J.plane];
-    cplx *A = (cplx *)(ws + G.a_ws);
+    cpx<R> *A = (cpx<R> *)(ws + G.a_ws);
     const long long n = (long long)G.fh * G.fw;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int y = (int)(i / G.fw), x = (int)(i - (long long)y * G.fw);
-        A[i] = {(y < P.h && x < P.w) ? arena[P.off + (long long)y * P.w + x] : 0.0, 0.0};
+        A[i] = {(R)((y < P.h && x < P.w) ? arena[P.off + (long long)y * P.w + x] : 0.0), (R)0};
     }
 }
 
 // the 8 kernels (38 x 38 complex, host-made) zero-padded to fh x fw
-__global__ void k_gab_padk(const double *__restrict__ kern, double *__restrict__ G, int fh, int fw) {
+template <typename R>
+__global__ void k_gab_padk(const double *__restrict__ kern, double *__restrict__ Gd, int fh, int fw) {
     const int f = blockIdx.y;
-    cplx *g = (cplx *)G + (long long)f * fh * fw;
+    const long long fstride = (long long)fh * fw * 16 / sizeof(cpx<R>);
+    cpx<R> *g = (cpx<R> *)Gd + (long long)f * fstride;
     const long long n = (long long)fh * fw;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int y = (int)(i / fw), x = (int)(i - (long long)y * fw);
-        cplx v = {0.0, 0.0};
-        if (y < 38 && x < 38) v = {kern[((long long)f * 38 * 38 + y * 38 + x) * 2], kern[((long long)f * 38 * 38 + y * 38 + x) * 2 + 1]};
+        cpx<R> v = {(R)0, (R)0};
+        if (y < 38 && x < 38)
+            v = {(R)kern[((long long)f * 38 * 38 + y * 38 + x) * 2], (R)kern[((long long)f * 38 * 38 + y * 38 + x) * 2 + 1]};
         g[i] = v;
     }
 }
 
-// C = conj(A .* G_f)  (the inverse transform is conj(FFT(conj(X))) / N)
-__global__ void k_gab_mul(const GabJob *__restrict__ gj, double *__restrict__ ws, int f) {
+// C_f = conj(A .* G_f) for the 8 filters at once (the inverse transform is
+// conj(FFT(conj(X))) / N)
+template <typename R>
+__global__ void k_gab_mul(const GabJob *__restrict__ gj, double *__restrict__ ws) {
     const GabJob G = gj[blockIdx.y];
-    const cplx *A = (const cplx *)(ws + G.a_ws);
-    const cplx *K = (const cplx *)(ws + G.g_ws) + (long long)f * G.fh * G.fw;
-    cplx *C = (cplx *)(ws + G.c_ws);
+    const int f = blockIdx.z;
+    const long long fstride = (long long)G.fh * G.fw * 16 / sizeof(cpx<R>);
+    const cpx<R> *A = (const cpx<R> *)(ws + G.a_ws);
+    const cpx<R> *K = (const cpx<R> *)(ws + G.g_ws) + (long long)f * fstride;
+    cpx<R> *Cf = (cpx<R> *)(ws + G.c_ws) + (long long)f * fstride;
     const long long n = (long long)G.fh * G.fw;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const cplx a = A[i], k = K[i];
-        C[i] = {a.x * k.x - a.y * k.y, -(a.x * k.y + a.y * k.x)};
+        const cpx<R> a = A[i], k = K[i];
+        Cf[i] = {a.x * k.x - a.y * k.y, -(a.x * k.y + a.y * k.x)};
     }
 }
 
-// energy map e_f(b, a) = |c(b + 19, a + 19)| / N
+// energy maps e_f(b, a) = |c_f(b + 19, a + 19)| / N, FP64
+template <typename R>
 __global__ void k_gab_crop(const Plane *__restrict__ planes, const FJob *__restrict__ jobs, const GabJob *__restrict__ gj,
-                           double *__restrict__ ws, int f) {
+                           double *__restrict__ ws) {
     const FJob J = jobs[blockIdx.y];
     const GabJob G = gj[blockIdx.y];
     const Plane P = planes[J.plane];
-    const cplx *C = (const cplx *)(ws + G.c_ws);
+    const int f = blockIdx.z;
+    const long long fstride = (long long)G.fh * G.fw * 16 / sizeof(cpx<R>);
+    const cpx<R> *Cf = (const cpx<R> *)(ws + G.c_ws) + (long long)f * fstride;
     double *e = ws + G.e_ws + (long long)f * P.w * P.h;
     const double invN = 1.0 / ((double)G.fh * G.fw);
     const long long n = (long long)P.w * P.h;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int b = (int)(i / P.w), a = (int)(i - (long long)b * P.w);
-        const cplx v = C[(long long)(b + 19) * G.fw + a + 19];
-        const double re = v.x * invN, im = v.y * invN;
+        const cpx<R> v = Cf[(long long)(b + 19) * G.fw + a + 19];
+        const double re = (double)v.x * invN, im = (double)v.y * invN;
         e[i] = sqrt(__dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
     }
 }
@@ -199,29 +217,38 @@ __global__ void k_gab_final(const FJob *__restrict__ jobs, const double *__restr
     if (threadIdx.x < 7) feat[J.out + threadIdx.x] = counts[blockIdx.x * 8 + 1 + threadIdx.x] / counts[blockIdx.x * 8];
 }
 
+template <typename R>
+static void gabor_convolve(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs,
+                           const GabJob *gj_d, const std::vector<GabSize> &sizes, const FFTPlan *plans_d,
+                           const double *tabs, long long kern_tab, double *ws) {
+    // kernels' spectra, once per padded size
+    for (const GabSize &S : sizes) {
+        WC_LAUNCH(c);
+        k_gab_padk<R><<<dim3(64, 8), 256, 0, c.st>>>(tabs + kern_tab, ws + S.g_ws, S.fh, S.fw);
+        cfft2<R>(c, ws + S.g_ws, 8, S.fh, S.fw, plans_d + S.plan_w, plans_d + S.plan_h, tabs);
+    }
+    WC_LAUNCH(c);
+    k_gab_pad<R><<<dim3(128, njobs), 256, 0, c.st>>>(arena, planes, jobs, gj_d, ws);
+    // the images' spectra, one batch per padded size (jobs of a size are contiguous)
+    for (const GabSize &S : sizes)
+        cfft2<R>(c, ws + S.a_ws, S.count, S.fh, S.fw, plans_d + S.plan_w, plans_d + S.plan_h, tabs);
+    WC_LAUNCH(c);
+    k_gab_mul<R><<<dim3(64, njobs, 8), 256, 0, c.st>>>(gj_d, ws);
+    for (const GabSize &S : sizes)
+        cfft2<R>(c, ws + S.c_ws, 8 * S.count, S.fh, S.fw, plans_d + S.plan_w, plans_d + S.plan_h, tabs);
+    WC_LAUNCH(c);
+    k_gab_crop<R><<<dim3(64, njobs, 8), 256, 0, c.st>>>(planes, jobs, gj_d, ws);
+}
+
 void launch_gabor(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, const GabJob *gj_d,
                   const std::vector<GabJob> &gj, const std::vector<GabSize> &sizes, const FFTPlan *plans_d,
                   const double *tabs, long long kern_tab, double *ws, double *counts, double *feat) {
     if (njobs <= 0) return;
-    // kernels' spectra, once per padded size
-    for (const GabSize &S : sizes) {
-        WC_LAUNCH(c);
-        k_gab_padk<<<dim3(64, 8), 256, 0, c.st>>>(tabs + kern_tab, ws + S.g_ws, S.fh, S.fw);
-        cfft2(c, ws + S.g_ws, 8, S.fh, S.fw, plans_d + S.plan_w, plans_d + S.plan_h, tabs);
-    }
-    WC_LAUNCH(c);
-    k_gab_pad<<<dim3(128, njobs), 256, 0, c.st>>>(arena, planes, jobs, gj_d, ws);
-    // the images' spectra (sizes may differ between jobs: one call per job)
-    for (int j = 0; j < njobs; j++)
-        cfft2(c, ws + gj[j].a_ws, 1, gj[j].fh, gj[j].fw, plans_d + gj[j].plan_w, plans_d + gj[j].plan_h, tabs);
-    for (int f = 0; f < 8; f++) {
-        WC_LAUNCH(c);
-        k_gab_mul<<<dim3(128, njobs), 256, 0, c.st>>>(gj_d, ws, f);
-        for (int j = 0; j < njobs; j++)
-            cfft2(c, ws + gj[j].c_ws, 1, gj[j].fh, gj[j].fw, plans_d + gj[j].plan_w, plans_d + gj[j].plan_h, tabs);
-        WC_LAUNCH(c);
-        k_gab_crop<<<dim3(128, njobs), 256, 0, c.st>>>(planes, jobs, gj_d, ws, f);
-    }
+    (void)gj;
+    if (c.prec == WC_PREC_MIXED)
+        gabor_convolve<float>(c, arena, planes, jobs, njobs, gj_d, sizes, plans_d, tabs, kern_tab, ws);
+    else
+        gabor_convolve<double>(c, arena, planes, jobs, njobs, gj_d, sizes, plans_d, tabs, kern_tab, ws);
     WC_LAUNCH(c);
     k_gab_count<<<dim3(njobs, 8), 1024, 0, c.st>>>(planes, jobs, gj_d, ws, counts);
     WC_LAUNCH(c);

@@ -67,7 +67,14 @@ __global__ void k_zern_moments(const double *__restrict__ arena, const Plane *__
 #define ZCHUNK 2048
 // second pass: per (chunk of pixels, half, job): per-CTA partial AR/AI.
 // HALF 0 covers n = 0..10, HALF 1 covers n = 11..15 (36 (n, m) pairs each).
-template <int HALF>
+// FAST = false is the FP64 form, with the reference's divisions (x / rad,
+// x / r, H3 / r^2, (n + 1) f / pi); FAST = true (mixed form) takes one
+// reciprocal per pixel and multiplies, and folds (n + 1) / pi: each such term
+// moves by at most an ulp or two, and the FP64 pipe does about half the work.
+// (FP32 is not used here: the order-15 moments of planes with mixed signs
+// cancel heavily, and FP32 basis rounding shows up at 1e-4 of the largest
+// coefficient.)
+template <int HALF, bool FAST>
 __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ arena, const Plane *__restrict__ planes,
                                                     const FJob *__restrict__ jobs, const double *__restrict__ mom,
                                                     double *__restrict__ part, int nchunk) {
@@ -83,18 +90,21 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
     if (c0 < npix) {
         const double sum = mom[3 * blockIdx.z], cx = mom[3 * blockIdx.z + 1], cy = mom[3 * blockIdx.z + 2];
         const double rad = (double)(P.w < P.h ? P.w : P.h);
+        const double inv_rad = 1.0 / rad, inv_sum = 1.0 / sum;
         const double *p = arena + P.off;
         const long long c1 = min(npix, c0 + ZCHUNK);
         for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
             const long long yy = i / P.w, xx = i - yy * P.w;
-            const double x = __dsub_rn((double)(xx + 1), cx) / rad, y = __dsub_rn((double)(yy + 1), cy) / rad;
+            const double dx = __dsub_rn((double)(xx + 1), cx), dy = __dsub_rn((double)(yy + 1), cy);
+            const double x = FAST ? dx * inv_rad : dx / rad, y = FAST ? dy * inv_rad : dy / rad;
             const double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), r = sqrt(r2);
             if (r < DBL_EPSILON || r > 1.0) continue;
             double R[16], CO[16], SI[16];
             R[0] = 1;
 #pragma unroll
             for (int n = 1; n <= 15; n++) R[n] = r * R[n - 1];
-            const double a = x / r, b = y / r;
+            const double inv_r = FAST ? 1.0 / r : 0.0, inv_r2 = inv_r * inv_r;
+            const double a = FAST ? x * inv_r : x / r, b = FAST ? y * inv_r : y / r;
             CO[0] = a;
             SI[0] = b;
 #pragma unroll
@@ -102,11 +112,11 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
                 CO[m] = a * CO[m - 1] - b * SI[m - 1];
                 SI[m] = a * SI[m - 1] + b * CO[m - 1];
             }
-            const double f = p[i] / sum;
+            const double f = FAST ? p[i] * inv_sum : p[i] / sum;
             int q = 0;
 #pragma unroll
             for (int n = NLO; n <= NHI; n++) {
-                const double ct = (n + 1) * f / kZPI;
+                const double ct = FAST ? f * ((n + 1) / kZPI) : (n + 1) * f / kZPI;
                 const double Rn = R[n], Rnm2 = n >= 2 ? R[n - 2] : 0.0;
                 double Rnm = 0, Rnmp2 = 0, Rnmp4 = 0;
                 const int cnt = n / 2 + 1;
@@ -120,7 +130,8 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
                         Rnm = n * Rn - (n - 1) * Rnm2;
                         Rnmp2 = Rnm;
                     } else {
-                        Rnm = c_zH1[n][m] * Rnmp4 + (c_zH2[n][m] + (c_zH3[n][m] / r2)) * Rnmp2;
+                        const double h3 = FAST ? c_zH3[n][m] * inv_r2 : c_zH3[n][m] / r2;
+                        Rnm = c_zH1[n][m] * Rnmp4 + (c_zH2[n][m] + h3) * Rnmp2;
                         Rnmp4 = Rnmp2;
                         Rnmp2 = Rnm;
                     }
@@ -170,9 +181,15 @@ void launch_zernike(Ctx &c, const double *arena, const Plane *planes, const FJob
     WC_LAUNCH(c);
     k_zern_moments<<<njobs, 512, 0, c.st>>>(arena, planes, jobs, mom);
     WC_LAUNCH(c);
-    k_zern_accum<0><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+    if (c.prec == WC_PREC_MIXED)
+        k_zern_accum<0, true><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+    else
+        k_zern_accum<0, false><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
     WC_LAUNCH(c);
-    k_zern_accum<1><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+    if (c.prec == WC_PREC_MIXED)
+        k_zern_accum<1, true><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+    else
+        k_zern_accum<1, false><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
     WC_LAUNCH(c);
     k_zern_finish<<<njobs, 96, 0, c.st>>>(jobs, part, nchunk, feat);
 }
@@ -306,6 +323,107 @@ __global__ void __launch_bounds__(256) k_cf_accum(const CFJob *__restrict__ cj, 
     }
 }
 
+// Mixed form of the accumulation: the unit-disc test and r stay FP64 (they
+// decide which pixels count, exactly as above); the basis is FP32 (T_a(2r-1) by
+// the three-term recurrence, e^{-i m phi} by repeated complex multiplication by
+// e^{-i phi}), and every thread sums at most CF_CHUNK / 8 products per output in
+// FP32 before the FP64 reduction over threads and chunks.
+// Threads: 8 pixel streams x 23 rows m; each owns the 2 x NN outputs of its row.
+#define CF32_PX 184
+__global__ void __launch_bounds__(192) k_cf_accum_f32(const CFJob *__restrict__ cj, const double *__restrict__ ws,
+                                                      double *__restrict__ part, int nchunk_max) {
+    extern __shared__ __align__(16) float cfsm[];  // Gc, Gs, Tb: [CF32_PX][24] each; red aliases them at the end
+    float(*Gc)[24] = (float(*)[24])cfsm;
+    float(*Gs)[24] = (float(*)[24])(cfsm + CF32_PX * 24);
+    float(*Tb)[24] = (float(*)[24])(cfsm + 2 * CF32_PX * 24);
+    double(*red)[47] = (double(*)[47])cfsm;
+    const CFJob C = cj[blockIdx.y];
+    const int m = C.new_h, n = C.new_w;
+    const long long npix = (long long)m * n;
+    const long long c0 = (long long)blockIdx.x * CF_CHUNK;
+    int N = 11;
+    const int Nmax = (min(m, n) - 1) / 2;
+    if (N > Nmax) N = Nmax;
+    const int NN = 2 * N + 1;
+    const double *img = ws + C.src_ws;
+    const double tn = 2.0 / ((double)n - 1), tm = 2.0 / ((double)m - 1);
+    const int t = threadIdx.x, st = t / 23, row = t - 23 * st;
+    float ar[23], ai[23];
+#pragma unroll
+    for (int a = 0; a < 23; a++) ar[a] = ai[a] = 0.f;
+    const long long cend = min(npix, c0 + CF_CHUNK);
+    for (long long s0 = c0; s0 < cend; s0 += CF32_PX) {
+        if (t < CF32_PX) {
+            const long long ind = s0 + t;  // x-major: ind = x*m + y
+            float I = 0.f, xx = 0.f, ca = 1.f, sa = 0.f;
+            if (ind < cend) {
+                const long long x = ind / m, y = ind - x * m;
+                const double xi = __dadd_rn(-1.0, __dmul_rn((double)x, tn)), yi = __dadd_rn(-1.0, __dmul_rn((double)y, tm));
+                const double r = sqrt(__dadd_rn(__dmul_rn(xi, xi), __dmul_rn(yi, yi)));
+                if (r < 1) {
+                    I = (float)img[y * n + x];
+                    double xd = __dsub_rn(__dmul_rn(r, 2.0), 1.0);
+                    xx = (float)fmin(1.0, fmax(-1.0, xd));
+                    const float ph = -atan2f((float)yi, (float)xi);  // phi; e^{-i phi} = (cos, -sin)
+                    sincosf(ph, &sa, &ca);
+                }
+            }
+            // T_a(xx), T_0 = 0.5 as the reference sets it
+            float tp = 1.f, tc = xx;
+            Tb[t][0] = 0.5f;
+            if (NN > 1) Tb[t][1] = xx;
+            for (int a = 2; a < NN; a++) {
+                const float tnx = 2.f * xx * tc - tp;
+                tp = tc;
+                tc = tnx;
+                Tb[t][a] = tnx;
+            }
+            // rows im = mf + N, mf = -N..N: Ft cos(mf phi) I, Ft sin(-mf phi) I
+            Gc[t][N] = 0.5f * I;
+            Gs[t][N] = 0.f;
+            float ck = 1.f, sk = 0.f;
+            for (int k = 1; k <= N; k++) {
+                const float c2 = ck * ca - sk * sa, s2 = sk * ca + ck * sa;  // cos(k phi), sin(k phi)
+                ck = c2;
+                sk = s2;
+                Gc[t][N + k] = ck * I;
+                Gs[t][N + k] = -sk * I;
+                Gc[t][N - k] = ck * I;
+                Gs[t][N - k] = sk * I;
+            }
+        }
+        __syncthreads();
+        if (t < CF32_PX && row < NN) {
+            const int npx = (int)min((long long)CF32_PX, cend - s0);
+            for (int p = st; p < npx; p += 8) {
+                const float gc = Gc[p][row], gs = Gs[p][row];
+#pragma unroll
+                for (int a = 0; a < 23; a++) {
+                    const float tb = Tb[p][a];
+                    ar[a] = fmaf(gc, tb, ar[a]);
+                    ai[a] = fmaf(gs, tb, ai[a]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // reduce the 8 streams in FP64, fixed order (the staging buffers are free now)
+    double *out = part + ((long long)blockIdx.y * nchunk_max + blockIdx.x) * (2 * 529);
+    for (int s = 0; s < 8; s++) {
+        if (st == s && t < CF32_PX)
+            for (int a = 0; a < 23; a++) {
+                red[row][2 * a] = (s ? red[row][2 * a] : 0.0) + (double)ar[a];
+                red[row][2 * a + 1] = (s ? red[row][2 * a + 1] : 0.0) + (double)ai[a];
+            }
+        __syncthreads();
+    }
+    for (int o = t; o < NN * NN; o += blockDim.x) {
+        const int im = o / NN, a = o - im * NN;
+        out[2 * o] = red[im][2 * a];
+        out[2 * o + 1] = red[im][2 * a + 1];
+    }
+}
+
 __global__ void k_cf_finish(const FJob *__restrict__ jobs, const CFJob *__restrict__ cj, const double *__restrict__ part,
                             int nchunk_max, double *__restrict__ feat) {
     __shared__ double co[529];
@@ -361,7 +479,17 @@ void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const 
         attr = true;
     }
     WC_LAUNCH(c);
-    k_cf_accum<<<dim3(nchunk_max, njobs), 256, sm, c.st>>>(cj, ws, part, nchunk_max);
+    if (c.prec == WC_PREC_MIXED) {
+        const int sm32 = 3 * CF32_PX * 24 * sizeof(float);
+        static bool attr32 = false;
+        if (!attr32) {
+            cudaFuncSetAttribute(k_cf_accum_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32);
+            attr32 = true;
+        }
+        k_cf_accum_f32<<<dim3(nchunk_max, njobs), 192, sm32, c.st>>>(cj, ws, part, nchunk_max);
+    }
+    else
+        k_cf_accum<<<dim3(nchunk_max, njobs), 256, sm, c.st>>>(cj, ws, part, nchunk_max);
     WC_LAUNCH(c);
     k_cf_finish<<<njobs, 256, 0, c.st>>>(jobs, cj, part, nchunk_max, feat);
 }

@@ -94,6 +94,21 @@ __global__ void __launch_bounds__(1024) k_har_glcm(const Plane *__restrict__ pla
         if (i == j) c *= 2;
         Pm[q] = (cnt_s == 0) ? 0.0 : c / count;
     }
+    // nonzero column range of every row (the matrix is symmetric, so also of every column)
+    int *lo = (int *)(wsb + H.mar_b + (long long)ang * HAR_MAR_BYTES + 4096), *hi = lo + 256;
+    for (int i = threadIdx.x; i < Ng; i += blockDim.x) {
+        int a = Ng, b = -1;
+        if (cnt_s != 0)
+            for (int j = 0; j < Ng; j++) {
+                const int x = min(i, j), y = max(i, j);
+                if (tri[x * 256 - x * (x - 1) / 2 + (y - x)]) {
+                    a = min(a, j);
+                    b = j;
+                }
+            }
+        lo[i] = a;
+        hi[i] = b;
+    }
 }
 
 // f1..f13 for one (job, angle); marginals summed sequentially per entry.
@@ -115,6 +130,9 @@ __global__ void __launch_bounds__(256) k_har_stats(const FJob *__restrict__ jobs
         }
         px[i] = s;
         py[i] = t;
+        double *mar = (double *)(wsb + H.mar_b + (long long)ang * HAR_MAR_BYTES);
+        mar[i] = s;
+        mar[256 + i] = t;
     }
     for (int k = threadIdx.x; k <= 2 * Ng - 2; k += blockDim.x) {
         double s = 0;
@@ -218,99 +236,137 @@ __device__ void hh_make(const double *v, int n, double *ess, double &tau, double
     }
 }
 
-// B = H B on rows r0..r0+m-1, columns c0..c0+nc-1 (threads over columns)
-__device__ void hh_left_par(double *A, int ld, int r0, int m, int c0, int nc, const double *ess, double tau) {
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-        double *col = A + (long long)r0 * ld + c0 + c;
-        if (m == 1) {
-            col[0] = __dmul_rn(col[0], __dsub_rn(1.0, tau));
-            continue;
-        }
-        double t = 0;
-        for (int r = 1; r < m; r++) t = __dadd_rn(t, __dmul_rn(ess[r - 1], col[(long long)r * ld]));
-        t = __dadd_rn(t, col[0]);
-        col[0] = __dsub_rn(col[0], __dmul_rn(tau, t));
-        for (int r = 1; r < m; r++)
-            col[(long long)r * ld] = __dsub_rn(col[(long long)r * ld], __dmul_rn(__dmul_rn(tau, ess[r - 1]), t));
-    }
-}
-
-// B = B H on rows r0..r0+m-1, columns c0..c0+nc-1 (threads over rows)
-__device__ void hh_right_par(double *A, int ld, int r0, int m, int c0, int nc, const double *ess, double tau) {
-    for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        double *row = A + (long long)(r0 + r) * ld + c0;
-        if (nc == 1) {
-            row[0] = __dmul_rn(row[0], __dsub_rn(1.0, tau));
-            continue;
-        }
-        double t = 0;
-        for (int c = 1; c < nc; c++) t = __dadd_rn(t, __dmul_rn(row[c], ess[c - 1]));
-        t = __dadd_rn(t, row[0]);
-        row[0] = __dsub_rn(row[0], __dmul_rn(tau, t));
-        for (int c = 1; c < nc; c++) row[c] = __dsub_rn(row[c], __dmul_rn(__dmul_rn(tau, t), ess[c - 1]));
-    }
-}
-
-__global__ void __launch_bounds__(256) k_har_qhess(const FJob *__restrict__ jobs, const HarJob *__restrict__ hj,
-                                                 char *__restrict__ wsb) {
-    __shared__ double px[256], py[256], v[256], ess[256];
-    __shared__ double s_tau, s_beta;
+// Q, one warp per row i: Q(i,j) = sum over k ascending of
+// RN(RN(P(i,k) P(j,k)) / RN(RN(px_i py_k) + 1e-13)), as _Q_calc_eigen sums it
+// (CVIPtexture.cpp:961-987).  Terms with P(i,k) P(j,k) = 0 add +0 to a sum of
+// nonnegative terms, so only k in the nonzeros of row i and j in the nonzeros of
+// row k (= column k: the matrix is symmetric) are visited; every Q(i,j) still
+// receives its nonzero terms in ascending k, with the same roundings.
+#define Q_WARPS 8
+__global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    __shared__ double qrow[Q_WARPS][256];
+    __shared__ double py[256];
     const int ang = blockIdx.y;
     const HarJob H = hj[blockIdx.x];
     const int n = ((const int *)(wsb + H.lut_b))[256];
     if (n < 3) return;
     const double *P = (const double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256;
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
-    // marginals as the oracle computes them (sequential sums)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double s = 0, t = 0;
-        for (int j = 0; j < n; j++) {
-            s += P[(long long)i * n + j];
-            t += P[(long long)j * n + i];
-        }
-        px[i] = s;
-        py[i] = t;
-    }
+    const double *mar = (const double *)(wsb + H.mar_b + (long long)ang * HAR_MAR_BYTES);
+    const int *lo = (const int *)(wsb + H.mar_b + (long long)ang * HAR_MAR_BYTES + 4096), *hi = lo + 256;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) py[k] = mar[256 + k];
     __syncthreads();
-    for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
-        const int i = (int)(q / n), j = (int)(q - (long long)i * n);
-        const double di = px[i];
-        double s = 0;
-        for (int k = 0; k < n; k++) {
-            const double a = P[(long long)i * n + k], b = P[(long long)j * n + k];
-            const double rp = __dmul_rn(a, b);
-            if (rp == 0.0) continue;  // adds +0: skipping is exact
-            s = __dadd_rn(s, rp / __dadd_rn(__dmul_rn(di, py[k]), 0.0000000000001));
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    double *q = qrow[wq];
+    for (int i = blockIdx.z * Q_WARPS + wq; i < n; i += gridDim.z * Q_WARPS) {
+        for (int j = lane; j < n; j += 32) q[j] = 0.0;
+        __syncwarp();
+        const double di = mar[i];
+        const double *Pi = P + (long long)i * n;
+        const int klo = lo[i], khi = hi[i];
+        for (int k0 = klo; k0 <= khi; k0 += 32) {
+            const int kk = k0 + lane;
+            const double al = kk <= khi ? Pi[kk] : 0.0;
+            unsigned m = __ballot_sync(0xffffffffu, al != 0.0);
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1;
+                const int k = k0 + b;
+                const double a = __shfl_sync(0xffffffffu, al, b);
+                const double d = __dadd_rn(__dmul_rn(di, py[k]), 0.0000000000001);
+                const double *Pk = P + (long long)k * n;
+                for (int j = lo[k] + lane; j <= hi[k]; j += 32) {
+                    const double rp = __dmul_rn(a, Pk[j]);
+                    if (rp != 0.0) q[j] = __dadd_rn(q[j], rp / d);
+                }
+                __syncwarp();
+            }
         }
-        A[q] = s;
+        double *Ai = A + (long long)i * n;
+        for (int j = lane; j < n; j += 32) Ai[j] = q[j];
+        __syncwarp();
     }
-    __syncthreads();
-    // Hessenberg reduction
+}
+
+// Hessenberg reduction of Q in place (HessenbergDecomposition::_compute,
+// HessenbergDecomposition.h:292-318): column i's reflector from the sequential
+// tail sum, then H A on the trailing rows and A H on all rows.  One CTA per
+// matrix; products that the reference forms per element (tau * ess_r, tau * t)
+// are formed once, with the same value.
+__global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    __shared__ double v[256], ess[256], tess[256];
+    __shared__ double s_tau, s_beta, s_den;
+    __shared__ int s_triv;
+    const int ang = blockIdx.y;
+    const HarJob H = hj[blockIdx.x];
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    if (n < 3) return;
+    double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
     for (int i = 0; i < n - 1; i++) {
         const int rem = n - i - 1;
         for (int k = threadIdx.x; k < rem; k += blockDim.x) v[k] = A[(long long)(i + 1 + k) * n + i];
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double tau, beta;
-            hh_make(v, rem, ess, tau, beta);
-            s_tau = tau;
-            s_beta = beta;
+        if (threadIdx.x == 0) {  // makeHouseholder (Householder.h:65-90)
+            double tail = 0;
+            for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, __dmul_rn(v[k], v[k]));
+            const double c0 = v[0];
+            if (rem == 1 || tail == 0) {
+                s_triv = 1;
+                s_tau = 0;
+                s_beta = c0;
+            } else {
+                double beta = sqrt(__dadd_rn(__dmul_rn(c0, c0), tail));
+                if (c0 >= 0) beta = -beta;
+                s_triv = 0;
+                s_beta = beta;
+                s_den = __dsub_rn(c0, beta);
+                s_tau = __dsub_rn(beta, c0) / beta;
+            }
         }
         __syncthreads();
         const double tau = s_tau;
+        for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) {
+            const double e = s_triv ? 0.0 : v[k] / s_den;
+            ess[k - 1] = e;
+            tess[k - 1] = __dmul_rn(tau, e);
+            A[(long long)(i + 1 + k) * n + i] = e;
+        }
         if (threadIdx.x == 0) A[(long long)(i + 1) * n + i] = s_beta;
-        for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) A[(long long)(i + 1 + k) * n + i] = ess[k - 1];
         __syncthreads();
-        hh_left_par(A, n, i + 1, rem, i + 1, rem, ess, tau);
+        // H A: rows i+1.., columns i+1.. (threads over columns)
+        for (int c = i + 1 + threadIdx.x; c < n; c += blockDim.x) {
+            double *col = A + (long long)(i + 1) * n + c;
+            if (rem == 1) {
+                col[0] = __dmul_rn(col[0], __dsub_rn(1.0, tau));
+                continue;
+            }
+            double t = 0;
+            for (int r = 1; r < rem; r++) t = __dadd_rn(t, __dmul_rn(ess[r - 1], col[(long long)r * n]));
+            t = __dadd_rn(t, col[0]);
+            col[0] = __dsub_rn(col[0], __dmul_rn(tau, t));
+            for (int r = 1; r < rem; r++) col[(long long)r * n] = __dsub_rn(col[(long long)r * n], __dmul_rn(tess[r - 1], t));
+        }
         __syncthreads();
-        hh_right_par(A, n, 0, n, i + 1, rem, ess, tau);
+        // A H: all rows, columns i+1.. (threads over rows)
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            double *row = A + (long long)r * n + i + 1;
+            if (rem == 1) {
+                row[0] = __dmul_rn(row[0], __dsub_rn(1.0, tau));
+                continue;
+            }
+            double t = 0;
+            for (int c = 1; c < rem; c++) t = __dadd_rn(t, __dmul_rn(row[c], ess[c - 1]));
+            t = __dadd_rn(t, row[0]);
+            const double tt = __dmul_rn(tau, t);
+            row[0] = __dsub_rn(row[0], tt);
+            for (int c = 1; c < rem; c++) row[c] = __dsub_rn(row[c], __dmul_rn(tt, ess[c - 1]));
+        }
         __syncthreads();
     }
     for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
         const int r = (int)(q / n), c = (int)(q - (long long)r * n);
         if (c < r - 1) A[q] = 0;
     }
-    __syncthreads();
 }
 
 // Real-Schur QR iteration of one Hessenberg matrix per warp (RealSchur::compute,
@@ -321,12 +377,69 @@ __global__ void __launch_bounds__(256) k_har_qhess(const FJob *__restrict__ jobs
 // window are never read again (columns > iu are deflated, the block above il
 // is decoupled).  All lanes take the same decisions from the same (broadcast)
 // values; lane-parallel loops run over the columns/rows of a reflector.
-#define QR_WARPS 4
-__global__ void __launch_bounds__(32 * QR_WARPS) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb, int nmat) {
-    __shared__ double rowsum[QR_WARPS][256];
-    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-    const int m = blockIdx.x * QR_WARPS + wq;
-    if (m >= nmat) return;
+// x + 0.0 in round-to-nearest: x, except -0 -> +0 (integer ops, off the FP64 pipe)
+__device__ __forceinline__ double plus_zero(double x) {
+    const long long b = __double_as_longlong(x);
+    return b == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+
+// makeHouseholder of a 3-vector with the scalar work spread over lanes: lanes
+// 1, 2 square v1, v2 at once, and lanes 0, 1, 2 form v1/(c0-beta),
+// v2/(c0-beta) and (beta-c0)/beta in one division.  Same operations and
+// roundings as the sequential form (0 + v1^2 = v1^2 exactly, as v1^2 >= +0).
+__device__ __forceinline__ void hh_make3(const double v0, const double v1, const double v2, int lane, double &e0,
+                                         double &e1, double &tau, double &beta) {
+    const double vl = lane == 2 ? v2 : v1;
+    const double sq = __dmul_rn(vl, vl);
+    const double s1 = __shfl_sync(0xffffffffu, sq, 1), s2 = __shfl_sync(0xffffffffu, sq, 2);
+    const double tail = __dadd_rn(s1, s2);
+    if (tail == 0) {
+        tau = 0;
+        beta = v0;
+        e0 = e1 = 0;
+        return;
+    }
+    beta = sqrt(__dadd_rn(__dmul_rn(v0, v0), tail));
+    if (v0 >= 0) beta = -beta;
+    const double den = __dsub_rn(v0, beta);
+    const double num = lane == 0 ? v1 : (lane == 1 ? v2 : __dsub_rn(beta, v0));
+    const double q = num / (lane < 2 ? den : beta);
+    e0 = __shfl_sync(0xffffffffu, q, 0);
+    e1 = __shfl_sync(0xffffffffu, q, 1);
+    tau = __shfl_sync(0xffffffffu, q, 2);
+}
+
+// Matrices in descending Ng (counting sort; the order only schedules, every
+// matrix is computed alone), so the longest QR runs start first.
+__global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj, const char *__restrict__ wsb, int nmat,
+                                                   int *__restrict__ perm) {
+    __shared__ int cnt[258];
+    for (int t = threadIdx.x; t < 258; t += blockDim.x) cnt[t] = 0;
+    __syncthreads();
+    for (int m = threadIdx.x; m < nmat; m += blockDim.x) {
+        const int n = ((const int *)(wsb + hj[m >> 2].lut_b))[256];
+        atomicAdd(&cnt[256 - n], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r = 0;
+        for (int k = 0; k < 257; k++) {
+            const int c = cnt[k];
+            cnt[k] = r;
+            r += c;
+        }
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m < nmat; m += blockDim.x) {
+        const int n = ((const int *)(wsb + hj[m >> 2].lut_b))[256];
+        perm[atomicAdd(&cnt[256 - n], 1)] = m;
+    }
+}
+
+__global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb, const int *__restrict__ perm) {
+    __shared__ double rowsum[256];
+    const int lane = threadIdx.x & 31;
+    const int m = perm[blockIdx.x];
     const int job = m >> 2, ang = m & 3;
     const HarJob H = hj[job];
     const int n = ((const int *)(wsb + H.lut_b))[256];
@@ -342,11 +455,11 @@ __global__ void __launch_bounds__(32 * QR_WARPS) k_har_qr(const HarJob *__restri
         const int s0 = j - 1 > 0 ? j - 1 : 0;
         double s = 0;
         for (int c = s0; c < n; c++) s = __dadd_rn(s, fabs(T_(j, c)));
-        rowsum[wq][j] = s;
+        rowsum[j] = s;
     }
     __syncwarp();
     double norm = 0;
-    for (int j = 0; j < n; j++) norm = __dadd_rn(norm, rowsum[wq][j]);
+    for (int j = 0; j < n; j++) norm = __dadd_rn(norm, rowsum[j]);
     const double eps = DBL_EPSILON;
     const int maxIter = 40 * n;
     int iu = n - 1, iter = 0, totalIter = 0;
@@ -476,10 +589,9 @@ __global__ void __launch_bounds__(32 * QR_WARPS) k_har_qr(const HarJob *__restri
                 // performFrancisQRStep, restricted to the window
                 for (int k = im; k <= iu - 2; ++k) {
                     const bool first = (k == im);
-                    double vv[3], ess[2], tau, beta;
-                    if (first) { vv[0] = fv0; vv[1] = fv1; vv[2] = fv2; }
-                    else { vv[0] = T_(k, k - 1); vv[1] = T_(k + 1, k - 1); vv[2] = T_(k + 2, k - 1); }
-                    hh_make(vv, 3, ess, tau, beta);
+                    double ess[2], tau, beta;
+                    if (first) hh_make3(fv0, fv1, fv2, lane, ess[0], ess[1], tau, beta);
+                    else hh_make3(T_(k, k - 1), T_(k + 1, k - 1), T_(k + 2, k - 1), lane, ess[0], ess[1], tau, beta);
                     __syncwarp();
                     if (beta != 0) {
                         if (lane == 0) {
@@ -488,7 +600,7 @@ __global__ void __launch_bounds__(32 * QR_WARPS) k_har_qr(const HarJob *__restri
                         }
                         for (int cc = k + lane; cc <= iu; cc += 32) {  // left: rows k..k+2
                             const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
-                            double t = __dadd_rn(__dmul_rn(ess[0], a1), 0.0);
+                            double t = plus_zero(__dmul_rn(ess[0], a1));
                             t = __dadd_rn(t, __dmul_rn(ess[1], a2));
                             t = __dadd_rn(t, a0);
                             T_(k, cc) = __dsub_rn(a0, __dmul_rn(tau, t));
@@ -499,7 +611,7 @@ __global__ void __launch_bounds__(32 * QR_WARPS) k_har_qr(const HarJob *__restri
                         const int rend = min(iu, k + 3);
                         for (int rr = il + lane; rr <= rend; rr += 32) {  // right: cols k..k+2
                             const double b0 = T_(rr, k), b1 = T_(rr, k + 1), b2 = T_(rr, k + 2);
-                            double t = __dadd_rn(__dmul_rn(b1, ess[0]), 0.0);
+                            double t = plus_zero(__dmul_rn(b1, ess[0]));
                             t = __dadd_rn(t, __dmul_rn(b2, ess[1]));
                             t = __dadd_rn(t, b0);
                             const double tt = __dmul_rn(tau, t);
@@ -589,7 +701,7 @@ __global__ void k_har_final(const FJob *__restrict__ jobs, const HarJob *__restr
 }
 
 void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
-                     int njobs, const HarJob *hj, char *wsb, double *feat) {
+                     int njobs, const HarJob *hj, char *wsb, int *perm, double *feat) {
     if (njobs <= 0) return;
     const int sm = 256 * 257 / 2 * sizeof(unsigned int);
     static bool attr = false;
@@ -604,9 +716,13 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     WC_LAUNCH(c);
     k_har_stats<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
     WC_LAUNCH(c);
-    k_har_qhess<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
+    k_har_q<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
     WC_LAUNCH(c);
-    k_har_qr<<<(4 * njobs + QR_WARPS - 1) / QR_WARPS, 32 * QR_WARPS, 0, c.st>>>(hj, wsb, 4 * njobs);
+    k_har_hess<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    WC_LAUNCH(c);
+    k_har_order<<<1, 256, 0, c.st>>>(hj, wsb, 4 * njobs, perm);
+    WC_LAUNCH(c);
+    k_har_qr<<<4 * njobs, 32, 0, c.st>>>(hj, wsb, perm);
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);
 }

@@ -57,7 +57,14 @@ __device__ __forceinline__ double local_mean(const double *__restrict__ S, int W
     const double ol = ((sy - 1 < 0) || (sx - 1 < 0)) ? 0 : S[(ey - 1) * W + sx - 1];
     const double unten = S[ey * W + sx];
     const long long cnt = (ey - sy + 1) * (ex - sx + 1);
-    return __dadd_rn(__dsub_rn(__dsub_rn(unten, links), oben), ol) / (double)cnt;
+    const double v = __dadd_rn(__dsub_rn(__dsub_rn(unten, links), oben), ol);
+    // an unclipped window holds a power-of-two count: dividing by 2^e and
+    // multiplying by the exact 2^-e round identically, and spare the FP64 pipe
+    if ((cnt & (cnt - 1)) == 0) {
+        const int e = __ffsll(cnt) - 1;
+        return __dmul_rn(v, __longlong_as_double((long long)(1023 - e) << 52));
+    }
+    return v / (double)cnt;
 }
 
 #define TAM_TILE 1024

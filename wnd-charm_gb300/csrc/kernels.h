@@ -78,10 +78,14 @@ void launch_tamura(Ctx &c, const Plane *planes, const PlaneStats *stats, const d
 
 // k_haralick.cu
 struct HarJob {
-    long long gray_b, lut_b, glcm_b, q_b, res_b;  // byte offsets into the workspace
+    // byte offsets into the workspace: gray image, tone LUT (+ Ng), 4 co-occurrence
+    // matrices, 4 Q / Hessenberg / Schur matrices, 4 x 14 results, and per angle the
+    // marginals px[256], py[256] and the nonzero column range of every row
+    long long gray_b, lut_b, glcm_b, q_b, res_b, mar_b;
 };
+#define HAR_MAR_BYTES 6144  // per angle: px, py (2 x 256 doubles), lo, hi (2 x 256 ints)
 void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs,
-                     int njobs, const HarJob *hj, char *wsb, double *feat);
+                     int njobs, const HarJob *hj, char *wsb, int *perm, double *feat);
 
 // k_groupa.cu
 struct EFJob {
@@ -102,12 +106,14 @@ void launch_objects(Ctx &c, const double *arena, const Plane *planes, const Plan
 
 // k_gabor.cu
 struct GabJob {
-    long long a_ws, c_ws, e_ws, g_ws;  // doubles offsets: image spectrum, product, 8 energy maps, kernel spectra
+    long long a_ws, c_ws, e_ws, g_ws;  // doubles offsets: image spectrum, 8 products, 8 energy maps, kernel spectra
     int fh, fw, plan_h, plan_w;
 };
 struct GabSize {
     int fh, fw, plan_h, plan_w;
-    long long g_ws;
+    long long g_ws;        // the 8 kernel spectra of this padded size
+    long long a_ws, c_ws;  // first job's image spectrum / 8 products; the size's jobs follow contiguously
+    int count;             // jobs of this padded size
 };
 void launch_gabor(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, const GabJob *gj_d,
                   const std::vector<GabJob> &gj, const std::vector<GabSize> &sizes, const FFTPlan *plans_d,

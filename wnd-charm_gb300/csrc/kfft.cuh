@@ -1,21 +1,37 @@
 // Stockham mixed-radix DFT of several lines held in shared memory (any
 // length; radix-p stages with host-computed FP64 twiddles
 // tw[k] = exp(-2 pi i k / n)).  Shared by the Fourier transform node and the
-// Gabor FFT convolution.
+// Gabor FFT convolution; templated on the element type (FP64 form, and FP32
+// for the mixed form's Gabor filtering, which rounds the twiddles on load).
 #pragma once
 #include "kernels.h"
 
 namespace wc {
 
-struct cplx {
-    double x, y;
+template <typename R>
+struct cpx {
+    R x, y;
 };
-__device__ __forceinline__ cplx cmul(cplx a, cplx b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
-__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return {a.x + b.x, a.y + b.y}; }
+typedef cpx<double> cplx;
+template <typename R>
+__device__ __forceinline__ cpx<R> cmul(cpx<R> a, cpx<R> b) {
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> cadd(cpx<R> a, cpx<R> b) {
+    return {a.x + b.x, a.y + b.y};
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> twid(const cplx *tw, long long i) {
+    const cplx t = tw[i];
+    return {(R)t.x, (R)t.y};
+}
 
 // One Stockham pass over `lines` lines of length n held in src (line-major),
 // writing dst.  Ns = product of the radices already applied.
-static __device__ void stockham_stage(const cplx *src, cplx *dst, int lines, int n, int p, int Ns, const cplx *tw) {
+template <typename R>
+static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines, int n, int p, int Ns, const cplx *tw) {
+    typedef cpx<R> C;
     const int m = n / p;
     const int total = lines * m;
     const int twstep_k = n / (Ns * p);  // twiddle W_{Ns p}^{r k} = tw[r k twstep_k]
@@ -23,31 +39,31 @@ static __device__ void stockham_stage(const cplx *src, cplx *dst, int lines, int
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
         const int l = idx / m, j = idx - l * m;
         const int k = j % Ns;
-        const cplx *s = src + (long long)l * n;
-        cplx *d = dst + (long long)l * n;
+        const C *s = src + (long long)l * n;
+        C *d = dst + (long long)l * n;
         const int obase = (j / Ns) * Ns * p + k;
         if (p <= 8) {
-            cplx v[8];
+            C v[8];
 #pragma unroll
             for (int r = 0; r < 8; r++) {
                 if (r < p) {
-                    cplx a = s[j + r * m];
-                    if (r > 0 && k > 0) a = cmul(a, tw[(long long)r * k * twstep_k % n]);
+                    C a = s[j + r * m];
+                    if (r > 0 && k > 0) a = cmul(a, twid<R>(tw, (long long)r * k * twstep_k % n));
                     v[r] = a;
                 }
             }
             for (int q = 0; q < p; q++) {
-                cplx acc = v[0];
-                for (int r = 1; r < p; r++) acc = cadd(acc, cmul(v[r], tw[(long long)((r * q) % p) * twstep_q]));
+                C acc = v[0];
+                for (int r = 1; r < p; r++) acc = cadd(acc, cmul(v[r], twid<R>(tw, (long long)((r * q) % p) * twstep_q)));
                 d[obase + q * Ns] = acc;
             }
         } else {
             for (int q = 0; q < p; q++) {
-                cplx acc = s[j];
+                C acc = s[j];
                 for (int r = 1; r < p; r++) {
-                    cplx a = s[j + r * m];
-                    if (k > 0) a = cmul(a, tw[(long long)r * k * twstep_k % n]);
-                    acc = cadd(acc, cmul(a, tw[(long long)((r * q) % p) * twstep_q]));
+                    C a = s[j + r * m];
+                    if (k > 0) a = cmul(a, twid<R>(tw, (long long)r * k * twstep_k % n));
+                    acc = cadd(acc, cmul(a, twid<R>(tw, (long long)((r * q) % p) * twstep_q)));
                 }
                 d[obase + q * Ns] = acc;
             }
@@ -56,14 +72,15 @@ static __device__ void stockham_stage(const cplx *src, cplx *dst, int lines, int
 }
 
 // returns which buffer (0 or 1) holds the result
-static __device__ int stockham(cplx *b0, cplx *b1, int lines, const FFTPlan &P, const cplx *tw) {
-    cplx *src = b0, *dst = b1;
+template <typename R>
+static __device__ int stockham(cpx<R> *b0, cpx<R> *b1, int lines, const FFTPlan &P, const cplx *tw) {
+    cpx<R> *src = b0, *dst = b1;
     int Ns = 1, cur = 0;
     for (int s = 0; s < P.nstages; s++) {
         stockham_stage(src, dst, lines, P.n, P.radix[s], Ns, tw);
         __syncthreads();
         Ns *= P.radix[s];
-        cplx *t = src;
+        cpx<R> *t = src;
         src = dst;
         dst = t;
         cur ^= 1;

@@ -26,8 +26,10 @@ struct FeatureSetup {
     std::vector<GabSize> gab_sizes;
 };
 
+#define WC_LANES 6
 struct FeatureRun {
     Ctx *ctx;
+    Ctx *lanes;  // WC_LANES contexts on streams forked from ctx->st; families run on them concurrently
     double *arena;
     const Plane *planes;
     const PlaneStats *stats;

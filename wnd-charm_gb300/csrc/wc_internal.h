@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include "../../include/wndcharm_gb300.h"
+
 namespace wc {
 
 // Feature algorithms of the reference (src/FeatureAlgorithms.h): the 15

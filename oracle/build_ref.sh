@@ -37,7 +37,7 @@ done
 for f in fftw_shim.cpp tiff_stub.cpp ref_capi.cpp; do
   o="$OUT/obj/shim_${f%.cpp}.o"
   OBJS="$OBJS $o"
-  $CXX $FLAGS -c "$HERE/ref_shim/$f" -o "$o" &
+  $CXX $FLAGS -ffp-contract=off -c "$HERE/ref_shim/$f" -o "$o" &
   pids="$pids $!"
 done
 for p in $pids; do wait "$p"; done

@@ -7,12 +7,16 @@
 //     unmodified reference sources link without libfftw3;
 //   * oracle/wc_oracle.cpp: the oracle restatement of ImageMatrix::fft2.
 //
-// Algorithm: recursive mixed-radix decimation in time (Cooley-Tukey).  n is
-// factored into 4s, 2s, then odd primes; each stage combines p interleaved
-// sub-transforms with a direct p-point butterfly, so a prime length p costs
-// O(p^2) (a plain DFT).  Twiddles come from one exact table
-// w[k] = exp(-2*pi*i*k/n), indexed modulo n, so the result is accurate to a
-// few ulps times log(n) for every n.
+// The reference leaves the DFT to FFTW (FFTW_MEASURE: the plan, and so the
+// rounding, is chosen at run time), so no particular rounding of the DFT is
+// the reference's.  This one is a Stockham autosort FFT with the radix order
+// 8, 4, 2, then odd primes (a prime p costs O(p) per output), twiddles
+// w[k] = (cos(2 pi k / n), -sin(2 pi k / n)) from the host libm, and every
+// complex product and sum formed as (a.x b.x - a.y b.y, a.x b.y + a.y b.x) with
+// separate roundings (this file is compiled with -ffp-contract=off).  The GPU's
+// Fourier node performs the same operations in the same order, so the two
+// agree bit for bit and the integer features of Fourier-derived planes (GLCMs,
+// histograms) can be compared exactly; against FFTW both agree to ~1e-12.
 #pragma once
 #include <cmath>
 #include <complex>
@@ -22,12 +26,19 @@ namespace wcfft {
 
 typedef std::complex<double> cd;
 
+struct cx {
+    double x, y;
+};
+static inline cx cx_mul(cx a, cx b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+static inline cx cx_add(cx a, cx b) { return {a.x + b.x, a.y + b.y}; }
+
 struct Plan1D {
     int n = 0;
-    std::vector<int> radices;   // product == n
-    std::vector<cd> tw;         // tw[k] = exp(-2 pi i k / n)
+    std::vector<int> radices;  // product == n
+    std::vector<cx> tw;        // tw[k] = exp(-2 pi i k / n)
     explicit Plan1D(int n_) : n(n_) {
         int m = n;
+        while (m % 8 == 0) { radices.push_back(8); m /= 8; }
         while (m % 4 == 0) { radices.push_back(4); m /= 4; }
         while (m % 2 == 0) { radices.push_back(2); m /= 2; }
         for (int p = 3; (long)p * p <= m; p += 2)
@@ -37,42 +48,45 @@ struct Plan1D {
         const double two_pi = 6.283185307179586476925286766559;
         for (int k = 0; k < n; k++) {
             double a = two_pi * (double)k / (double)n;
-            tw[k] = cd(std::cos(a), -std::sin(a));
+            tw[k] = {std::cos(a), -std::sin(a)};
         }
     }
 
-    // out[k] = sum_j in[j*stride] * w^(j*k), recursion over radices[level..]
-    void rec(const cd *in, long stride, cd *out, int len, int level, long tw_step,
-             std::vector<cd> &scratch) const {
-        if (len == 1) { out[0] = in[0]; return; }
-        const int p = radices[level];
-        const int m = len / p;
-        for (int r = 0; r < p; r++)
-            rec(in + r * stride, stride * p, out + (long)r * m, m, level + 1, tw_step * p, scratch);
-        // combine: X[k + q*m] = sum_r w_len^{r (k + q m)} * Y_r[k]
-        if ((int)scratch.size() < p) scratch.resize(p);
-        std::vector<cd> y(p);
-        for (int k = 0; k < m; k++) {
+    // one Stockham pass of radix p; Ns = product of the radices already applied
+    void stage(const cx *src, cx *dst, int p, int Ns) const {
+        const int m = n / p;
+        const int twstep_k = n / (Ns * p), twstep_q = m;
+        std::vector<cx> v(p);
+        for (int j = 0; j < m; j++) {
+            const int k = j % Ns;
+            const int obase = (j / Ns) * Ns * p + k;
             for (int r = 0; r < p; r++) {
-                long e = ((long)r * k * tw_step) % n;
-                y[r] = out[(long)r * m + k] * tw[e];
+                cx a = src[j + r * m];
+                if (r > 0 && k > 0) a = cx_mul(a, tw[(long long)r * k * twstep_k % n]);
+                v[r] = a;
             }
             for (int q = 0; q < p; q++) {
-                cd s(0.0, 0.0);
-                for (int r = 0; r < p; r++) {
-                    long e = ((long)r * q * m % len) * tw_step % n;
-                    s += y[r] * tw[e];
-                }
-                scratch[q] = s;
+                cx acc = v[0];
+                for (int r = 1; r < p; r++) acc = cx_add(acc, cx_mul(v[r], tw[(long long)((r * q) % p) * twstep_q]));
+                dst[obase + q * Ns] = acc;
             }
-            for (int q = 0; q < p; q++) out[k + (long)q * m] = scratch[q];
         }
     }
 
     void forward(const cd *in, long stride, cd *out) const {
-        std::vector<cd> scratch;
         if (n <= 0) return;
-        rec(in, stride, out, n, 0, 1, scratch);
+        std::vector<cx> b0(n), b1(n);
+        for (int i = 0; i < n; i++) b0[i] = {in[(long)i * stride].real(), in[(long)i * stride].imag()};
+        cx *src = b0.data(), *dst = b1.data();
+        int Ns = 1;
+        for (int p : radices) {
+            stage(src, dst, p, Ns);
+            Ns *= p;
+            cx *t = src;
+            src = dst;
+            dst = t;
+        }
+        for (int i = 0; i < n; i++) out[i] = cd(src[i].x, src[i].y);
     }
 };
 

@@ -71,6 +71,9 @@ def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=2, skip=()):
 #   ("counts", moves):     at most `moves` single-count moves per group
 MIXED_RULES = {
     "Chebyshev-Fourier Coefficients": ("counts", 3),
+    # ratios of threshold counts over FP32 filter energies: a few pixels of the
+    # 512 x 512 maps may cross the threshold
+    "Gabor Textures": ("float", 1e-4, 0.0),
 }
 
 

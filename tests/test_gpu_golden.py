@@ -109,14 +109,11 @@ def test_edge_cases(eng, long_plan):
         fin = np.isfinite(exp)
         diff = np.nonzero(np.isfinite(got) != fin)[0]
         assert not len(diff), (img.shape, [(names[i], got[i], exp[i]) for i in diff[:8]])
-        # The DFT of the constant image is zero off DC, and the block image has
-        # exact sinc zeros; what an FFT returns there is rounding noise (different
-        # in every FFT implementation, FFTW's included), and features that test
-        # "> 0" (Gini) or bin that noise depend on it: skip Fourier-derived groups
-        # for these two degenerate images.
-        skip = [n.rsplit(" [", 1)[0] for n in names if "Fourier" in n.split(" (", 1)[1]] if k >= 2 else ()
-        fails = compare(np.where(fin, got, 0), np.where(fin, exp, 0), names, rtol=1e-7, atol=1e-9, count_moves=2,
-                        skip=tuple(set(skip)))
+        # The DFT of the constant image is zero off DC and the block image has
+        # exact sinc zeros: what an FFT returns there is rounding noise, which the
+        # oracle's DFT reproduces bit for bit (same operations), so even the
+        # features that test "> 0" (Gini) or bin that noise are compared.
+        fails = compare(np.where(fin, got, 0), np.where(fin, exp, 0), names, rtol=1e-7, atol=1e-9, count_moves=2)
         assert not fails, (img.shape, list(fails.items())[:3])
 
 

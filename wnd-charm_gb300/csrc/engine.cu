@@ -69,6 +69,13 @@ struct Tables {
     std::map<std::string, long long> idx;
     DevBuf dev;
     bool dirty = true;
+    // the generator runs only for a key not seen before (tables persist across batches)
+    template <typename Gen>
+    long long add_lazy(const std::string &key, Gen gen) {
+        auto it = idx.find(key);
+        if (it != idx.end()) return it->second;
+        return add(key, gen());
+    }
     long long add(const std::string &key, const std::vector<double> &v) {
         auto it = idx.find(key);
         if (it != idx.end()) return it->second;
@@ -122,14 +129,16 @@ FFTPlan fft_plan(Tables &tabs, int n) {
     if (m > 1) r.push_back(m);
     P.nstages = (int)r.size();
     for (size_t i = 0; i < r.size() && i < 16; i++) P.radix[i] = r[i];
-    std::vector<double> tw(2 * (size_t)n);
-    const double two_pi = 6.283185307179586476925286766559;
-    for (int k = 0; k < n; k++) {
-        double a = two_pi * (double)k / (double)n;
-        tw[2 * k] = std::cos(a);
-        tw[2 * k + 1] = -std::sin(a);
-    }
-    P.tw_off = tabs.add("tw" + std::to_string(n), tw);
+    P.tw_off = tabs.add_lazy("tw" + std::to_string(n), [n] {
+        std::vector<double> tw(2 * (size_t)n);
+        const double two_pi = 6.283185307179586476925286766559;
+        for (int k = 0; k < n; k++) {
+            double a = two_pi * (double)k / (double)n;
+            tw[2 * k] = std::cos(a);
+            tw[2 * k + 1] = -std::sin(a);
+        }
+        return tw;
+    });
     return P;
 }
 
@@ -319,8 +328,10 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
                     int N = std::min(S.w, S.h);
                     offs.push_back((long long)tot);
                     tot += (size_t)S.h * N + 32;
-                    toff.push_back(E->tabs.add("ch" + std::to_string(S.w) + "_" + std::to_string(N), cheb_table(S.w, N)));
-                    toff.push_back(E->tabs.add("ch" + std::to_string(S.h) + "_" + std::to_string(N), cheb_table(S.h, N)));
+                    toff.push_back(E->tabs.add_lazy("ch" + std::to_string(S.w) + "_" + std::to_string(N),
+                                                    [&] { return cheb_table(S.w, N); }));
+                    toff.push_back(E->tabs.add_lazy("ch" + std::to_string(S.h) + "_" + std::to_string(N),
+                                                    [&] { return cheb_table(S.h, N); }));
                 }
                 L.ws = ws.take(tot * sizeof(double));
                 L.aux1 = put_copy(offs.data(), offs.size() * sizeof(long long));
@@ -332,7 +343,9 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     FeatureSetup fs;
     fs.planes = &planes;
     fs.fj = &fj;
-    fs.tabs_add = [&](const std::string &k, const std::vector<double> &v) { return E->tabs.add(k, v); };
+    fs.tabs_add = [&](const std::string &k, const std::function<std::vector<double>()> &gen) {
+        return E->tabs.add_lazy(k, gen);
+    };
     fs.fft_plan = [&](int len) { return fft_plan(E->tabs, len); };
     fs.put_copy = put_copy;
     fs.ws_take = [&](size_t bytes) { return ws.take(bytes); };
@@ -511,8 +524,12 @@ int wc_engine_create(int device, int precision, wc_engine **out) {
     }
     set_radon_table(cs);
     features_init();
+    // lane 0 carries the longest dependent chain (Haralick f14): it gets the
+    // highest priority, so its blocks are dispatched ahead of the other lanes'
+    int prio_lo = 0, prio_hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
     for (int k = 0; k < WC_LANES; k++) {
-        CK(cudaStreamCreateWithFlags(&E->lanes[k], cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithPriority(&E->lanes[k], cudaStreamNonBlocking, k == 0 ? prio_hi : prio_lo));
         CK(cudaEventCreateWithFlags(&E->join_ev[k], cudaEventDisableTiming));
     }
     CK(cudaEventCreateWithFlags(&E->fork_ev, cudaEventDisableTiming));

@@ -137,8 +137,8 @@ int features_prepare(FeatureSetup &fs) {
         for (auto &j : fj[A_CHEB]) {
             const Plane &Q = P[j.plane];
             int N = std::min(20, std::min(Q.w, Q.h));
-            toff.push_back(fs.tabs_add("ch" + std::to_string(Q.w) + "_" + std::to_string(N), cheb_table(Q.w, N)));
-            toff.push_back(fs.tabs_add("ch" + std::to_string(Q.h) + "_" + std::to_string(N), cheb_table(Q.h, N)));
+            toff.push_back(fs.tabs_add("ch" + std::to_string(Q.w) + "_" + std::to_string(N), [&] { return cheb_table(Q.w, N); }));
+            toff.push_back(fs.tabs_add("ch" + std::to_string(Q.h) + "_" + std::to_string(N), [&] { return cheb_table(Q.h, N); }));
             moff.push_back((long long)tot);
             tot += (size_t)Q.h * N + 32;
         }
@@ -176,9 +176,9 @@ int features_prepare(FeatureSetup &fs) {
                 c.cnt_y = (int)ys.size();
                 char key[96];
                 snprintf(key, sizeof key, "ds%d_%.17g", Q.w, c.dx);
-                c.xs_tab = fs.tabs_add(key, xs);
+                c.xs_tab = fs.tabs_add(key, [&] { return xs; });
                 snprintf(key, sizeof key, "ds%d_%.17g", Q.h, 1 / yr);
-                c.ys_tab = fs.tabs_add(key, ys);
+                c.ys_tab = fs.tabs_add(key, [&] { return ys; });
                 c.tmp_ws = (long long)(fs.ws_take((size_t)Q.h * c.cnt_x * sizeof(double)) / sizeof(double));
             } else {
                 c.new_w = Q.w;
@@ -234,7 +234,7 @@ int features_prepare(FeatureSetup &fs) {
             hj.push_back(h);
         }
         fs.off["har_jobs"] = fs.put_copy(hj.data(), hj.size() * sizeof(HarJob));
-        fs.off["har_perm"] = fs.ws_take(4 * hj.size() * sizeof(int));
+        fs.off["har_perm"] = fs.ws_take((4 * hj.size() + 1) * sizeof(int));  // + the count of large matrices
     }
     // Edge features: magnitude / direction planes in the workspace, sorted copies
     if (!fj[A_EDGEF].empty()) {
@@ -337,12 +337,14 @@ int features_prepare(FeatureSetup &fs) {
             if (!pidx.count(n)) { pidx[n] = (int)plans.size(); plans.push_back(fs.fft_plan(n)); }
             return pidx[n];
         };
-        std::vector<double> kt;
-        for (double f0 : {0.1, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0}) {
-            std::vector<double> g = gabor_kernel(f0);
-            kt.insert(kt.end(), g.begin(), g.end());
-        }
-        fs.val["gab_kern"] = fs.tabs_add("gabor38", kt);
+        fs.val["gab_kern"] = fs.tabs_add("gabor38", [] {
+            std::vector<double> kt;
+            for (double f0 : {0.1, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0}) {
+                std::vector<double> g = gabor_kernel(f0);
+                kt.insert(kt.end(), g.begin(), g.end());
+            }
+            return kt;
+        });
         for (auto &j : fj[A_GABOR]) {
             const Plane &Q = P[j.plane];
             GabJob g;

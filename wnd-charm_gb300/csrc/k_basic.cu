@@ -499,6 +499,34 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
         else { if (line < NY) { n = 0; m = line; } else { n = line - NY + 1; m = NY - 1; } }
         int cur = -1;
         double lo = 0, hi = 0;
+        if (ang == 0 || ang == 2) {
+            // columns at 0 deg, rows at 90 deg: the bin position is a rounded,
+            // monotone function of the one coordinate that moves along the line
+            // (cos 90 deg is 6e-17, not 0), so equal values at both ends mean it
+            // is the same for every sub-pixel: split with one fraction
+            const int n1 = ang == 0 ? n : NX - 1, m1 = ang == 0 ? NY - 1 : m;
+            const double xa = -xo - 0.25 + 0.5 * n, ya = -yo - 0.25 + 0.5 * (NY - 1 - m);
+            const double xb = -xo - 0.25 + 0.5 * n1, yb = -yo - 0.25 + 0.5 * (NY - 1 - m1);
+            const double ra = __dadd_rn(__dsub_rn(__dmul_rn(xa, cs), (double)rFirst), __dmul_rn(ya, sn));
+            const double rb = __dadd_rn(__dsub_rn(__dmul_rn(xb, cs), (double)rFirst), __dmul_rn(yb, sn));
+            if (ra == rb) {
+                const int rl = (int)ra;
+                const double fr = __dadd_rn(__dsub_rn(1.0, ra), (double)rl);
+                for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
+                    double pix = p[(long long)(m / 2) * W + n / 2];
+                    if (pix == 0.0) continue;
+                    pix *= 0.25;
+                    const double pl = __dmul_rn(pix, fr);
+                    lo += pl;
+                    hi += __dsub_rn(pix, pl);
+                }
+                if (rl >= 0) {
+                    atomicAdd(&pr[rl], lo);
+                    atomicAdd(&pr[rl + 1], hi);
+                }
+                continue;
+            }
+        }
         for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
             double pix = p[(long long)(m / 2) * W + n / 2];
             if (pix == 0.0) continue;

@@ -5,9 +5,7 @@
 // Both products are FP64 register-tiled GEMMs whose threads accumulate every
 // output over k in ascending order with separate multiply and add, which is
 // the reference's order of operations (getChCoeff1D, chebyshev.cpp:82-102), so
-// on identical input the result is bit-identical to the CPU.  The mixed form
-// fuses each multiply-add (one FP64 instruction instead of two, one rounding
-// instead of two: within an ulp of the FP64 form per step).
+// on identical input the result is bit-identical to the CPU.
 #include "kcommon.cuh"
 #include "kernels.h"
 
@@ -19,7 +17,6 @@ namespace wc {
 
 // C[i][j] = sum_k A(i,k) B(k,j); A(i,k) = A[i*sai + k*sak], B(k,j) = B[k*ldb + j],
 // C[i*ldc + j].  One CTA per 64x64 tile, 256 threads, 4x4 outputs each.
-template <bool FUSED>
 __device__ void gemm_tile(const double *__restrict__ A, long long sai, long long sak, const double *__restrict__ B,
                           long long ldb, double *__restrict__ C, long long ldc, int M, int N, int K, int ti, int tj) {
     __shared__ double As[GT_K][GT_M + 1];
@@ -53,8 +50,7 @@ __device__ void gemm_tile(const double *__restrict__ A, long long sai, long long
 #pragma unroll
             for (int r = 0; r < 4; r++)
 #pragma unroll
-                for (int s = 0; s < 4; s++)
-                    acc[r][s] = FUSED ? __fma_rn(a[r], b[s], acc[r][s]) : __dadd_rn(acc[r][s], __dmul_rn(a[r], b[s]));
+                for (int s = 0; s < 4; s++) acc[r][s] = __dadd_rn(acc[r][s], __dmul_rn(a[r], b[s]));
         }
         __syncthreads();
     }
@@ -68,7 +64,6 @@ __device__ void gemm_tile(const double *__restrict__ A, long long sai, long long
 }
 
 // stage 0: Mid = I * TA ; stage 1: Out = Mid^T * TB
-template <bool FUSED>
 __global__ void __launch_bounds__(256) k_cheb_gemm(double *__restrict__ arena, const Plane *__restrict__ planes,
                                                    const TJob *__restrict__ jobs, const double *__restrict__ tabs,
                                                    const long long *__restrict__ tab_off, double *__restrict__ mid,
@@ -80,11 +75,11 @@ __global__ void __launch_bounds__(256) k_cheb_gemm(double *__restrict__ arena, c
     const double *TA = tabs + tab_off[2 * blockIdx.z], *TB = tabs + tab_off[2 * blockIdx.z + 1];
     if (stage == 0) {
         if (blockIdx.x * GT_N >= N || blockIdx.y * GT_M >= H) return;
-        gemm_tile<FUSED>(arena + S.off, W, 1, TA, N, Mid, N, H, N, W, blockIdx.y, blockIdx.x);
+        gemm_tile(arena + S.off, W, 1, TA, N, Mid, N, H, N, W, blockIdx.y, blockIdx.x);
     } else {
         const Plane D = planes[J.dst];
         if (blockIdx.x * GT_N >= N || blockIdx.y * GT_M >= N) return;
-        gemm_tile<FUSED>(Mid, 1, N, TB, N, arena + D.off, N, N, N, H, blockIdx.y, blockIdx.x);
+        gemm_tile(Mid, 1, N, TB, N, arena + D.off, N, N, N, H, blockIdx.y, blockIdx.x);
     }
 }
 
@@ -92,14 +87,12 @@ void launch_chebyshev(Ctx &c, double *arena, const Plane *planes, const TJob *jo
                       const double *tabs, const long long *tab_off, double *mid, const long long *mid_off) {
     if (njobs <= 0) return;
     const int N = maxw < maxh ? maxw : maxh;
-    const dim3 g0((N + GT_N - 1) / GT_N, (maxh + GT_M - 1) / GT_M, njobs), g1((N + GT_N - 1) / GT_N, (N + GT_M - 1) / GT_M, njobs);
-    const bool fused = c.prec == WC_PREC_MIXED;
     WC_LAUNCH(c);
-    if (fused) k_cheb_gemm<true><<<g0, 256, 0, c.st>>>(arena, planes, jobs, tabs, tab_off, mid, mid_off, 0);
-    else k_cheb_gemm<false><<<g0, 256, 0, c.st>>>(arena, planes, jobs, tabs, tab_off, mid, mid_off, 0);
+    k_cheb_gemm<<<dim3((N + GT_N - 1) / GT_N, (maxh + GT_M - 1) / GT_M, njobs), 256, 0, c.st>>>(arena, planes, jobs, tabs,
+                                                                                            tab_off, mid, mid_off, 0);
     WC_LAUNCH(c);
-    if (fused) k_cheb_gemm<true><<<g1, 256, 0, c.st>>>(arena, planes, jobs, tabs, tab_off, mid, mid_off, 1);
-    else k_cheb_gemm<false><<<g1, 256, 0, c.st>>>(arena, planes, jobs, tabs, tab_off, mid, mid_off, 1);
+    k_cheb_gemm<<<dim3((N + GT_N - 1) / GT_N, (N + GT_M - 1) / GT_M, njobs), 256, 0, c.st>>>(arena, planes, jobs, tabs,
+                                                                                         tab_off, mid, mid_off, 1);
 }
 
 }  // namespace wc

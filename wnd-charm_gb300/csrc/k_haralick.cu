@@ -409,6 +409,8 @@ __device__ __forceinline__ void hh_make3(const double v0, const double v1, const
     tau = __shfl_sync(0xffffffffu, q, 2);
 }
 
+#define QR_BIG 96  // matrices with at least this many tones get a 4-warp group in k_har_qr
+
 // Matrices in descending Ng (counting sort; the order only schedules, every
 // matrix is computed alone), so the longest QR runs start first.
 __global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj, const char *__restrict__ wsb, int nmat,
@@ -434,30 +436,37 @@ __global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj
         const int n = ((const int *)(wsb + hj[m >> 2].lut_b))[256];
         perm[atomicAdd(&cnt[256 - n], 1)] = m;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) perm[nmat] = cnt[256 - QR_BIG];  // after placement cnt[k] = end of key k: matrices with Ng >= QR_BIG
 }
 
-__global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb, const int *__restrict__ perm) {
-    __shared__ double rowsum[256];
-    const int lane = threadIdx.x & 31;
-    const int m = perm[blockIdx.x];
-    const int job = m >> 2, ang = m & 3;
-    const HarJob H = hj[job];
-    const int n = ((const int *)(wsb + H.lut_b))[256];
-    double *res = (double *)(wsb + H.res_b) + ang * 14;
+#define QR_SYNC()                    \
+    do {                             \
+        if (NW > 1) __syncthreads(); \
+        else __syncwarp();           \
+    } while (0)
+// One matrix per group of NW warps (tid = thread in the group): every thread
+// takes the same decisions from the same values; writes of single entries are
+// made by tid 0; the reflector updates spread their columns / rows over the
+// group, with a barrier between dependent phases.
+template <int NW>
+__device__ void har_schur(double *__restrict__ A, const int n, double *__restrict__ rowsum, double *__restrict__ res,
+                          const int tid) {
+    const int lane = tid & 31;
+    constexpr int GS = 32 * NW;
     if (n < 3) {
-        if (lane == 0) res[13] = 0.0;
+        if (tid == 0) res[13] = 0.0;
         return;
     }
-    double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
 #define T_(r, c) A[(long long)(r) * n + (c)]
     // computeNormOfT: row sums (sequential within a row), then rows in order
-    for (int j = lane; j < n; j += 32) {
+    for (int j = tid; j < n; j += GS) {
         const int s0 = j - 1 > 0 ? j - 1 : 0;
         double s = 0;
         for (int c = s0; c < n; c++) s = __dadd_rn(s, fabs(T_(j, c)));
         rowsum[j] = s;
     }
-    __syncwarp();
+    QR_SYNC();
     double norm = 0;
     for (int j = 0; j < n; j++) norm = __dadd_rn(norm, rowsum[j]);
     const double eps = DBL_EPSILON;
@@ -484,23 +493,23 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                 }
             }
             if (il == iu) {
-                __syncwarp();
-                if (lane == 0) {
+                QR_SYNC();
+                if (tid == 0) {
                     T_(iu, iu) = __dadd_rn(T_(iu, iu), exshift);
                     if (iu > 0) T_(iu, iu - 1) = 0;
                 }
-                __syncwarp();
+                QR_SYNC();
                 iu--;
                 iter = 0;
             } else if (il == iu - 1) {
                 const double p = __dmul_rn(0.5, __dsub_rn(T_(iu - 1, iu - 1), T_(iu, iu)));
                 const double q = __dadd_rn(__dmul_rn(p, p), __dmul_rn(T_(iu, iu - 1), T_(iu - 1, iu)));
-                __syncwarp();
-                if (lane == 0) {
+                QR_SYNC();
+                if (tid == 0) {
                     T_(iu, iu) = __dadd_rn(T_(iu, iu), exshift);
                     T_(iu - 1, iu - 1) = __dadd_rn(T_(iu - 1, iu - 1), exshift);
                 }
-                __syncwarp();
+                QR_SYNC();
                 if (q >= 0) {
                     const double z = sqrt(fabs(q));
                     const double gp = (p >= 0) ? __dadd_rn(p, z) : __dsub_rn(p, z), gq = T_(iu, iu - 1);
@@ -520,8 +529,9 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                         s = -1 / u;
                         c = __dmul_rn(-t, s);
                     }
+                    QR_SYNC();  // every thread has read gq before the block changes
                     // the 2x2 block: left (rows iu-1, iu), then right (cols iu-1, iu)
-                    if (lane == 0) {
+                    if (tid == 0) {
                         for (int col = iu - 1; col <= iu; col++) {
                             const double xi = T_(iu - 1, col), yi = T_(iu, col);
                             T_(iu - 1, col) = __dadd_rn(__dmul_rn(c, xi), __dmul_rn(-s, yi));
@@ -535,17 +545,17 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                         T_(iu, iu - 1) = 0;
                     }
                 }
-                if (lane == 0 && iu > 1) T_(iu - 1, iu - 2) = 0;
-                __syncwarp();
+                if (tid == 0 && iu > 1) T_(iu - 1, iu - 2) = 0;
+                QR_SYNC();
                 iu -= 2;
                 iter = 0;
             } else {
                 double sh0 = T_(iu, iu), sh1 = T_(iu - 1, iu - 1), sh2 = __dmul_rn(T_(iu, iu - 1), T_(iu - 1, iu));
                 if (iter == 10) {
                     exshift = __dadd_rn(exshift, sh0);
-                    __syncwarp();
-                    for (int i = lane; i <= iu; i += 32) T_(i, i) = __dsub_rn(T_(i, i), sh0);
-                    __syncwarp();
+                    QR_SYNC();
+                    for (int i = tid; i <= iu; i += GS) T_(i, i) = __dsub_rn(T_(i, i), sh0);
+                    QR_SYNC();
                     const double s = __dadd_rn(fabs(T_(iu, iu - 1)), fabs(T_(iu - 1, iu - 2)));
                     sh0 = __dmul_rn(0.75, s);
                     sh1 = __dmul_rn(0.75, s);
@@ -560,9 +570,9 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                         s = __dadd_rn(s, __dsub_rn(sh1, sh0) / 2.0);
                         s = __dsub_rn(sh0, sh2 / s);
                         exshift = __dadd_rn(exshift, s);
-                        __syncwarp();
-                        for (int i = lane; i <= iu; i += 32) T_(i, i) = __dsub_rn(T_(i, i), s);
-                        __syncwarp();
+                        QR_SYNC();
+                        for (int i = tid; i <= iu; i += GS) T_(i, i) = __dsub_rn(T_(i, i), s);
+                        QR_SYNC();
                         sh0 = sh1 = sh2 = 0.964;
                     }
                 }
@@ -592,13 +602,13 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                     double ess[2], tau, beta;
                     if (first) hh_make3(fv0, fv1, fv2, lane, ess[0], ess[1], tau, beta);
                     else hh_make3(T_(k, k - 1), T_(k + 1, k - 1), T_(k + 2, k - 1), lane, ess[0], ess[1], tau, beta);
-                    __syncwarp();
+                    QR_SYNC();
                     if (beta != 0) {
-                        if (lane == 0) {
+                        if (tid == 0) {
                             if (first && k > il) T_(k, k - 1) = -T_(k, k - 1);
                             else if (!first) T_(k, k - 1) = beta;
                         }
-                        for (int cc = k + lane; cc <= iu; cc += 32) {  // left: rows k..k+2
+                        for (int cc = k + tid; cc <= iu; cc += GS) {  // left: rows k..k+2
                             const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
                             double t = plus_zero(__dmul_rn(ess[0], a1));
                             t = __dadd_rn(t, __dmul_rn(ess[1], a2));
@@ -607,9 +617,9 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                             T_(k + 1, cc) = __dsub_rn(a1, __dmul_rn(__dmul_rn(tau, ess[0]), t));
                             T_(k + 2, cc) = __dsub_rn(a2, __dmul_rn(__dmul_rn(tau, ess[1]), t));
                         }
-                        __syncwarp();
+                        QR_SYNC();
                         const int rend = min(iu, k + 3);
-                        for (int rr = il + lane; rr <= rend; rr += 32) {  // right: cols k..k+2
+                        for (int rr = il + tid; rr <= rend; rr += GS) {  // right: cols k..k+2
                             const double b0 = T_(rr, k), b1 = T_(rr, k + 1), b2 = T_(rr, k + 2);
                             double t = plus_zero(__dmul_rn(b1, ess[0]));
                             t = __dadd_rn(t, __dmul_rn(b2, ess[1]));
@@ -620,23 +630,23 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                             T_(rr, k + 2) = __dsub_rn(b2, __dmul_rn(tt, ess[1]));
                         }
                     }
-                    __syncwarp();
+                    QR_SYNC();
                 }
                 {
                     double vv[2] = {T_(iu - 1, iu - 2), T_(iu, iu - 2)}, ess[1], tau, beta;
                     hh_make(vv, 2, ess, tau, beta);
-                    __syncwarp();
+                    QR_SYNC();
                     if (beta != 0) {
-                        if (lane == 0) T_(iu - 1, iu - 2) = beta;
-                        for (int cc = iu - 1 + lane; cc <= iu; cc += 32) {
+                        if (tid == 0) T_(iu - 1, iu - 2) = beta;
+                        for (int cc = iu - 1 + tid; cc <= iu; cc += GS) {
                             const double a0 = T_(iu - 1, cc), a1 = T_(iu, cc);
                             double t = __dadd_rn(__dmul_rn(ess[0], a1), 0.0);
                             t = __dadd_rn(t, a0);
                             T_(iu - 1, cc) = __dsub_rn(a0, __dmul_rn(tau, t));
                             T_(iu, cc) = __dsub_rn(a1, __dmul_rn(__dmul_rn(tau, ess[0]), t));
                         }
-                        __syncwarp();
-                        for (int rr = il + lane; rr <= iu; rr += 32) {
+                        QR_SYNC();
+                        for (int rr = il + tid; rr <= iu; rr += GS) {
                             const double b0 = T_(rr, iu - 1), b1 = T_(rr, iu);
                             double t = __dadd_rn(__dmul_rn(b1, ess[0]), 0.0);
                             t = __dadd_rn(t, b0);
@@ -645,17 +655,17 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
                             T_(rr, iu) = __dsub_rn(b1, __dmul_rn(tt, ess[0]));
                         }
                     }
-                    __syncwarp();
+                    QR_SYNC();
                 }
-                for (int i = im + 2 + lane; i <= iu; i += 32) {
+                for (int i = im + 2 + tid; i <= iu; i += GS) {
                     T_(i, i - 2) = 0;
                     if (i > im + 2) T_(i, i - 3) = 0;
                 }
-                __syncwarp();
+                QR_SYNC();
             }
         }
     }
-    if (lane == 0) {
+    if (tid == 0) {
         double f = 0;
         if (!failed) {
             // eigenvalue #2 in Schur order (EigenSolver::compute, EigenSolver.h:363-381)
@@ -677,6 +687,32 @@ __global__ void __launch_bounds__(32) k_har_qr(const HarJob *__restrict__ hj, ch
         res[13] = f;  // no convergence: 0, as the oracle
     }
 #undef T_
+}
+
+// Matrices with at least QR_BIG tones (the long chains) get 4 warps each, one
+// per SM sub-partition, which quarters the reflector updates on the critical
+// path; the rest run one per warp, 4 to a block.  perm lists the matrices by
+// descending Ng and nbig counts the large ones.
+__global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb,
+                                                const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat) {
+    __shared__ double rowsum[4][256];
+    const int nbig = *nbig_p;
+    int m, wq = 0;
+    if ((int)blockIdx.x < nbig) {
+        m = perm[blockIdx.x];
+    } else {
+        wq = threadIdx.x >> 5;
+        const int idx = nbig + ((int)blockIdx.x - nbig) * 4 + wq;
+        if (idx >= nmat) return;
+        m = perm[idx];
+    }
+    const HarJob H = hj[m >> 2];
+    const int ang = m & 3;
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    double *res = (double *)(wsb + H.res_b) + ang * 14;
+    double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
+    if ((int)blockIdx.x < nbig) har_schur<4>(A, n, rowsum[0], res, threadIdx.x);
+    else har_schur<1>(A, n, rowsum[wq], res, threadIdx.x & 31);
 }
 
 // mean and range over the angles, permuted into the output order
@@ -722,7 +758,7 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     WC_LAUNCH(c);
     k_har_order<<<1, 256, 0, c.st>>>(hj, wsb, 4 * njobs, perm);
     WC_LAUNCH(c);
-    k_har_qr<<<4 * njobs, 32, 0, c.st>>>(hj, wsb, perm);
+    k_har_qr<<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs);
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);
 }

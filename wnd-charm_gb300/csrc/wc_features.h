@@ -14,7 +14,8 @@ struct FeatureSetup {
     // inputs
     const std::vector<Plane> *planes;
     const std::vector<std::vector<FJob>> *fj;  // per algorithm
-    std::function<long long(const std::string &, const std::vector<double> &)> tabs_add;
+    // table by key; the generator runs only for a key the engine has not seen
+    std::function<long long(const std::string &, const std::function<std::vector<double>()> &)> tabs_add;
     std::function<FFTPlan(int)> fft_plan;
     std::function<size_t(const void *, size_t)> put_copy;  // metadata blob, returns offset
     std::function<size_t(size_t)> ws_take;                 // workspace bytes, returns offset

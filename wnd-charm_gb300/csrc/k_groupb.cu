@@ -67,14 +67,8 @@ __global__ void k_zern_moments(const double *__restrict__ arena, const Plane *__
 #define ZCHUNK 2048
 // second pass: per (chunk of pixels, half, job): per-CTA partial AR/AI.
 // HALF 0 covers n = 0..10, HALF 1 covers n = 11..15 (36 (n, m) pairs each).
-// FAST = false is the FP64 form, with the reference's divisions (x / rad,
-// x / r, H3 / r^2, (n + 1) f / pi); FAST = true (mixed form) takes one
-// reciprocal per pixel and multiplies, and folds (n + 1) / pi: each such term
-// moves by at most an ulp or two, and the FP64 pipe does about half the work.
-// (FP32 is not used here: the order-15 moments of planes with mixed signs
-// cancel heavily, and FP32 basis rounding shows up at 1e-4 of the largest
-// coefficient.)
-template <int HALF, bool FAST>
+// (FP64 form, the reference's operations; the mixed form uses k_zern_cmom.)
+template <int HALF>
 __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ arena, const Plane *__restrict__ planes,
                                                     const FJob *__restrict__ jobs, const double *__restrict__ mom,
                                                     double *__restrict__ part, int nchunk) {
@@ -90,21 +84,19 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
     if (c0 < npix) {
         const double sum = mom[3 * blockIdx.z], cx = mom[3 * blockIdx.z + 1], cy = mom[3 * blockIdx.z + 2];
         const double rad = (double)(P.w < P.h ? P.w : P.h);
-        const double inv_rad = 1.0 / rad, inv_sum = 1.0 / sum;
         const double *p = arena + P.off;
         const long long c1 = min(npix, c0 + ZCHUNK);
         for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
             const long long yy = i / P.w, xx = i - yy * P.w;
             const double dx = __dsub_rn((double)(xx + 1), cx), dy = __dsub_rn((double)(yy + 1), cy);
-            const double x = FAST ? dx * inv_rad : dx / rad, y = FAST ? dy * inv_rad : dy / rad;
+            const double x = dx / rad, y = dy / rad;
             const double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), r = sqrt(r2);
             if (r < DBL_EPSILON || r > 1.0) continue;
             double R[16], CO[16], SI[16];
             R[0] = 1;
 #pragma unroll
             for (int n = 1; n <= 15; n++) R[n] = r * R[n - 1];
-            const double inv_r = FAST ? 1.0 / r : 0.0, inv_r2 = inv_r * inv_r;
-            const double a = FAST ? x * inv_r : x / r, b = FAST ? y * inv_r : y / r;
+            const double a = x / r, b = y / r;
             CO[0] = a;
             SI[0] = b;
 #pragma unroll
@@ -112,11 +104,11 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
                 CO[m] = a * CO[m - 1] - b * SI[m - 1];
                 SI[m] = a * SI[m - 1] + b * CO[m - 1];
             }
-            const double f = FAST ? p[i] * inv_sum : p[i] / sum;
+            const double f = p[i] / sum;
             int q = 0;
 #pragma unroll
             for (int n = NLO; n <= NHI; n++) {
-                const double ct = FAST ? f * ((n + 1) / kZPI) : (n + 1) * f / kZPI;
+                const double ct = (n + 1) * f / kZPI;
                 const double Rn = R[n], Rnm2 = n >= 2 ? R[n - 2] : 0.0;
                 double Rnm = 0, Rnmp2 = 0, Rnmp4 = 0;
                 const int cnt = n / 2 + 1;
@@ -130,8 +122,7 @@ __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ a
                         Rnm = n * Rn - (n - 1) * Rnm2;
                         Rnmp2 = Rnm;
                     } else {
-                        const double h3 = FAST ? c_zH3[n][m] * inv_r2 : c_zH3[n][m] / r2;
-                        Rnm = c_zH1[n][m] * Rnmp4 + (c_zH2[n][m] + h3) * Rnmp2;
+                        Rnm = c_zH1[n][m] * Rnmp4 + (c_zH2[n][m] + (c_zH3[n][m] / r2)) * Rnmp2;
                         Rnmp4 = Rnmp2;
                         Rnmp2 = Rnm;
                     }
@@ -174,22 +165,146 @@ __global__ void k_zern_finish(const FJob *__restrict__ jobs, const double *__res
     feat[J.out + t] = fabs(sqrt(ar + ai));
 }
 
+// Mixed form: the same moments through complex moments.  With the reference's
+// angular factor cos((m+1) phi), sin((m+1) phi) (its COST/SINT arrays start at
+// the first harmonic, zernike.cpp:287-296) and R_nm(r) = sum_s c_nms r^(n-2s),
+//   R_nm e^{-i(m+1) phi} = sum_s c_nms (r^2)^j zbar^(m+1) / r,   j = (n-m)/2 - s,
+// zbar = x - i y; so A_nm = (n+1)/pi sum_s c_nms M(j, m+1) with the 72 complex
+// moments M(j, m') = sum f (r^2)^j zbar^m' / r (FP64, about half the FP64
+// instructions per pixel of the q-recursion), and the exact integer
+// coefficients c_nms = (-1)^s (n-s)! / (s! ((n+m)/2-s)! ((n-m)/2-s)!) applied once
+// per job in FP64.  HALF 0: m' = 1..5, HALF 1: m' = 6..16 (36 moments each,
+// m' ascending, j = 0..(16-m')/2 ascending).
+template <int HALF>
+__global__ void __launch_bounds__(256) k_zern_cmom(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                   const FJob *__restrict__ jobs, const double *__restrict__ mom,
+                                                   double *__restrict__ part, int nchunk) {
+    constexpr int M0 = HALF ? 6 : 1, M1 = HALF ? 16 : 5, JMAX = (16 - M0) / 2;
+    __shared__ double red[8][72];
+    const FJob J = jobs[blockIdx.z];
+    const Plane P = planes[J.plane];
+    const long long npix = (long long)P.w * P.h;
+    const long long c0 = (long long)blockIdx.x * ZCHUNK;
+    double acc[72];
+#pragma unroll
+    for (int q = 0; q < 72; q++) acc[q] = 0.0;
+    if (c0 < npix) {
+        const double sum = mom[3 * blockIdx.z], cx = mom[3 * blockIdx.z + 1], cy = mom[3 * blockIdx.z + 2];
+        const double inv_rad = 1.0 / (double)(P.w < P.h ? P.w : P.h), inv_sum = 1.0 / sum;
+        const double *p = arena + P.off;
+        const long long c1 = min(npix, c0 + ZCHUNK);
+        for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+            const long long yy = i / P.w, xx = i - yy * P.w;
+            const double x = __dsub_rn((double)(xx + 1), cx) * inv_rad, y = __dsub_rn((double)(yy + 1), cy) * inv_rad;
+            const double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), r = sqrt(r2);
+            if (r < DBL_EPSILON || r > 1.0) continue;
+            double q[JMAX + 1];
+            q[0] = p[i] * inv_sum / r;
+#pragma unroll
+            for (int j = 1; j <= JMAX; j++) q[j] = q[j - 1] * r2;
+            double zr = x, zi = -y;  // zbar^1
+#pragma unroll
+            for (int mp = 2; mp <= M0; mp++) {
+                const double t = zr * x + zi * y;  // (zr + i zi)(x - i y)
+                zi = zi * x - zr * y;
+                zr = t;
+            }
+            int slot = 0;
+#pragma unroll
+            for (int mp = M0; mp <= M1; mp++) {
+                if (mp > M0) {
+                    const double t = zr * x + zi * y;
+                    zi = zi * x - zr * y;
+                    zr = t;
+                }
+#pragma unroll
+                for (int j = 0; j <= (16 - mp) / 2; j++) {
+                    acc[2 * slot] += q[j] * zr;
+                    acc[2 * slot + 1] += q[j] * zi;
+                    slot++;
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int qq = 0; qq < 72; qq++) {
+        double v = warp_sum(acc[qq]);
+        if (lane == 0) red[wid][qq] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 72) {
+        double s = 0;
+        for (int w = 0; w < 8; w++) s += red[w][threadIdx.x];
+        part[(((long long)blockIdx.z * 2 + HALF) * nchunk + blockIdx.x) * 72 + threadIdx.x] = s;
+    }
+}
+
+__device__ __forceinline__ double dfact(int k) {
+    double f = 1;
+    for (int i = 2; i <= k; i++) f *= i;
+    return f;
+}
+
+__global__ void k_zern_finish_cmom(const FJob *__restrict__ jobs, const double *__restrict__ part, int nchunk,
+                                   double *__restrict__ feat) {
+    __shared__ double M[144];
+    const FJob J = jobs[blockIdx.x];
+    const int t = threadIdx.x;
+    for (int v = t; v < 144; v += blockDim.x) {
+        const int half = v >= 72, k = v - 72 * half;
+        double s = 0;
+        for (int c = 0; c < nchunk; c++) s += part[(((long long)blockIdx.x * 2 + half) * nchunk + c) * 72 + k];
+        M[v] = s;
+    }
+    __syncthreads();
+    if (t >= 72) return;
+    int n = 0, m = 0, idx = 0;  // output t is the t-th (n, m), n ascending, m ascending, n - m even
+    for (n = 0; n <= 15; n++) {
+        const int cnt = n / 2 + 1;
+        if (t < idx + cnt) {
+            m = (n & 1) + 2 * (t - idx);
+            break;
+        }
+        idx += cnt;
+    }
+    const int mp = m + 1, half = mp >= 6, m0 = half ? 6 : 1;
+    int base = 0;
+    for (int u = m0; u < mp; u++) base += (16 - u) / 2 + 1;
+    double zr = 0, zi = 0;
+    for (int s = 0; s <= (n - m) / 2; s++) {
+        const double c = ((s & 1) ? -1.0 : 1.0) * dfact(n - s) / (dfact(s) * dfact((n + m) / 2 - s) * dfact((n - m) / 2 - s));
+        const int j = (n - m) / 2 - s;
+        const int v = 72 * half + 2 * (base + j);
+        zr += c * M[v];
+        zi += c * M[v + 1];
+    }
+    const double sc = (n + 1) / kZPI;
+    double ar = zr * sc, ai = zi * sc;
+    ar *= ar;
+    ai *= ai;
+    feat[J.out + t] = fabs(sqrt(ar + ai));
+}
+
 void launch_zernike(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, long long maxpix,
                     double *mom, double *part, double *feat) {
     if (njobs <= 0) return;
     const int nchunk = (int)((maxpix + ZCHUNK - 1) / ZCHUNK);
     WC_LAUNCH(c);
     k_zern_moments<<<njobs, 512, 0, c.st>>>(arena, planes, jobs, mom);
+    if (c.prec == WC_PREC_MIXED) {
+        WC_LAUNCH(c);
+        k_zern_cmom<0><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+        WC_LAUNCH(c);
+        k_zern_cmom<1><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+        WC_LAUNCH(c);
+        k_zern_finish_cmom<<<njobs, 160, 0, c.st>>>(jobs, part, nchunk, feat);
+        return;
+    }
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED)
-        k_zern_accum<0, true><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
-    else
-        k_zern_accum<0, false><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+    k_zern_accum<0><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED)
-        k_zern_accum<1, true><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
-    else
-        k_zern_accum<1, false><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+    k_zern_accum<1><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
     WC_LAUNCH(c);
     k_zern_finish<<<njobs, 96, 0, c.st>>>(jobs, part, nchunk, feat);
 }

@@ -293,6 +293,8 @@ __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict
 // tail sum, then H A on the trailing rows and A H on all rows.  One CTA per
 // matrix; products that the reference forms per element (tau * ess_r, tau * t)
 // are formed once, with the same value.
+// FUSED (mixed form): fused multiply-adds in the two updates.
+template <bool FUSED>
 __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
     __shared__ double v[256], ess[256], tess[256];
     __shared__ double s_tau, s_beta, s_den;
@@ -341,6 +343,13 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
                 continue;
             }
             double t = 0;
+            if (FUSED) {
+                for (int r = 1; r < rem; r++) t = __fma_rn(ess[r - 1], col[(long long)r * n], t);
+                t = __dadd_rn(t, col[0]);
+                col[0] = __fma_rn(-tau, t, col[0]);
+                for (int r = 1; r < rem; r++) col[(long long)r * n] = __fma_rn(-tess[r - 1], t, col[(long long)r * n]);
+                continue;
+            }
             for (int r = 1; r < rem; r++) t = __dadd_rn(t, __dmul_rn(ess[r - 1], col[(long long)r * n]));
             t = __dadd_rn(t, col[0]);
             col[0] = __dsub_rn(col[0], __dmul_rn(tau, t));
@@ -355,6 +364,14 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
                 continue;
             }
             double t = 0;
+            if (FUSED) {
+                for (int c = 1; c < rem; c++) t = __fma_rn(row[c], ess[c - 1], t);
+                t = __dadd_rn(t, row[0]);
+                const double tt = __dmul_rn(tau, t);
+                row[0] = __dsub_rn(row[0], tt);
+                for (int c = 1; c < rem; c++) row[c] = __fma_rn(-tt, ess[c - 1], row[c]);
+                continue;
+            }
             for (int c = 1; c < rem; c++) t = __dadd_rn(t, __dmul_rn(row[c], ess[c - 1]));
             t = __dadd_rn(t, row[0]);
             const double tt = __dmul_rn(tau, t);
@@ -449,7 +466,10 @@ __global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj
 // takes the same decisions from the same values; writes of single entries are
 // made by tid 0; the reflector updates spread their columns / rows over the
 // group, with a barrier between dependent phases.
-template <int NW>
+// FUSED (mixed form): the bulge-chasing updates use fused multiply-adds, as a
+// reference build with FP contraction does; f14 then follows that build's
+// rounding instead of the oracle's (it is range-checked, never compared).
+template <int NW, bool FUSED>
 __device__ void har_schur(double *__restrict__ A, const int n, double *__restrict__ rowsum, double *__restrict__ res,
                           const int tid) {
     const int lane = tid & 31;
@@ -610,6 +630,13 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                         }
                         for (int cc = k + tid; cc <= iu; cc += GS) {  // left: rows k..k+2
                             const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
+                            if (FUSED) {
+                                const double t = __dadd_rn(__fma_rn(ess[1], a2, __dmul_rn(ess[0], a1)), a0);
+                                T_(k, cc) = __fma_rn(-tau, t, a0);
+                                T_(k + 1, cc) = __fma_rn(-__dmul_rn(tau, ess[0]), t, a1);
+                                T_(k + 2, cc) = __fma_rn(-__dmul_rn(tau, ess[1]), t, a2);
+                                continue;
+                            }
                             double t = plus_zero(__dmul_rn(ess[0], a1));
                             t = __dadd_rn(t, __dmul_rn(ess[1], a2));
                             t = __dadd_rn(t, a0);
@@ -621,6 +648,13 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                         const int rend = min(iu, k + 3);
                         for (int rr = il + tid; rr <= rend; rr += GS) {  // right: cols k..k+2
                             const double b0 = T_(rr, k), b1 = T_(rr, k + 1), b2 = T_(rr, k + 2);
+                            if (FUSED) {
+                                const double tt = __dmul_rn(tau, __dadd_rn(__fma_rn(b2, ess[1], __dmul_rn(b1, ess[0])), b0));
+                                T_(rr, k) = __dsub_rn(b0, tt);
+                                T_(rr, k + 1) = __fma_rn(-tt, ess[0], b1);
+                                T_(rr, k + 2) = __fma_rn(-tt, ess[1], b2);
+                                continue;
+                            }
                             double t = plus_zero(__dmul_rn(b1, ess[0]));
                             t = __dadd_rn(t, __dmul_rn(b2, ess[1]));
                             t = __dadd_rn(t, b0);
@@ -693,6 +727,7 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
 // per SM sub-partition, which quarters the reflector updates on the critical
 // path; the rest run one per warp, 4 to a block.  perm lists the matrices by
 // descending Ng and nbig counts the large ones.
+template <bool FUSED>
 __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb,
                                                 const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat) {
     __shared__ double rowsum[4][256];
@@ -711,8 +746,8 @@ __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, c
     const int n = ((const int *)(wsb + H.lut_b))[256];
     double *res = (double *)(wsb + H.res_b) + ang * 14;
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
-    if ((int)blockIdx.x < nbig) har_schur<4>(A, n, rowsum[0], res, threadIdx.x);
-    else har_schur<1>(A, n, rowsum[wq], res, threadIdx.x & 31);
+    if ((int)blockIdx.x < nbig) har_schur<4, FUSED>(A, n, rowsum[0], res, threadIdx.x);
+    else har_schur<1, FUSED>(A, n, rowsum[wq], res, threadIdx.x & 31);
 }
 
 // mean and range over the angles, permuted into the output order
@@ -754,11 +789,13 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     WC_LAUNCH(c);
     k_har_q<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
     WC_LAUNCH(c);
-    k_har_hess<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    if (c.prec == WC_PREC_MIXED) k_har_hess<true><<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    else k_har_hess<false><<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
     WC_LAUNCH(c);
     k_har_order<<<1, 256, 0, c.st>>>(hj, wsb, 4 * njobs, perm);
     WC_LAUNCH(c);
-    k_har_qr<<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs);
+    if (c.prec == WC_PREC_MIXED) k_har_qr<true><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs);
+    else k_har_qr<false><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs);
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);
 }

@@ -349,7 +349,12 @@ def main():
             cmp = compare_mixed if args.precision == "mixed" else compare
             if cmp(mixed_rows[i], ref[i], names):
                 ok = False
-        line["error_vs_oracle"] = {"images": ncpu, "tolerances_met": ok,
+        # f14 (Haralick in-group 16, 17) is range-checked only; report how often it agrees anyway
+        from parity import F14, group_of, index_of
+        f14i = np.array([i for i, nm in enumerate(names) if group_of(nm).startswith("Haralick") and index_of(nm) in F14])
+        a14, b14 = mixed_rows[:ncpu][:, f14i], ref[:ncpu][:, f14i]
+        f14_agree = float(np.mean(np.abs(a14 - b14) <= 1e-6 * np.maximum(np.abs(b14), 1e-12)))
+        line["error_vs_oracle"] = {"images": ncpu, "tolerances_met": ok, "f14_agree_1e-6": f14_agree,
                                    "max_rel": {k: float("%.3g" % v[0]) for k, v in sorted(errs.items())},
                                    "max_rel_to_group_max": {k: float("%.3g" % v[1]) for k, v in sorted(errs.items())},
                                    "worst": {k: v[2] for k, v in sorted(errs.items()) if v[1] > 0}}

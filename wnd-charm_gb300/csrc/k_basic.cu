@@ -467,9 +467,19 @@ void set_radon_table(const double *cs8) { cudaMemcpyToSymbol(c_radon_cs, cs8, 8 
 // linear split between two bins) + vd_RadonTextures, src/cmatrix.cpp:1463-1514,
 // src/transforms/radon.cpp:14-115.  One CTA per (plane, angle); projections in
 // shared memory, then a 3-bin histogram per angle.
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+
+// R = double: FP64 form.  R = float (mixed form): FP32 projections and splits;
+// the bin of a sub-pixel comes from an FP32 estimate of its position, and from
+// the exact FP64 position whenever the estimate lies within 4e-3 of a bin
+// boundary (the estimate's error is below 1e-3 for images up to 2048 px), so
+// every sub-pixel lands in the bin the FP64 form gives it.
+template <typename R>
 __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
-                        double *__restrict__ feat, double *__restrict__ proj_ws, int rsize_max) {
-    extern __shared__ double pr[];
+                        double *__restrict__ feat, int rsize_max) {
+    extern __shared__ __align__(16) unsigned char rsm[];
+    R *pr = (R *)rsm;
     __shared__ double sh[32];
     const FJob J = jobs[blockIdx.y];
     const Plane P = planes[J.plane];
@@ -477,7 +487,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
     const int rLast = (int)ceil(sqrt(pow((double)(W - 1 - (W - 1) / 2), 2) + pow((double)(H - 1 - (H - 1) / 2), 2))) + 1;
     const int rFirst = -rLast, rSize = rLast - rFirst + 1;
     const int xo = (W - 1) / 2, yo = (H - 1) / 2;
-    for (int i = threadIdx.x; i < rSize; i += blockDim.x) pr[i] = 0.0;
+    for (int i = threadIdx.x; i < rSize; i += blockDim.x) pr[i] = (R)0;
     __syncthreads();
     const double cs = c_radon_cs[2 * ang], sn = c_radon_cs[2 * ang + 1];
     const double *p = arena + P.off;
@@ -498,7 +508,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
         else if (ang == 1) { if (line < NX) { n = line; m = 0; } else { n = 0; m = line - NX + 1; } }
         else { if (line < NY) { n = 0; m = line; } else { n = line - NY + 1; m = NY - 1; } }
         int cur = -1;
-        double lo = 0, hi = 0;
+        R lo = 0, hi = 0;
         if (ang == 0 || ang == 2) {
             // columns at 0 deg, rows at 90 deg: the bin position is a rounded,
             // monotone function of the one coordinate that moves along the line
@@ -511,14 +521,14 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
             const double rb = __dadd_rn(__dsub_rn(__dmul_rn(xb, cs), (double)rFirst), __dmul_rn(yb, sn));
             if (ra == rb) {
                 const int rl = (int)ra;
-                const double fr = __dadd_rn(__dsub_rn(1.0, ra), (double)rl);
+                const R fr = (R)__dadd_rn(__dsub_rn(1.0, ra), (double)rl);
                 for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
-                    double pix = p[(long long)(m / 2) * W + n / 2];
-                    if (pix == 0.0) continue;
-                    pix *= 0.25;
-                    const double pl = __dmul_rn(pix, fr);
+                    const double pd = p[(long long)(m / 2) * W + n / 2];
+                    if (pd == 0.0) continue;
+                    const R pix = (R)pd * (R)0.25;
+                    const R pl = rmul(pix, fr);  // no contraction into the sum (the FP64 form's rounding)
                     lo += pl;
-                    hi += __dsub_rn(pix, pl);
+                    hi += pix - pl;
                 }
                 if (rl >= 0) {
                     atomicAdd(&pr[rl], lo);
@@ -527,15 +537,32 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 continue;
             }
         }
+        const float csf = (float)cs, snf = (float)sn, rff = (float)rFirst;
         for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
-            double pix = p[(long long)(m / 2) * W + n / 2];
-            if (pix == 0.0) continue;
-            pix *= 0.25;
+            const double pd = p[(long long)(m / 2) * W + n / 2];
+            if (pd == 0.0) continue;
             const double xT = -xo - 0.25 + 0.5 * n;              // exact: multiples of 0.25
             const double yT = -yo - 0.25 + 0.5 * (NY - 1 - m);   // exact
-            const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
-            const int rl = (int)ri;
-            const double pl = __dmul_rn(pix, __dadd_rn(__dsub_rn(1.0, ri), (double)rl));
+            int rl;
+            R pix, pl;
+            bool exact = sizeof(R) == 8;
+            if (!exact) {
+                const float rif = fmaf((float)yT, snf, fmaf((float)xT, csf, -rff));
+                const float fl = floorf(rif), fr = rif - fl;
+                if (fr < 4e-3f || fr > 1.f - 4e-3f) exact = true;
+                else {
+                    rl = (int)fl;
+                    pix = (R)pd * (R)0.25;
+                    pl = rmul(pix, (R)(1.f - fr));
+                }
+            }
+            if (exact) {
+                const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
+                rl = (int)ri;
+                const double pdq = pd * 0.25;
+                pix = (R)pdq;
+                pl = (R)__dmul_rn(pdq, __dadd_rn(__dsub_rn(1.0, ri), (double)rl));
+            }
             if (rl != cur) {
                 if (cur >= 0) {
                     atomicAdd(&pr[cur], lo);
@@ -546,7 +573,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 hi = 0;
             }
             lo += pl;
-            hi += __dsub_rn(pix, pl);
+            hi += pix - pl;
         }
         if (cur >= 0) {
             atomicAdd(&pr[cur], lo);
@@ -556,8 +583,8 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
     __syncthreads();
     double lo = 10E200, hi = -10E200;
     for (int i = threadIdx.x; i < rSize; i += blockDim.x) {
-        lo = fmin(lo, pr[i]);
-        hi = fmax(hi, pr[i]);
+        lo = fmin(lo, (double)pr[i]);
+        hi = fmax(hi, (double)pr[i]);
     }
     lo = block_min(lo, sh);
     hi = block_max(hi, sh);
@@ -565,7 +592,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
     if (threadIdx.x < 3) bins[threadIdx.x] = 0;
     __syncthreads();
     const double sc = hist_scale(lo, hi, 3);
-    for (int i = threadIdx.x; i < rSize; i += blockDim.x) atomicAdd(&bins[hist_bin(pr[i], lo, sc, 3)], 1u);
+    for (int i = threadIdx.x; i < rSize; i += blockDim.x) atomicAdd(&bins[hist_bin((double)pr[i], lo, sc, 3)], 1u);
     __syncthreads();
     if (threadIdx.x < 3) {
         // raw index ang*3 + b, permuted by vd_RadonTextures: out = [0 1 2 9 10 11 3 4 5 6 7 8]
@@ -581,7 +608,8 @@ void launch_radon(Ctx &c, const double *arena, const Plane *planes, const FJob *
     int rLast = (int)ceil(sqrt(pow((double)(maxw - 1 - (maxw - 1) / 2), 2) + pow((double)(maxh - 1 - (maxh - 1) / 2), 2))) + 1;
     int rsize = 2 * rLast + 1;
     WC_LAUNCH(c);
-    k_radon<<<dim3(4, njobs), 1024, rsize * sizeof(double), c.st>>>(arena, planes, jobs, feat, nullptr, rsize);
+    if (c.prec == WC_PREC_MIXED) k_radon<float><<<dim3(4, njobs), 1024, rsize * sizeof(float), c.st>>>(arena, planes, jobs, feat, rsize);
+    else k_radon<double><<<dim3(4, njobs), 1024, rsize * sizeof(double), c.st>>>(arena, planes, jobs, feat, rsize);
 }
 
 // ---------------------------------------------------------------- Chebyshev coefficients

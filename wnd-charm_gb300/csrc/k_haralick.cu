@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict
 // FUSED (mixed form): fused multiply-adds in the two updates.
 template <bool FUSED>
 __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
-    __shared__ double v[256], ess[256], tess[256];
+    __shared__ double v[256], ess[256], tess[256], red[32];
     __shared__ double s_tau, s_beta, s_den;
     __shared__ int s_triv;
     const int ang = blockIdx.y;
@@ -308,9 +308,17 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
         const int rem = n - i - 1;
         for (int k = threadIdx.x; k < rem; k += blockDim.x) v[k] = A[(long long)(i + 1 + k) * n + i];
         __syncthreads();
+        double tail_mixed = 0;
+        if (FUSED) {  // the mixed form sums the tail as a tree (no 255-deep dependent chain)
+            double q = 0;
+            for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) q = __fma_rn(v[k], v[k], q);
+            tail_mixed = block_sum(q, red);
+        }
         if (threadIdx.x == 0) {  // makeHouseholder (Householder.h:65-90)
             double tail = 0;
-            for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, __dmul_rn(v[k], v[k]));
+            if (FUSED) tail = tail_mixed;
+            else
+                for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, __dmul_rn(v[k], v[k]));
             const double c0 = v[0];
             if (rem == 1 || tail == 0) {
                 s_triv = 1;

@@ -157,6 +157,12 @@ def main():
                         ref_w=w, ref_min=mn, ref_max=mx, ref_p=p, ref_pred=pr,
                         syn_w=sw, syn_min=smn, syn_max=smx,
                         syn_p=sp, syn_pred=spr)
+    # the reference's signature and training-set files as text, for the .sig/.fit writers and readers
+    texts = {}
+    for key, fn in (("sig_010067", "010067_301x300-l_precalculated.sig"), ("sig_t1", "t1_s01_c05_ij-l_precalculated.sig"),
+                    ("fit_unbalanced", "unbalanced.fit")):
+        texts[key] = np.array(open(os.path.join(T, fn)).read())
+    np.savez_compressed(os.path.join(HERE, "reference_text.npz"), **texts)
     print("done")
 
 

@@ -38,3 +38,20 @@ def test_wnd_full_scale():
     np.testing.assert_array_equal(mx, omx)
     np.testing.assert_array_equal(pred[:100], opred)
     np.testing.assert_allclose(p[:100], op, rtol=0, atol=1e-6)
+
+
+def test_wnd_full_scale_mixed_matches_fp64():
+    """The mixed form (FP32-pair distances) at full scale: predicted classes
+    identical to the FP64 form, marginal probabilities within 1e-6."""
+    import wndcharm
+    from wndcharm import synth
+    xtr, ytr, xte, yte = synth.feature_vectors(100000, 10000, 2919, 10, 4)
+    e64, emx = wndcharm.Engine(0, "fp64"), wndcharm.Engine(0, "mixed")
+    w, mn, mx = e64.wnd_fit(xtr, ytr, 10, 0.15)
+    p64, pr64 = e64.wnd_classify(xtr, ytr, 10, w, mn, mx, xte)
+    t0 = time.perf_counter()
+    pmx, prmx = emx.wnd_classify(xtr, ytr, 10, w, mn, mx, xte)
+    print("mixed classify %.2f s" % (time.perf_counter() - t0))
+    np.testing.assert_array_equal(prmx, pr64)
+    np.testing.assert_allclose(pmx, p64, rtol=0, atol=1e-6)
+    print("max |p_mixed - p_fp64| = %.3g" % np.abs(pmx - p64).max())

@@ -447,6 +447,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
 }  // namespace wc
 
 namespace wc {
+int engine_precision(const wc_engine *E) { return E->prec; }
 int engine_device(wc_engine *E, cudaStream_t *st, long long **launches) {
     CK(cudaSetDevice(E->dev));
     *st = E->st;

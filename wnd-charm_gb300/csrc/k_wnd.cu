@@ -20,6 +20,7 @@
 struct wc_engine;
 namespace wc {
 int engine_device(wc_engine *E, cudaStream_t *st, long long **launches);
+int engine_precision(const wc_engine *E);
 }
 
 namespace wc {
@@ -184,6 +185,112 @@ __global__ void __launch_bounds__(256) k_wnd_dist(const double *__restrict__ Tc,
     }
 }
 
+// Mixed form of the distance: features as FP32 pairs (hi + lo, 48 significant
+// bits), every term w^2 (t - x)^2 formed and summed with error-free
+// transformations (two-sum, FMA two-product), so d carries ~1e-14 relative
+// error at FP32-pipe speed; d^-5 in FP64.  (The FP64 form above follows the
+// reference's rounding and its |t - x| < DBL_EPSILON skip, which drops terms
+// below 5e-32 w^2; the mixed form keeps them.)
+__global__ void k_wnd_split(const double *__restrict__ src, long long n, float2 *__restrict__ dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = src[i];
+        const float h = (float)v;
+        dst[i] = make_float2(h, (float)(v - (double)h));
+    }
+}
+
+// error-free transformations: explicit roundings (no contraction may fuse them)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__global__ void __launch_bounds__(256) k_wnd_dist_df(const float2 *__restrict__ Tc, int T, const float2 *__restrict__ Xc,
+                                                     int N, const int *__restrict__ y, const float2 *__restrict__ w2,
+                                                     int K, int C, int per, double *__restrict__ psim,
+                                                     long long *__restrict__ pcnt) {
+    __shared__ float2 Ts[WK][WT + 1], Xs[WK][WT + 1];
+    __shared__ double D[WT][WT + 1];
+    __shared__ float2 ws[WK];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int t0 = blockIdx.x * WT, chunk = blockIdx.y;
+    const int sbeg = chunk * per, send = min(N, sbeg + per);
+    double acc[16];
+    long long cnt[16];
+    for (int c = 0; c < 16; c++) { acc[c] = 0; cnt[c] = 0; }
+    for (int s0 = sbeg; s0 < send; s0 += WT) {
+        float dh[4][4], dl[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) dh[a][b] = dl[a][b] = 0.f;
+        for (int k0 = 0; k0 < K; k0 += WK) {
+            for (int q = threadIdx.x; q < WK * WT; q += blockDim.x) {
+                const int kk = q / WT, ii = q - kk * WT, k = k0 + kk;
+                Ts[kk][ii] = (k < K && t0 + ii < T) ? Tc[(long long)k * T + t0 + ii] : make_float2(0.f, 0.f);
+                Xs[kk][ii] = (k < K && s0 + ii < send) ? Xc[(long long)k * N + s0 + ii] : make_float2(0.f, 0.f);
+            }
+            if (threadIdx.x < WK) ws[threadIdx.x] = (k0 + threadIdx.x < K) ? w2[k0 + threadIdx.x] : make_float2(0.f, 0.f);
+            __syncthreads();
+            const int kend = min(WK, K - k0);
+            for (int kk = 0; kk < kend; kk++) {
+                const float2 wk = ws[kk];
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    const float2 tv = Ts[kk][ty + 16 * a];
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        const float2 xv = Xs[kk][tx + 16 * b];
+                        float s, e;
+                        two_sum(tv.x, -xv.x, s, e);  // t - x
+                        e = __fadd_rn(e, __fsub_rn(tv.y, xv.y));
+                        const float sh = __fadd_rn(s, e);
+                        const float sl = __fsub_rn(e, __fsub_rn(sh, s));
+                        const float p = __fmul_rn(sh, sh);  // (t - x)^2
+                        float pe = __fmaf_rn(sh, sh, -p);
+                        pe = __fmaf_rn(2.f * sh, sl, pe);
+                        const float q = __fmul_rn(p, wk.x);  // w^2 (t - x)^2
+                        float qe = __fmaf_rn(p, wk.x, -q);
+                        qe = __fmaf_rn(p, wk.y, __fmaf_rn(pe, wk.x, qe));
+                        float u, ue;  // accumulate
+                        two_sum(dh[a][b], q, u, ue);
+                        ue = __fadd_rn(ue, __fadd_rn(dl[a][b], qe));
+                        dh[a][b] = __fadd_rn(u, ue);
+                        dl[a][b] = __fsub_rn(ue, __fsub_rn(dh[a][b], u));
+                    }
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) D[ty + 16 * a][tx + 16 * b] = (double)dh[a][b] + (double)dl[a][b];
+        __syncthreads();
+        if (threadIdx.x < WT && t0 + threadIdx.x < T) {
+            const int lim = min(WT, send - s0);
+            for (int j = 0; j < lim; j++) {
+                const double ds = D[threadIdx.x][j];
+                if (ds < DBL_EPSILON) continue;
+                const int c = y[s0 + j];
+                if (c < 1 || c > C) continue;
+                const double d2 = ds * ds;
+                acc[c - 1] += 1.0 / (d2 * d2 * ds);
+                cnt[c - 1] += 1;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < WT && t0 + threadIdx.x < T) {
+        const long long base = ((long long)(t0 + threadIdx.x) * gridDim.y + chunk) * C;
+        for (int c = 0; c < C; c++) {
+            psim[base + c] = acc[c];
+            pcnt[base + c] = cnt[c];
+        }
+    }
+}
+
 // per test row: sum the chunks in order, class means, argmax, probabilities
 __global__ void k_wnd_finish(const double *__restrict__ psim, const long long *__restrict__ pcnt, int T, int nchunk, int C,
                              double *__restrict__ probs, int *__restrict__ pred) {
@@ -318,8 +425,26 @@ extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, 
         ++*launches;
         k_wnd_gather<<<(int)(((long long)T * K + 255) / 256), 256, 0, st>>>(dT, T, F, dkeep, K, dmin, dmax, dTc);
     }
-    ++*launches;
-    k_wnd_dist<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, T, dXc, N, dy, dw2, K, C, per, dps, dpc);
+    if (engine_precision(E) == WC_PREC_MIXED && K) {
+        float2 *fX = nullptr, *fT = nullptr, *fw = nullptr;
+        CKW(cudaMalloc(&fX, (size_t)N * K * 8));
+        CKW(cudaMalloc(&fT, (size_t)T * K * 8));
+        CKW(cudaMalloc(&fw, (size_t)K * 8));
+        *launches += 4;
+        k_wnd_split<<<1024, 256, 0, st>>>(dXc, (long long)N * K, fX);
+        k_wnd_split<<<1024, 256, 0, st>>>(dTc, (long long)T * K, fT);
+        k_wnd_split<<<1, 256, 0, st>>>(dw2, K, fw);
+        k_wnd_dist_df<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(fT, T, fX, N, dy, fw, K, C, per, dps, dpc);
+        const cudaError_t le = cudaGetLastError();
+        cudaStreamSynchronize(st);
+        cudaFree(fX);
+        cudaFree(fT);
+        cudaFree(fw);
+        CKW(le);
+    } else {
+        ++*launches;
+        k_wnd_dist<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, T, dXc, N, dy, dw2, K, C, per, dps, dpc);
+    }
     ++*launches;
     k_wnd_finish<<<(T + 127) / 128, 128, 0, st>>>(dps, dpc, T, nchunk, C, dprob, dpred);
     CKW(cudaGetLastError());

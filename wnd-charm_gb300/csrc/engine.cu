@@ -158,7 +158,7 @@ struct wc_engine {
     std::mutex mu;
     Prof prof;
     cudaStream_t lanes[WC_LANES] = {};
-    cudaEvent_t fork_ev = nullptr, join_ev[WC_LANES] = {};
+    cudaEvent_t fork_ev = nullptr, early_ev = nullptr, join_ev[WC_LANES] = {};
 };
 
 namespace wc {
@@ -387,6 +387,39 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     const Plane *dplanes = (const Plane *)(dm + m_planes);
     PlaneStats *dstats = (PlaneStats *)(dm + m_stats);
 
+    FeatureRun fr;
+    fr.ctx = &ctx;
+    fr.arena = arena;
+    fr.planes = dplanes;
+    fr.stats = dstats;
+    fr.meta = dm;
+    fr.ws = dw;
+    fr.tabs = E->tabs.d();
+    fr.feat = dfeat;
+    Ctx lc[WC_LANES];
+    for (int k = 0; k < WC_LANES; k++) {
+        lc[k] = ctx;
+        lc[k].st = E->lanes[k];
+    }
+    fr.lanes = lc;
+    // Families that read only the root planes (Gabor, object and edge features in
+    // the standard plans) need nothing from the transforms: once the root planes'
+    // statistics exist they start on lanes 3 and 4, beside the transforms.
+    bool early = true;
+    for (int a : {A_EDGEF, A_OBJ, A_INVOBJ, A_GABOR})
+        for (auto &j : fj[a])
+            if (j.plane % NN) early = false;
+    int r_early = WC_OK;
+    if (early) {
+        {
+            ProfScope ps(ctx, "plane stats");
+            launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats, NN, 1);
+        }
+        CK(cudaEventRecord(E->early_ev, ctx.st));
+        for (int k : {3, 4}) CK(cudaStreamWaitEvent(E->lanes[k], E->early_ev, 0));
+        r_early = features_launch(fs, fr, 0, true);
+    }
+
     // ---- transforms, depth by depth
     for (int d = 1; d <= maxdepth; d++)
         for (int x = 0; x < X_COUNT; x++) {
@@ -411,33 +444,19 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
         }
     {
         ProfScope ps(ctx, "plane stats");
-        launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats);
+        launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats, NN, early ? 2 : 0);
     }
-
-    FeatureRun fr;
-    fr.ctx = &ctx;
-    fr.arena = arena;
-    fr.planes = dplanes;
-    fr.stats = dstats;
-    fr.meta = dm;
-    fr.ws = dw;
-    fr.tabs = E->tabs.d();
-    fr.feat = dfeat;
-    // the feature families are independent given the planes: fork them onto the
-    // engine's lane streams and join back before the caller's next operation
-    Ctx lc[WC_LANES];
+    // the other families are independent given the planes: fork them onto the
+    // remaining lanes, and join every lane back before the caller's next operation
     CK(cudaEventRecord(E->fork_ev, ctx.st));
-    for (int k = 0; k < WC_LANES; k++) {
-        lc[k] = ctx;
-        lc[k].st = E->lanes[k];
-        CK(cudaStreamWaitEvent(E->lanes[k], E->fork_ev, 0));
-    }
-    fr.lanes = lc;
-    r = features_launch(fs, fr);
+    for (int k = 0; k < WC_LANES; k++)
+        if (!early || (k != 3 && k != 4)) CK(cudaStreamWaitEvent(E->lanes[k], E->fork_ev, 0));
+    r = features_launch(fs, fr, 1, early);
     for (int k = 0; k < WC_LANES; k++) {
         CK(cudaEventRecord(E->join_ev[k], E->lanes[k]));
         CK(cudaStreamWaitEvent(ctx.st, E->join_ev[k], 0));
     }
+    if (r_early) return r_early;
     if (r) return r;
     CK(cudaGetLastError());
     if (planes_out) *planes_out = planes;
@@ -534,6 +553,7 @@ int wc_engine_create(int device, int precision, wc_engine **out) {
         CK(cudaEventCreateWithFlags(&E->join_ev[k], cudaEventDisableTiming));
     }
     CK(cudaEventCreateWithFlags(&E->fork_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&E->early_ev, cudaEventDisableTiming));
     *out = E;
     return WC_OK;
 }
@@ -547,6 +567,7 @@ void wc_engine_destroy(wc_engine *E) {
         if (E->join_ev[k]) cudaEventDestroy(E->join_ev[k]);
     }
     if (E->fork_ev) cudaEventDestroy(E->fork_ev);
+    if (E->early_ev) cudaEventDestroy(E->early_ev);
     delete E;
 }
 

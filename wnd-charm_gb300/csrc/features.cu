@@ -391,7 +391,7 @@ int features_prepare(FeatureSetup &fs) {
     return WC_OK;
 }
 
-int features_launch(FeatureSetup &fs, FeatureRun &fr) {
+int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early) {
     const auto &P = *fs.planes;
     const auto &fj = *fs.fj;
     // lanes: 0 Haralick; 1 Zernike, Chebyshev-Fourier; 2 Tamura, Chebyshev coefficients;
@@ -399,6 +399,39 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
     Ctx &c = fr.lanes[5];
     auto jobs = [&](int a) { return (const FJob *)(fr.meta + fs.off["jobs" + std::to_string(a)]); };
     auto nj = [&](int a) { return (int)fj[a].size(); };
+    // the families that read only the root planes (lanes 3, 4)
+    if (early ? phase == 0 : phase == 1) {
+        {
+            Ctx &c = fr.lanes[4];
+            ProfScope ps(c, "Edge Features");
+            if (nj(A_EDGEF))
+            launch_edgefeat(c, fr.arena, fr.planes, jobs(A_EDGEF), nj(A_EDGEF), maxw_of(P, fj[A_EDGEF]),
+                            maxh_of(P, fj[A_EDGEF]), (const EFJob *)(fr.meta + fs.off["ef_jobs"]), (double *)fr.ws,
+                            (const Plane *)(fr.meta + fs.off["ef_aux"]), (const int *)(fr.meta + fs.off["ef_ids"]),
+                            (PlaneStats *)(fr.meta + fs.off["ef_stats"]), (unsigned long long *)(fr.ws + fs.off["ef_keys"]),
+                            (unsigned long long *)(fr.ws + fs.off["ef_tmp"]), (const long long *)(fr.meta + fs.off["ef_koff"]),
+                            (const SortSeg *)(fr.meta + fs.off["ef_seg"]), fs.val["ef_maxn"], fr.ws + fs.off["ef_cnt"], fr.feat);
+        }
+        if (fs.val.count("ob_n")) {
+            Ctx &c = fr.lanes[4];
+            ProfScope ps(c, "Object Features (Otsu + Inverse)");
+            if (cudaMemsetAsync(fr.ws + fs.val["ob_zero_begin"], 0, (size_t)fs.val["ob_zero_bytes"], c.st) != cudaSuccess)
+                return set_err(WC_ERR_CUDA, "memset failed");
+            launch_objects(c, fr.arena, fr.planes, fr.stats, (const FJob *)(fr.meta + fs.off["ob_fjobs"]), (int)fs.val["ob_n"],
+                           fs.val["ob_maxpix"], (const OBJob *)(fr.meta + fs.off["ob_jobs"]), (double *)fr.ws,
+                           (const Plane *)(fr.meta + fs.off["ob_inv"]), (PlaneStats *)(fr.meta + fs.off["ob_invstats"]),
+                           (double *)(fr.ws + fs.off["ob_thr"]), (unsigned long long *)(fr.ws + fs.off["ob_acc"]), fr.feat);
+        }
+        {
+            Ctx &c = fr.lanes[3];
+            ProfScope ps(c, "Gabor Textures");
+            if (nj(A_GABOR))
+            launch_gabor(c, fr.arena, fr.planes, jobs(A_GABOR), nj(A_GABOR), (const GabJob *)(fr.meta + fs.off["gab_jobs"]),
+                         fs.gab_jobs, fs.gab_sizes, (const FFTPlan *)(fr.meta + fs.off["gab_plans"]), fr.tabs,
+                         fs.val["gab_kern"], (double *)fr.ws, (double *)(fr.ws + fs.off["gab_counts"]), fr.feat);
+        }
+    }
+    if (phase == 0) return WC_OK;
     // the longest dependent chain (Haralick f14) is issued first
     {
         Ctx &c = fr.lanes[0];
@@ -473,35 +506,6 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr) {
         launch_tamura(c, fr.planes, fr.stats, fr.arena, jobs(A_TAMURA), nj(A_TAMURA),
                       (const TamJob *)(fr.meta + fs.off["tam_jobs"]), (double *)fr.ws,
                       (double *)(fr.ws + fs.off["tam_part"]), fs.val["tam_maxpix"], fr.feat);
-    }
-    {
-        Ctx &c = fr.lanes[4];
-        ProfScope ps(c, "Edge Features");
-        if (nj(A_EDGEF))
-        launch_edgefeat(c, fr.arena, fr.planes, jobs(A_EDGEF), nj(A_EDGEF), maxw_of(P, fj[A_EDGEF]),
-                        maxh_of(P, fj[A_EDGEF]), (const EFJob *)(fr.meta + fs.off["ef_jobs"]), (double *)fr.ws,
-                        (const Plane *)(fr.meta + fs.off["ef_aux"]), (const int *)(fr.meta + fs.off["ef_ids"]),
-                        (PlaneStats *)(fr.meta + fs.off["ef_stats"]), (unsigned long long *)(fr.ws + fs.off["ef_keys"]),
-                        (unsigned long long *)(fr.ws + fs.off["ef_tmp"]), (const long long *)(fr.meta + fs.off["ef_koff"]),
-                        (const SortSeg *)(fr.meta + fs.off["ef_seg"]), fs.val["ef_maxn"], fr.ws + fs.off["ef_cnt"], fr.feat);
-    }
-    if (fs.val.count("ob_n")) {
-        Ctx &c = fr.lanes[4];
-        ProfScope ps(c, "Object Features (Otsu + Inverse)");
-        if (cudaMemsetAsync(fr.ws + fs.val["ob_zero_begin"], 0, (size_t)fs.val["ob_zero_bytes"], c.st) != cudaSuccess)
-            return set_err(WC_ERR_CUDA, "memset failed");
-        launch_objects(c, fr.arena, fr.planes, fr.stats, (const FJob *)(fr.meta + fs.off["ob_fjobs"]), (int)fs.val["ob_n"],
-                       fs.val["ob_maxpix"], (const OBJob *)(fr.meta + fs.off["ob_jobs"]), (double *)fr.ws,
-                       (const Plane *)(fr.meta + fs.off["ob_inv"]), (PlaneStats *)(fr.meta + fs.off["ob_invstats"]),
-                       (double *)(fr.ws + fs.off["ob_thr"]), (unsigned long long *)(fr.ws + fs.off["ob_acc"]), fr.feat);
-    }
-    {
-        Ctx &c = fr.lanes[3];
-        ProfScope ps(c, "Gabor Textures");
-        if (nj(A_GABOR))
-        launch_gabor(c, fr.arena, fr.planes, jobs(A_GABOR), nj(A_GABOR), (const GabJob *)(fr.meta + fs.off["gab_jobs"]),
-                     fs.gab_jobs, fs.gab_sizes, (const FFTPlan *)(fr.meta + fs.off["gab_plans"]), fr.tabs,
-                     fs.val["gab_kern"], (double *)fr.ws, (double *)(fr.ws + fs.off["gab_counts"]), fr.feat);
     }
     return WC_OK;
 }

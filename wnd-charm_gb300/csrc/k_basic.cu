@@ -35,9 +35,11 @@ void launch_convert(Ctx &c, const void *src, int dtype, double *dst, long long n
 // Moments2 of every plane (src/statistics/Moments.h:61-107): min, max, mean,
 // var = M2/(n-1) for n > 2.  Two deterministic passes per plane, one CTA each.
 __global__ void __launch_bounds__(1024) k_plane_stats(const double *__restrict__ arena, const Plane *__restrict__ planes,
-                                                      PlaneStats *__restrict__ out) {
+                                                      PlaneStats *__restrict__ out, int nn, int sel) {
     __shared__ double sh[32];
-    const Plane P = planes[blockIdx.x];
+    // sel 0: every plane; 1: the root plane of each image (index b*nn); 2: the others
+    const int pi = sel == 0 ? blockIdx.x : sel == 1 ? blockIdx.x * nn : (blockIdx.x / (nn - 1)) * nn + 1 + blockIdx.x % (nn - 1);
+    const Plane P = planes[pi];
     const double *p = arena + P.off;
     const long long n = (long long)P.w * P.h;
     double mn = DBL_MAX, mx = -DBL_MAX, s = 0;
@@ -72,14 +74,15 @@ __global__ void __launch_bounds__(1024) k_plane_stats(const double *__restrict__
         r.var = cnt > 2 ? m2 / (cnt - 1) : 0.0;
         r.sum = s;
         r.n = cnt;
-        out[blockIdx.x] = r;
+        out[pi] = r;
     }
 }
 
-void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int nplanes, PlaneStats *out) {
-    if (nplanes <= 0) return;
+void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int nplanes, PlaneStats *out, int nn, int sel) {
+    const int nb = sel == 0 ? nplanes : sel == 1 ? nplanes / nn : nplanes / nn * (nn - 1);
+    if (nb <= 0) return;
     WC_LAUNCH(c);
-    k_plane_stats<<<nplanes, 1024, 0, c.st>>>(arena, planes, out);
+    k_plane_stats<<<nb, 1024, 0, c.st>>>(arena, planes, out, nn, sel);
 }
 
 // ---------------------------------------------------------------- Edge transform

@@ -110,7 +110,7 @@ void launch_edgefeat(Ctx &c, const double *arena, const Plane *planes, const FJo
     if (njobs <= 0) return;
     WC_LAUNCH(c);
     k_ef_prewitt<<<dim3((maxw + 31) / 32, (maxh + 7) / 8, njobs), dim3(32, 8), 0, c.st>>>(arena, planes, jobs, ej, ws);
-    launch_plane_stats(c, ws, aux_planes, 2 * njobs, aux_stats);
+    launch_plane_stats(c, ws, aux_planes, 2 * njobs, aux_stats, 1, 0);
     launch_sort_planes(c, ws, aux_planes, aux_ids, seg, 2 * njobs, maxn, keys, tmp, scratch);
     WC_LAUNCH(c);
     k_ef_final<<<njobs, 512, 0, c.st>>>(planes, jobs, ej, ws, aux_stats, keys, koff, feat);
@@ -388,7 +388,7 @@ void launch_objects(Ctx &c, const double *arena, const Plane *planes, const Plan
     if (blocks > 256) blocks = 256;
     WC_LAUNCH(c);
     k_ob_invert<<<dim3(blocks, njobs), 256, 0, c.st>>>(arena, planes, stats, jobs, oj, ws);
-    launch_plane_stats(c, ws, inv_planes, njobs, inv_stats);
+    launch_plane_stats(c, ws, inv_planes, njobs, inv_stats, 1, 0);
     WC_LAUNCH(c);
     k_ob_otsu<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, inv_stats, jobs, oj, ws, thr);
     for (int stage = 0; stage < 3; stage++) {

@@ -8,7 +8,8 @@ namespace wc {
 
 // k_basic.cu
 void launch_convert(Ctx &c, const void *src, int dtype, double *dst, long long n);
-void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int nplanes, PlaneStats *out);
+// sel 0: all planes; 1: each image's root plane (index b*nn); 2: all but the roots
+void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int nplanes, PlaneStats *out, int nn, int sel);
 void launch_edge(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh);
 void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
                     double *tmp, const long long *tmp_off);

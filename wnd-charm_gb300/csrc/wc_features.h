@@ -42,7 +42,9 @@ struct FeatureRun {
 
 void features_init();
 int features_prepare(FeatureSetup &fs);
-int features_launch(FeatureSetup &fs, FeatureRun &fr);
+// phase 0: the families that read only root planes (Gabor, object and edge
+// features) on lanes 3 and 4; phase 1: the rest (or everything, with early == false)
+int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early);
 // reads and clears the device error word; *dev_err != 0 if a kernel flagged one
 int features_check(cudaStream_t st, int *dev_err);
 int set_err(int code, const char *fmt, ...);

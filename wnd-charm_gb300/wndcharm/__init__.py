@@ -264,3 +264,18 @@ def wnd_fit(train, labels, n_classes, frac=0.15, precision="fp64"):
 
 def wnd_classify(train, labels, n_classes, weights, mins, maxs, test, precision="fp64"):
     return default_engine(precision).wnd_classify(train, labels, n_classes, weights, mins, maxs, test)
+
+
+def tiles(pixels, tiles_x, tiles_y):
+    """The tiles wndchrm samples from an image (TrainingSet::AddImageFile,
+    src/wndchrm_src/TrainingSet.cpp:1465-1476, enumerated x-major as in
+    src/wndchrm_src/wndchrm.cpp:95-122): tile (ix, iy) covers columns
+    [ix*tw, (ix+1)*tw) and rows [iy*th, (iy+1)*th), tw = W // tiles_x,
+    th = H // tiles_y (the remainder at the right and bottom is dropped).
+    Returns the list of 2-D views, ix outer, iy inner."""
+    a = np.asarray(pixels)
+    h, w = a.shape
+    tw, th = w // tiles_x, h // tiles_y
+    if tw < 1 or th < 1:
+        raise WndcharmError("image %dx%d is smaller than %dx%d tiles" % (w, h, tiles_x, tiles_y))
+    return [a[iy * th:(iy + 1) * th, ix * tw:(ix + 1) * tw] for ix in range(tiles_x) for iy in range(tiles_y)]

@@ -288,6 +288,7 @@ def main():
     step_dev()
     stream.synchronize()
     prof = eng.profile_report()
+    timeline = eng.profile_timeline()
     eng.profile(False)
     tot_prof = sum(ms for _, ms, _ in prof) or 1.0
     dom = max(prof, key=lambda r: r[1]) if prof else ("none", 0.0, 1)
@@ -329,7 +330,8 @@ def main():
             "clocks": clocks,
             "roofline": roof,
             "forms": forms,
-            "stages_ms": {n: round(ms, 3) for n, ms, _ in prof}}
+            "stages_ms": {n: round(ms, 3) for n, ms, _ in prof},
+            "timeline_ms": {n: [round(a, 1), round(b, 1)] for n, a, b in timeline}}
     if rank == 0 and not args.no_cpu_baseline:
         nth = os.cpu_count() or 1
         ncpu = min(nth, B)

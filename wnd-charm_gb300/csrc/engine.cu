@@ -585,6 +585,8 @@ int wc_engine_profile(wc_engine *E, int on) {
     E->prof.order.clear();
     E->prof.ms.clear();
     E->prof.calls.clear();
+    E->prof.t0.clear();
+    E->prof.t1.clear();
     return WC_OK;
 }
 
@@ -593,7 +595,8 @@ int wc_engine_profile_report(wc_engine *E, char *buf, int buflen) {
     std::string s;
     char line[256];
     for (size_t k = 0; k < E->prof.order.size(); k++) {
-        snprintf(line, sizeof line, "%s\t%.6f\t%lld\n", E->prof.order[k].c_str(), E->prof.ms[k], E->prof.calls[k]);
+        snprintf(line, sizeof line, "%s\t%.6f\t%lld\t%.6f\t%.6f\n", E->prof.order[k].c_str(), E->prof.ms[k],
+                 E->prof.calls[k], E->prof.t0[k], E->prof.t1[k]);
         s += line;
     }
     strncpy(buf, s.c_str(), (size_t)buflen - 1);

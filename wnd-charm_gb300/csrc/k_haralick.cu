@@ -733,13 +733,18 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
 
 // Matrices with at least QR_BIG tones (the long chains) get 4 warps each, one
 // per SM sub-partition, which quarters the reflector updates on the critical
-// path; the rest run one per warp, 4 to a block.  perm lists the matrices by
-// descending Ng and nbig counts the large ones.
+// path, as long as there are no more of them than max_groups; the rest (and
+// all of them beyond that) run one per warp, 4 to a block.  perm lists the
+// matrices by descending Ng and nbig counts the large ones.
 template <bool FUSED>
 __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb,
-                                                const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat) {
+                                                const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat,
+                                                int max_groups) {
     __shared__ double rowsum[4][256];
-    const int nbig = *nbig_p;
+    // groups only while every large matrix can have an SM to itself; beyond that
+    // the FP64 pipes are shared anyway and one warp per matrix issues fewer
+    // instructions (no reflector formed four times)
+    const int nbig = *nbig_p <= max_groups ? *nbig_p : 0;
     int m, wq = 0;
     if ((int)blockIdx.x < nbig) {
         m = perm[blockIdx.x];
@@ -788,22 +793,36 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
         cudaFuncSetAttribute(k_har_glcm, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         attr = true;
     }
+    {
+    ProfScope p1(c, "Haralick: quantise, GLCM, f1-f13");
     WC_LAUNCH(c);
     k_har_quant<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, jobs, hj, wsb);
     WC_LAUNCH(c);
     k_har_glcm<<<dim3(njobs, 4), 1024, sm, c.st>>>(planes, jobs, hj, wsb);
     WC_LAUNCH(c);
     k_har_stats<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
+    }
+    {
+    ProfScope p2(c, "Haralick: Q");
     WC_LAUNCH(c);
     k_har_q<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
+    }
+    {
+    ProfScope p3(c, "Haralick: Hessenberg");
     WC_LAUNCH(c);
     if (c.prec == WC_PREC_MIXED) k_har_hess<true><<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
     else k_har_hess<false><<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    }
+    {
+    ProfScope p4(c, "Haralick: real Schur (f14)");
     WC_LAUNCH(c);
     k_har_order<<<1, 256, 0, c.st>>>(hj, wsb, 4 * njobs, perm);
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED) k_har_qr<true><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs);
-    else k_har_qr<false><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs);
+    if (c.prec == WC_PREC_MIXED) k_har_qr<true><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, c.sms);
+    // the FP64 form keeps the 4-warp groups at every batch size (measured faster there:
+    // its other families load the FP64 pipes more)
+    else k_har_qr<false><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, 1 << 30);
+    }
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);
 }

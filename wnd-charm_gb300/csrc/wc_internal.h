@@ -58,30 +58,45 @@ struct Prof {
     std::vector<Mark> pending;
     std::vector<std::string> order;
     std::vector<double> ms;
+    std::vector<double> t0, t1;  // earliest start, latest end (ms after the batch's first mark)
     std::vector<long long> calls;
-    void begin(const std::string &name, cudaStream_t st) {
-        if (!on) return;
+    long long begin(const std::string &name, cudaStream_t st) {
+        if (!on) return -1;
         Mark m{name, nullptr, nullptr};
         cudaEventCreate(&m.a);
         cudaEventCreate(&m.b);
         cudaEventRecord(m.a, st);
         pending.push_back(m);
+        return (long long)pending.size() - 1;
     }
-    void end(cudaStream_t st) {
-        if (!on || pending.empty() || !pending.back().b) return;
-        cudaEventRecord(pending.back().b, st);
+    void end(long long idx, cudaStream_t st) {
+        if (!on || idx < 0 || idx >= (long long)pending.size()) return;
+        cudaEventRecord(pending[idx].b, st);
     }
     void collect() {  // after the stream has been synchronised
+        cudaEvent_t ref = pending.empty() ? nullptr : pending[0].a;
         for (auto &m : pending) {
-            float t = 0;
+            float t = 0, s0 = 0, s1 = 0;
             cudaEventElapsedTime(&t, m.a, m.b);
-            cudaEventDestroy(m.a);
-            cudaEventDestroy(m.b);
+            cudaEventElapsedTime(&s0, ref, m.a);
+            cudaEventElapsedTime(&s1, ref, m.b);
             size_t k = 0;
             while (k < order.size() && order[k] != m.name) k++;
-            if (k == order.size()) { order.push_back(m.name); ms.push_back(0); calls.push_back(0); }
+            if (k == order.size()) {
+                order.push_back(m.name);
+                ms.push_back(0);
+                calls.push_back(0);
+                t0.push_back(s0);
+                t1.push_back(s1);
+            }
             ms[k] += t;
             calls[k] += 1;
+            t0[k] = t0[k] < s0 ? t0[k] : s0;
+            t1[k] = t1[k] > s1 ? t1[k] : s1;
+        }
+        for (auto &m : pending) {
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
         }
         pending.clear();
     }
@@ -95,10 +110,11 @@ struct Ctx {
     int sms;              // multiprocessors on the device
     Prof *prof;
 };
-struct ProfScope {
+struct ProfScope {  // may nest (e.g. a family's phases inside the family)
     Ctx &c;
-    ProfScope(Ctx &c_, const char *name) : c(c_) { if (c.prof) c.prof->begin(name, c.st); }
-    ~ProfScope() { if (c.prof) c.prof->end(c.st); }
+    long long idx = -1;
+    ProfScope(Ctx &c_, const char *name) : c(c_) { if (c.prof) idx = c.prof->begin(name, c.st); }
+    ~ProfScope() { if (c.prof) c.prof->end(idx, c.st); }
 };
 
 }  // namespace wc

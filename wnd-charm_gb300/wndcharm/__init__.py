@@ -155,8 +155,19 @@ class Engine(object):
         check(lib().wc_engine_profile_report(self._h, buf, 1 << 16))
         out = []
         for line in buf.value.decode().splitlines():
-            name, ms, calls = line.split("\t")
-            out.append((name, float(ms), int(calls)))
+            f = line.split("\t")
+            out.append((f[0], float(f[1]), int(f[2])))
+        return out
+
+    def profile_timeline(self):
+        """Per stage: (name, start_ms, end_ms) after the profiled batch's first
+        stage started (stages on different lanes overlap)."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        check(lib().wc_engine_profile_report(self._h, buf, 1 << 16))
+        out = []
+        for line in buf.value.decode().splitlines():
+            f = line.split("\t")
+            out.append((f[0], float(f[3]), float(f[4])))
         return out
 
     def set_stream(self, stream_ptr):

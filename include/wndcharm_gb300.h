@@ -30,6 +30,7 @@ extern "C" {
 #define WC_ERR_NOMEM (-3)       /* device allocation failed */
 #define WC_ERR_UNSUPPORTED (-4) /* request outside what this build supports */
 #define WC_ERR_DEVICE (-5)      /* a kernel reported a bounded-wait timeout or an internal check */
+#define WC_ERR_IO (-6)          /* a file could not be read or is malformed */
 
 /* plan kinds: the reference's standard feature sets */
 #define WC_PLAN_SHORT 0 /* 1059 features, StdFeatureComputationPlans::getFeatureSet */
@@ -125,6 +126,16 @@ int wc_wnd_fit(wc_engine *engine, const double *train, int N, int F, const int *
 int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const int *labels, int C,
                     const double *weights, const double *mins, const double *maxs, const double *test, int T,
                     double *probs, int *pred);
+
+/* ---- image files ----
+ * Grayscale TIFF as ImageMatrix::LoadTIFF reads it (src/cmatrix.cpp:85-203): one
+ * image directory, one sample per pixel, 8 or 16 bits, strips uncompressed, LZW
+ * (optionally with the horizontal predictor) or PackBits, either byte order.
+ * wc_tiff_info gives the size and bit depth; wc_tiff_read writes the samples
+ * row-major (uint8, or uint16 in native byte order) into `pixels` (capacity in
+ * bytes).  Colour and multi-directory files give WC_ERR_UNSUPPORTED. */
+int wc_tiff_info(const char *path, int *width, int *height, int *bits);
+int wc_tiff_read(const char *path, void *pixels, long long capacity);
 
 /* ---- allocation-free entry point ----
  * wc_wavelet_noalloc: the Wavelet transform (one-level Symlet-5, as wc_transform

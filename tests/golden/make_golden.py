@@ -163,6 +163,12 @@ def main():
                     ("fit_unbalanced", "unbalanced.fit")):
         texts[key] = np.array(open(os.path.join(T, fn)).read())
     np.savez_compressed(os.path.join(HERE, "reference_text.npz"), **texts)
+    # the reference's test TIFFs as bytes (uncompressed and LZW, big-endian), for the TIFF reader
+    tifs = {}
+    for key, fn in (("t1_s01_c05_ij", "t1_s01_c05_ij.tif"), ("010067_301x300", "010067_301x300.tif"),
+                    ("binuc1", "images/binuc/binuc1.tiff"), ("norm1", "images/norm/norm1.tiff")):
+        tifs[key] = np.frombuffer(open(os.path.join(T, fn), "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "reference_tiff.npz"), **tifs)
     print("done")
 
 

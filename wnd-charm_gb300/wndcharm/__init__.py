@@ -113,6 +113,25 @@ class ImageMatrix(object):
             self.bits = bits
         return self
 
+    def OpenImage(self, path, downsample=0, bounding_rect=None, mean=0, stddev=0):
+        """Read a grayscale 8/16-bit TIFF as ImageMatrix::OpenImage does
+        (src/cmatrix.cpp:252-294): optional crop to bounding_rect = (x, y, w, h).
+        Returns 1 on success, 0 when the file name has no ".tif"/".TIF" (as
+        the reference); downsampling and mean/stddev normalisation are not
+        supported here (WndcharmError)."""
+        if ".tif" not in path and ".TIF" not in path:
+            return 0
+        if (downsample and 0 < downsample < 100) or mean > 0:
+            raise WndcharmError("OpenImage: downsample / normalisation are not supported")
+        pix, bits = read_tiff(path)
+        if bounding_rect is not None and bounding_rect[0] >= 0:
+            x, y, w, h = bounding_rect
+            if x + w > pix.shape[1] or y + h > pix.shape[0]:
+                raise WndcharmError("OpenImage: bounding_rect outside the image")
+            pix = pix[y:y + h, x:x + w]
+        self.set(np.ascontiguousarray(pix), bits)
+        return 1
+
     @property
     def width(self):
         return self.pix_plane.shape[1]
@@ -290,3 +309,15 @@ def tiles(pixels, tiles_x, tiles_y):
     if tw < 1 or th < 1:
         raise WndcharmError("image %dx%d is smaller than %dx%d tiles" % (w, h, tiles_x, tiles_y))
     return [a[iy * th:(iy + 1) * th, ix * tw:(ix + 1) * tw] for ix in range(tiles_x) for iy in range(tiles_y)]
+
+
+def read_tiff(path):
+    """(pixels, bits) of a grayscale 8/16-bit TIFF (uint8 or uint16 array, height x
+    width), read as ImageMatrix::LoadTIFF reads it."""
+    L = lib()
+    w, h, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    p = path.encode()
+    check(L.wc_tiff_info(p, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b)))
+    out = np.empty((h.value, w.value), dtype=np.uint8 if b.value == 8 else np.uint16)
+    check(L.wc_tiff_read(p, out.ctypes.data_as(ctypes.c_void_p), out.nbytes))
+    return out, b.value

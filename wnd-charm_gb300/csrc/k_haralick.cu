@@ -724,7 +724,9 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                     i += 2;
                 }
             }
-            if (im2 == 0) f = sqrt(re2);
+            // Q's eigenvalues are >= 0; a negative one is rounding.  The FP64 form
+            // keeps the reference's sqrt (NaN there); the mixed form reads it as 0.
+            if (im2 == 0) f = sqrt(FUSED ? fmax(re2, 0.0) : re2);
         }
         res[13] = f;  // no convergence: 0, as the oracle
     }

@@ -15,6 +15,8 @@
  *   TrainingSet::normalize, SetFisherScores, classify2               src/wndchrm_src/TrainingSet.h:205-243,
  *                                                                    src/wndchrm_src/TrainingSet.cpp:2090-2123, 2183-2324, 2429-2586
  *   signatures::normalize                                            src/wndchrm_src/signatures.cpp:196-215
+ *   ImageMatrix::OpenImage, submatrix, Downsample, normalize, Rotate src/cmatrix.cpp:252-294, 414-470, 579-769, 836-888
+ *   TrainingSet::AddImageFile's sample loop (rotations x tiles)      src/wndchrm_src/TrainingSet.cpp:1442-1481
  */
 #ifndef WNDCHARM_GB300_H
 #define WNDCHARM_GB300_H
@@ -136,6 +138,52 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
  * bytes).  Colour and multi-directory files give WC_ERR_UNSUPPORTED. */
 int wc_tiff_info(const char *path, int *width, int *height, int *bits);
 int wc_tiff_read(const char *path, void *pixels, long long capacity);
+
+/* ---- preprocessing and sampling ----
+ * How wndchrm turns one opened image into its samples, on the GPU:
+ * ImageMatrix::OpenImage (src/cmatrix.cpp:252-294) crops to a bounding
+ * rectangle (submatrix, :414-470), area-downsamples (Downsample, :579-720) and
+ * normalises (normalize, :836-888); TrainingSet::AddImageFile
+ * (src/wndchrm_src/TrainingSet.cpp:1442-1481) then rotates (Rotate, :727-769)
+ * and cuts a tile (submatrix) for each sample.  Samples are numbered as
+ * wndchrm enumerates them (src/wndchrm_src/wndchrm.cpp:93-124): rotation
+ * outermost, then tile x, then tile y; sample k has rotation k / (tx*ty),
+ * tile x (k % (tx*ty)) / ty, tile y k % ty.  As in the reference, a
+ * "rotation" of 270 degrees is the transpose (Rotate's case 270), and for
+ * rotations 1 and 3 the tile width is the rotated image's height / tiles_y and
+ * the tile height its width / tiles_x (TrainingSet.cpp:1465-1471).  A tile
+ * that does not fit the rotated image (the reference then keeps the previous
+ * sample's pixels) is WC_ERR_ARG.  Arithmetic is FP64 in the reference's
+ * order (crop, rotation, tiles and Downsample are bit-identical to it); the
+ * mean / standard deviation that normalisation divides by are two-pass sums
+ * (the reference: Welford updates), so normalised pixels agree to ~1e-15. */
+typedef struct {
+    int crop_x, crop_y, crop_w, crop_h; /* bounding rectangle; crop_x < 0: the whole image */
+    double downsample_x, downsample_y;  /* Downsample ratios in (0, 1); >= 1: no downsampling */
+    double norm_min, norm_max;          /* normalize to [0, norm_range] when norm_min >= 0, norm_max > 0 */
+    long long norm_range;               /* ... and norm_range > 0 */
+    double norm_mean, norm_std;         /* normalize to norm_mean (and norm_std when > 0) when norm_mean > 0 */
+    int rotations;                      /* 1 (as is) or 4 (also 90, 180, 270 degrees) */
+    int tiles_x, tiles_y;               /* tiles per rotated image, >= 1 each */
+} wc_sampling;
+
+/* No crop, no downsampling, no normalisation, 1 rotation, 1 x 1 tile. */
+void wc_sampling_default(wc_sampling *s);
+/* Samples per image: rotations * tiles_x * tiles_y (or a negative status). */
+int wc_sampling_count(const wc_sampling *s);
+/* Size of sample `sample` of a width x height image. */
+int wc_sample_size(const wc_sampling *s, int width, int height, int sample, int *out_width, int *out_height);
+/* One sample plane of one image: out receives out_width * out_height doubles
+ * (row-major; out_capacity in doubles), host memory unless out_on_device. */
+int wc_preprocess(wc_engine *engine, const wc_image_desc *image, const wc_sampling *s, int sample, double *out,
+                  long long out_capacity, int *out_width, int *out_height, int out_on_device);
+/* wc_extract_batch over every sample of every image: out is
+ * (n * wc_sampling_count(s)) x n_features, image-major, samples in the order
+ * above.  The images go to the GPU once; crop, downsampling, normalisation,
+ * rotations and tiles run there, and the samples stay in device memory until
+ * their feature rows are written. */
+int wc_extract_samples(wc_engine *engine, const wc_plan *plan, const wc_image_desc *images, int n,
+                       const wc_sampling *s, double *out, int out_on_device);
 
 /* ---- allocation-free entry point ----
  * wc_wavelet_noalloc: the Wavelet transform (one-level Symlet-5, as wc_transform

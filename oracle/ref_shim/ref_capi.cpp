@@ -141,4 +141,82 @@ int wcref_wnd(const double *train, int N, int F, const int *labels, int C, doubl
     return 0;
 }
 
+// The reference's own preprocessing and sampling of one image: the steps of
+// ImageMatrix::OpenImage (src/cmatrix.cpp:252-294) after LoadTIFF, then the
+// Rotate and tile submatrix of TrainingSet::AddImageFile
+// (src/wndchrm_src/TrainingSet.cpp:1455-1481), on the unmodified ImageMatrix
+// methods.  opt[14]: crop x, y, w, h (x < 0: none); Downsample x, y ratios
+// (both >= 1: not called); normalize min, max, range, mean, std (called when
+// either branch applies); rotations; tiles x, y.  Writes the sample's pixels
+// (and, with feat_kind >= 0, its standard-plan features).  Returns -1 where
+// submatrix refuses a rectangle.
+int wcref_preprocess(const double *pix, int w, int h, int bits, const double *opt, int sample, double *out,
+                     long cap, int *ow, int *oh, int feat_kind, double *feat) {
+    const int cx = (int)opt[0], cy = (int)opt[1], cw = (int)opt[2], ch = (int)opt[3];
+    const double dsx = opt[4], dsy = opt[5], nmin = opt[6], nmax = opt[7], nmean = opt[9], nstd = opt[10];
+    const long nrange = (long)opt[8];
+    const int rotations = (int)opt[11], tiles_x = (int)opt[12], tiles_y = (int)opt[13];
+    const int tiles = tiles_x * tiles_y;
+    ImageMatrix image_matrix;
+    image_matrix.bits = (unsigned short)bits;
+    if (cx >= 0) {
+        ImageMatrix copy_matrix;
+        copy_matrix.bits = (unsigned short)bits;
+        copy_matrix.allocate(w, h);
+        writeablePixels cp = copy_matrix.WriteablePixels();
+        for (int y = 0; y < h; y++)
+            for (int x = 0; x < w; x++) cp(y, x) = copy_matrix.stats.add(pix[(size_t)y * w + x]);
+        if (!image_matrix.submatrix(copy_matrix, (unsigned int)cx, (unsigned int)cy, (unsigned int)cx + cw - 1,
+                                    (unsigned int)cy + ch - 1))
+            return -1;
+    } else {
+        image_matrix.allocate(w, h);
+        writeablePixels pp = image_matrix.WriteablePixels();
+        for (int y = 0; y < h; y++)
+            for (int x = 0; x < w; x++) pp(y, x) = image_matrix.stats.add(pix[(size_t)y * w + x]);
+    }
+    if (!(dsx >= 1 && dsy >= 1)) image_matrix.Downsample(image_matrix, dsx, dsy);
+    if (nmean > 0 || (nmin >= 0 && nmax > 0 && nrange > 0)) image_matrix.normalize(nmin, nmax, nrange, nmean, nstd);
+    image_matrix.finish();
+    const int rot_index = sample / tiles, rem = sample % tiles, tile_index_x = rem / tiles_y, tile_index_y = rem % tiles_y;
+    if (rot_index >= rotations) return -1;
+    ImageMatrix rot_matrix, tile_matrix;
+    ImageMatrix *rot_matrix_p = &image_matrix, *tile_matrix_p;
+    if (rot_index > 0) {
+        rot_matrix.Rotate(image_matrix, 90.0 * rot_index);
+        rot_matrix_p = &rot_matrix;
+    }
+    if (tiles != 1) {
+        long tile_x_size, tile_y_size;
+        if (rot_index == 1 || rot_index == 3) {
+            tile_y_size = (long)(rot_matrix_p->width / tiles_x);
+            tile_x_size = (long)(rot_matrix_p->height / tiles_y);
+        } else {
+            tile_x_size = (long)(rot_matrix_p->width / tiles_x);
+            tile_y_size = (long)(rot_matrix_p->height / tiles_y);
+        }
+        if (!tile_matrix.submatrix(*rot_matrix_p, tile_index_x * tile_x_size, tile_index_y * tile_y_size,
+                                   (tile_index_x + 1) * tile_x_size - 1, (tile_index_y + 1) * tile_y_size - 1))
+            return -1;
+        tile_matrix_p = &tile_matrix;
+    } else {
+        tile_matrix_p = rot_matrix_p;
+    }
+    tile_matrix_p->finish();
+    *ow = (int)tile_matrix_p->width;
+    *oh = (int)tile_matrix_p->height;
+    if ((long)(*ow) * (*oh) > cap) return -2;
+    readOnlyPixels rp = tile_matrix_p->ReadablePixels();
+    for (int y = 0; y < *oh; y++)
+        for (int x = 0; x < *ow; x++) out[(size_t)y * (*ow) + x] = rp(y, x);
+    if (feat_kind >= 0 && feat) {
+        const FeatureComputationPlan *plan = std_plan(feat_kind);
+        std::vector<double> row(plan->n_features, 0.0);
+        FeatureComputationPlanExecutor ex(plan);
+        ex.run(tile_matrix_p, row, 0);
+        std::memcpy(feat, row.data(), row.size() * sizeof(double));
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -1505,6 +1505,104 @@ static Img make_img(const double *pix, int w, int h) {
     return im;
 }
 
+// ---------------------------------------------------------------- preprocessing
+// ImageMatrix::submatrix (src/cmatrix.cpp:414-470): rows y1..y2, columns
+// x1..x2 of `in`; false (nothing copied) when x2 or y2 lies outside.
+static bool submatrix(const Img &in, unsigned x1, unsigned y1, unsigned x2, unsigned y2, Img &out) {
+    if (x2 >= (unsigned)in.w || y2 >= (unsigned)in.h || x2 < x1 || y2 < y1) return false;
+    Img o((int)(x2 - x1 + 1), (int)(y2 - y1 + 1));
+    for (int y = 0; y < o.h; y++)
+        for (int x = 0; x < o.w; x++) o.at(y, x) = in.at((int)y1 + y, (int)x1 + x);
+    out = o;
+    return true;
+}
+
+// ImageMatrix::normalize (src/cmatrix.cpp:836-888).  mean() and std() are the
+// Moments2 of the current pixels in raster order (UpdateStats, :803-811).
+static void normalize(Img &im, double n_min, double n_max, long n_range, double n_mean, double n_std, int bits) {
+    if (n_min >= 0 && n_max > 0 && n_range > 0) {
+        double norm_fact = n_range / (n_max - n_min);
+        for (double &v : im.p) {
+            double val = v;
+            if (val < n_min) val = 0;
+            else if (val > n_max) val = n_range;
+            else val = norm_fact * (val - n_min);
+            v = val;
+        }
+    }
+    if (n_mean > 0) {
+        Moments2 st = stats_of(im);
+        double d_mean = st.mean - n_mean, std_fact = (n_std > 0 ? n_std : 0) / st.std_();
+        double max_range = std::pow((double)2, bits) - 1;
+        for (double &v : im.p) {
+            double val = v - d_mean;
+            if (n_std > 0) val = n_mean + (val - n_mean) * std_fact;
+            if (val < 0) val = 0;
+            else if (val > max_range) val = max_range;
+            v = val;
+        }
+    }
+}
+
+// ImageMatrix::Rotate (src/cmatrix.cpp:727-769): 90 = transpose, then each row
+// reversed; 180 = both axes reversed; 270 = the transpose.
+static Img rotate(const Img &in, int quarter) {
+    if (quarter == 2) {
+        Img o(in.w, in.h);
+        for (int y = 0; y < in.h; y++)
+            for (int x = 0; x < in.w; x++) o.at(y, x) = in.at(in.h - 1 - y, in.w - 1 - x);
+        return o;
+    }
+    Img o(in.h, in.w);
+    for (int y = 0; y < o.h; y++)
+        for (int x = 0; x < o.w; x++) o.at(y, x) = quarter == 1 ? in.at(in.h - 1 - x, y) : in.at(x, y);
+    return o;
+}
+
+// ImageMatrix::OpenImage's preprocessing (src/cmatrix.cpp:252-294) and the
+// sample cut of TrainingSet::AddImageFile (src/wndchrm_src/TrainingSet.cpp:1455-1481).
+// opt: crop x, y, w, h; downsample x, y ratios; normalize min, max, range,
+// mean, std; rotations; tiles x, y.  Returns -1 where the reference's
+// submatrix refuses the rectangle.
+static int preprocess(const Img &src, int bits, const double *opt, int sample, Img &out) {
+    const int cx = (int)opt[0], cy = (int)opt[1], cw = (int)opt[2], ch = (int)opt[3];
+    const double dsx = opt[4], dsy = opt[5];
+    const int rotations = (int)opt[11], tiles_x = (int)opt[12], tiles_y = (int)opt[13];
+    if (rotations < 1 || rotations > 4 || tiles_x < 1 || tiles_y < 1 || !(dsx > 0) || !(dsy > 0)) return -1;
+    const int tiles = tiles_x * tiles_y;
+    if (sample < 0 || sample >= rotations * tiles) return -1;
+    Img im = src;
+    if (cx >= 0) {
+        if (cy < 0 || cw < 1 || ch < 1) return -1;
+        Img c;
+        if (!submatrix(src, (unsigned)cx, (unsigned)cy, (unsigned)cx + cw - 1, (unsigned)cy + ch - 1, c)) return -1;
+        im = c;
+    }
+    if (!(dsx >= 1 && dsy >= 1)) {
+        im = downsample(im, dsx, dsy);
+        if (im.w < 1 || im.h < 1) return -1;
+    }
+    normalize(im, opt[6], opt[7], (long)opt[8], opt[9], opt[10], bits);
+    const int rot = sample / tiles, rem = sample % tiles, ix = rem / tiles_y, iy = rem % tiles_y;
+    Img r = rot ? rotate(im, rot) : im;
+    if (tiles == 1) {
+        out = r;
+        return 0;
+    }
+    long tx, ty;
+    if (rot == 1 || rot == 3) {
+        ty = (long)(r.w / tiles_x);
+        tx = (long)(r.h / tiles_y);
+    } else {
+        tx = (long)(r.w / tiles_x);
+        ty = (long)(r.h / tiles_y);
+    }
+    if (!submatrix(r, (unsigned)(ix * tx), (unsigned)(iy * ty), (unsigned)((ix + 1) * tx - 1),
+                   (unsigned)((iy + 1) * ty - 1), out))
+        return -1;
+    return 0;
+}
+
 // parse "Alg (T2 (T1 ()))" into a Group
 static bool parse_group(const std::string &s, Group &g) {
     size_t p = s.find(" (");
@@ -1669,6 +1767,17 @@ int wco_transform(const char *name, const double *pix, int w, int h, double *out
     *ow = r.w;
     *oh = r.h;
     std::memcpy(out, r.p.data(), sizeof(double) * r.n());
+    return 0;
+}
+
+int wco_preprocess(const double *pix, int w, int h, int bits, const double *opt, int sample, double *out,
+                   long cap, int *ow, int *oh) {
+    Img o;
+    if (preprocess(make_img(pix, w, h), bits, opt, sample, o)) return -1;
+    if ((long)o.n() > cap) return -2;
+    *ow = o.w;
+    *oh = o.h;
+    std::memcpy(out, o.p.data(), sizeof(double) * o.n());
     return 0;
 }
 

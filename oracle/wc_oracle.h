@@ -32,6 +32,14 @@ int wco_extract_group(const char *group, const double *pix, int w, int h, int bi
 // One transform ("Fourier", "Chebyshev", "Wavelet", "Edge"); out holds >= 4*w*h.
 int wco_transform(const char *name, const double *pix, int w, int h, double *out, int *ow, int *oh);
 
+// Preprocessing and one sample (crop, Downsample, normalize, Rotate, tile) of
+// a width x height image.  opt[14]: crop x, y, w, h (x < 0: none); downsample
+// x, y ratios (>= 1: none); normalize min, max, range, mean, std; rotations;
+// tiles x, y.  Returns 0, -1 where the reference refuses a rectangle, -2 when
+// out (cap doubles) is too small.
+int wco_preprocess(const double *pix, int w, int h, int bits, const double *opt, int sample, double *out,
+                   long cap, int *ow, int *oh);
+
 // Haralick per-angle tone count Ng of an image (diagnostic for cost models).
 int wco_haralick_tones(const double *pix, int w, int h);
 

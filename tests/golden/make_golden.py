@@ -8,7 +8,7 @@ Sources:
     (oracle/_ref/libwndref.so), run on those images and on small seeded
     synthetic images, for feature vectors, transform outputs and WND-5.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only preproc]
 """
 import ctypes
 import os
@@ -24,7 +24,8 @@ sys.path.insert(0, os.path.join(REPO, "wnd-charm_gb300"))
 from tiffread import read_tiff  # noqa: E402
 from wndcharm import synth  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ARGS = [a for i, a in enumerate(sys.argv[1:]) if not a.startswith("--") and sys.argv[i] != "--only"]
+REF = ARGS[0] if ARGS else "/root/reference"
 T = os.path.join(REF, "tests", "wndchrm_tests")
 LIB = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libwndref.so"))
 D = ctypes.POINTER(ctypes.c_double)
@@ -66,6 +67,78 @@ def ref_wnd(xtr, ytr, xte, C, frac):
                   np.ascontiguousarray(xte).ctypes.data_as(D), Tn, w.ctypes.data_as(D), mn.ctypes.data_as(D),
                   mx.ctypes.data_as(D), p.ctypes.data_as(D), pr.ctypes.data_as(I))
     return w, mn, mx, p, pr
+
+
+def ref_preprocess(img, bits, opt, sample, feat_kind=-1):
+    """The reference's OpenImage preprocessing + AddImageFile sample cut (oracle/ref_shim/ref_capi.cpp)."""
+    pix = np.ascontiguousarray(img, dtype=np.float64)
+    out = np.zeros(pix.size + 64)
+    ow, oh = ctypes.c_int(), ctypes.c_int()
+    feat = np.zeros(LIB.wcref_plan_n_features(max(feat_kind, 0)))
+    o = np.ascontiguousarray(opt, dtype=np.float64)
+    r = LIB.wcref_preprocess(pix.ctypes.data_as(D), img.shape[1], img.shape[0], bits, o.ctypes.data_as(D), sample,
+                             out.ctypes.data_as(D), ctypes.c_long(out.size), ctypes.byref(ow), ctypes.byref(oh),
+                             feat_kind, feat.ctypes.data_as(D))
+    if r:
+        return None, None
+    plane = out[: ow.value * oh.value].reshape(oh.value, ow.value).copy()
+    return plane, (feat if feat_kind >= 0 else None)
+
+
+# opt: crop x, y, w, h; downsample x, y; normalize min, max, range, mean, std; rotations; tiles x, y
+NONE_OPT = [-1, -1, -1, -1, 1, 1, -1, -1, -1, -1, -1, 1, 1, 1]
+
+
+def _opt(**kw):
+    o = list(NONE_OPT)
+    keys = ["cx", "cy", "cw", "ch", "dsx", "dsy", "nmin", "nmax", "nrange", "nmean", "nstd", "rot", "tx", "ty"]
+    for k, v in kw.items():
+        o[keys.index(k)] = v
+    return np.array(o, dtype=np.float64)
+
+
+def preproc_fixtures():
+    """Preprocessing and sampling (crop, Downsample, normalize, Rotate, tiles) by
+    the reference, on a seeded 12-bit image, an 8-bit image and a crop of one of
+    the reference's test images; features for a few samples."""
+    rng = np.random.default_rng(31337)
+    a = synth.blob_image(rng, 0, 61, 83, mean=320, sd=80, scale=16, maxval=4095).astype(np.uint16)
+    b = synth.blob_image(rng, 1, 64, 48).astype(np.uint8)
+    c = read_tiff(os.path.join(T, "t1_s01_c05_ij.tif"))[0]
+    images = {"a": (a, 16), "b": (b, 8), "c": (c, 16)}
+    cases = [
+        ("crop", "a", _opt(cx=10, cy=7, cw=40, ch=70), []),
+        ("ds50", "a", _opt(dsx=0.5, dsy=0.5), []),
+        ("ds37", "a", _opt(dsx=0.37, dsy=0.37), []),
+        ("ds_xy", "a", _opt(dsx=0.8, dsy=0.45), []),
+        ("norm_ms", "a", _opt(nmean=1000, nstd=300), []),
+        ("norm_m", "a", _opt(nmean=500, nstd=0), []),
+        ("norm_mm", "a", _opt(nmin=200, nmax=3000, nrange=255), []),
+        ("norm_both", "a", _opt(nmin=200, nmax=3000, nrange=4000, nmean=1500, nstd=200), []),
+        ("rot4", "a", _opt(rot=4), []),
+        ("tiles", "a", _opt(rot=4, tx=2, ty=3), []),
+        ("u8", "b", _opt(dsx=0.6, dsy=0.6, nmean=100, nstd=30), []),
+        ("full", "c", _opt(cx=5, cy=9, cw=96, ch=96, dsx=0.75, dsy=0.75, nmean=2000, nstd=500, rot=4, tx=2, ty=2),
+         [0, 5]),
+        ("crop_bad", "a", _opt(cx=30, cy=0, cw=40, ch=10), []),
+    ]
+    out = {"img_a": a, "img_b": b, "img_c": c}
+    for name, im, opt, feats in cases:
+        img, bits = images[im]
+        out["opt_" + name] = opt
+        out["src_" + name] = np.array(im)
+        n = int(opt[11] * opt[12] * opt[13])
+        ok = []
+        for k in range(n):
+            plane, f = ref_preprocess(img, bits, opt, k, 1 if k in feats else -1)
+            ok.append(plane is not None)
+            if plane is not None:
+                out["%s_%d" % (name, k)] = plane
+            if f is not None:
+                out["%s_%d_long" % (name, k)] = f
+        out["ok_" + name] = np.array(ok)
+        print("preproc", name, sum(ok), "/", n, flush=True)
+    np.savez_compressed(os.path.join(HERE, "reference_preproc.npz"), **out)
 
 
 def read_sig(path):
@@ -173,4 +246,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "preproc":
+        preproc_fixtures()
+    else:
+        main()
+        preproc_fixtures()

@@ -21,6 +21,7 @@
 #include "wc_features.h"
 #include "kernels.h"
 #include "plan.h"
+#include "engine.h"
 
 namespace wc {
 
@@ -35,68 +36,6 @@ int set_err(int code, const char *fmt, ...) {
     return code;
 }
 
-#define CK(x)                                                                                         \
-    do {                                                                                              \
-        cudaError_t e_ = (x);                                                                         \
-        if (e_ != cudaSuccess) return set_err(WC_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_)); \
-    } while (0)
-
-// grow-only device buffer
-struct DevBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    int ensure(size_t bytes) {
-        if (bytes <= cap) return WC_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = bytes + bytes / 4 + 4096;
-        if (cudaMalloc(&p, want) != cudaSuccess) {
-            cudaGetLastError();
-            return set_err(WC_ERR_NOMEM, "cudaMalloc of %zu bytes failed", want);
-        }
-        cap = want;
-        return WC_OK;
-    }
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
-};
-
-// Host-computed tables kept on the device: Chebyshev bases, FFT twiddles.
-struct Tables {
-    std::vector<double> host;
-    std::map<std::string, long long> idx;
-    DevBuf dev;
-    bool dirty = true;
-    // the generator runs only for a key not seen before (tables persist across batches)
-    template <typename Gen>
-    long long add_lazy(const std::string &key, Gen gen) {
-        auto it = idx.find(key);
-        if (it != idx.end()) return it->second;
-        return add(key, gen());
-    }
-    long long add(const std::string &key, const std::vector<double> &v) {
-        auto it = idx.find(key);
-        if (it != idx.end()) return it->second;
-        long long off = (long long)host.size();
-        host.insert(host.end(), v.begin(), v.end());
-        while (host.size() % 32) host.push_back(0.0);
-        idx[key] = off;
-        dirty = true;
-        return off;
-    }
-    int sync(cudaStream_t st) {
-        if (!dirty) return WC_OK;
-        int r = dev.ensure(host.size() * sizeof(double));
-        if (r) return r;
-        CK(cudaMemcpyAsync(dev.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-        CK(cudaStreamSynchronize(st));
-        dirty = false;
-        return WC_OK;
-    }
-    const double *d() const { return (const double *)dev.p; }
-};
 
 // Chebyshev basis of Chebyshev2D for a line of `len` samples and N terms:
 // tab[x*N + j] = T_j(x_x) * (j ? 2 : 1) / len / 2, x_x = 2(x+1)/len - 1,
@@ -146,20 +85,6 @@ FFTPlan fft_plan(Tables &tabs, int n) {
 
 using namespace wc;
 
-struct wc_engine {
-    int dev = 0;
-    cudaStream_t st = 0;
-    int prec = WC_PREC_FP64;
-    int sms = 1;
-    long long launches = 0;
-    DevBuf arena, feat, ws, meta, stage;
-    Tables tabs;
-    std::vector<char> hmeta;
-    std::mutex mu;
-    Prof prof;
-    cudaStream_t lanes[WC_LANES] = {};
-    cudaEvent_t fork_ev = nullptr, early_ev = nullptr, join_ev[WC_LANES] = {};
-};
 
 namespace wc {
 
@@ -195,7 +120,7 @@ static int out_shape(int xf, int w, int h, int &ow, int &oh) {
 
 // Runs `plan` over `n` images; `dfeat` receives n x n_features on the device.
 int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, double *dfeat,
-              std::vector<Plane> *planes_out = nullptr) {
+              std::vector<Plane> *planes_out) {
     Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof};
     // ---- nodes: every prefix of every group's transform chain
     std::vector<Node> nodes(1);
@@ -476,6 +401,34 @@ int engine_device(wc_engine *E, cudaStream_t *st, long long **launches) {
 }  // namespace wc
 
 // ================================================================= C ABI
+namespace wc {
+int extract_locked(wc_engine *E, const Plan &plan, const wc_image_desc *images, int n, double *out, int out_on_device) {
+    CK(cudaSetDevice(E->dev));
+    double *dfeat = out;
+    size_t fbytes = (size_t)n * plan.n_features * sizeof(double);
+    if (!out_on_device) {
+        int r = E->feat.ensure(fbytes);
+        if (r) return r;
+        dfeat = (double *)E->feat.p;
+    }
+    CK(cudaMemsetAsync(dfeat, 0, fbytes, E->st));
+    int r = run_batch(E, plan, images, n, dfeat);
+    if (r) return r;
+    if (!out_on_device) {
+        CK(cudaMemcpyAsync(out, dfeat, fbytes, cudaMemcpyDeviceToHost, E->st));
+        CK(cudaStreamSynchronize(E->st));
+    }
+    if (E->prof.on) {
+        CK(cudaStreamSynchronize(E->st));
+        E->prof.collect();
+    }
+    int dev_err = 0;
+    if ((r = features_check(E->st, &dev_err))) return r;
+    if (dev_err) return set_err(WC_ERR_DEVICE, "a kernel reported error code %d", dev_err);
+    return WC_OK;
+}
+}  // namespace wc
+
 extern "C" {
 
 const char *wc_last_error(void) { return g_err.c_str(); }
@@ -608,29 +561,7 @@ int wc_extract_batch(wc_engine *E, const wc_plan *plan, const wc_image_desc *ima
                      int out_on_device) {
     if (!E || !plan || !images || n < 1 || !out) return set_err(WC_ERR_ARG, "wc_extract_batch: bad arguments");
     std::lock_guard<std::mutex> lk(E->mu);
-    CK(cudaSetDevice(E->dev));
-    double *dfeat = out;
-    size_t fbytes = (size_t)n * plan->n_features * sizeof(double);
-    if (!out_on_device) {
-        int r = E->feat.ensure(fbytes);
-        if (r) return r;
-        dfeat = (double *)E->feat.p;
-    }
-    CK(cudaMemsetAsync(dfeat, 0, fbytes, E->st));
-    int r = run_batch(E, *plan, images, n, dfeat);
-    if (r) return r;
-    if (!out_on_device) {
-        CK(cudaMemcpyAsync(out, dfeat, fbytes, cudaMemcpyDeviceToHost, E->st));
-        CK(cudaStreamSynchronize(E->st));
-    }
-    if (E->prof.on) {
-        CK(cudaStreamSynchronize(E->st));
-        E->prof.collect();
-    }
-    int dev_err = 0;
-    if ((r = features_check(E->st, &dev_err))) return r;
-    if (dev_err) return set_err(WC_ERR_DEVICE, "a kernel reported error code %d", dev_err);
-    return WC_OK;
+    return extract_locked(E, *plan, images, n, out, out_on_device);
 }
 
 int wc_transform(wc_engine *E, const char *name, const double *pixels, int width, int height, double *out,

@@ -105,6 +105,37 @@ void launch_objects(Ctx &c, const double *arena, const Plane *planes, const Plan
                     long long maxpix, const OBJob *oj, double *ws, const Plane *inv_planes, PlaneStats *inv_stats,
                     double *thr, unsigned long long *acc, double *feat);
 
+// k_pre.cu: preprocessing (crop, Downsample, normalize) of each image into its
+// opened plane, then one rotated / tiled plane per sample.  Offsets are in
+// doubles into the preprocessing arena (tables: into the position table).
+struct PreJob {
+    const void *src;  // device address of the image
+    int dtype, sw;    // pixel type, row length
+    int cx, cy, cw, ch;
+    long long a_off;  // crop plane, cw x ch
+    int down, nw, nh;
+    double dx, dy;              // Downsample steps 1 / ratio
+    long long xs_tab, ys_tab;   // accumulated start positions
+    long long t_off;            // x pass, ch x nw
+    long long o_off;            // opened plane (a_off when not downsampled)
+    int ow, oh;
+    int mm, ms;                 // normalize: range branch, mean branch
+    double n_min, n_max, n_range, n_mean, n_std, max_range;
+};
+struct SampleJob {
+    int img, rot;
+    int x1, y1, tw, th;  // tile in the rotated opened plane
+    long long off;       // the sample plane, tw x th
+};
+struct PreGeomMax {  // launch extents: maxima over the batch
+    int cw, ch, nw, nh, ow, oh, tw, th;
+    int down, norm_range, norm_mean;
+};
+// tab: Downsample positions; yh, yl: RN(1/k) and RN(1/k - RN(1/k)) for k = 1, 2, ...
+// (index k - 1); fact: 2 doubles per image written by the device
+void launch_preprocess(Ctx &c, const PreJob *jobs, int n, const PreGeomMax &g, const double *tab, const double *yh,
+                       const double *yl, double *fact, double *pre, const SampleJob *sj, int ns);
+
 // k_gabor.cu
 struct GabJob {
     long long a_ws, c_ws, e_ws, g_ws;  // doubles offsets: image spectrum, 8 products, 8 energy maps, kernel spectra

@@ -7,7 +7,10 @@ Reference interface mirrored (paths in the wnd-charm source tree):
     getFeatureNameByIndex(i)                                        src/Tasks.h:272-316
   * FeatureComputationPlanExecutor(plan).run(image, feature_vec, row)
                                                                     src/Tasks.h:318-348
-  * ImageMatrix: a pixel plane with bits/width/height               src/cmatrix.h:164-339
+  * ImageMatrix: a pixel plane with bits/width/height, OpenImage, submatrix,
+    Downsample, normalize, Rotate                                   src/cmatrix.h:164-339, src/cmatrix.cpp:252-888
+  * the samples of one image (rotations x tiles, with OpenImage's
+    preprocessing) as TrainingSet::AddImageFile cuts them           src/wndchrm_src/TrainingSet.cpp:1442-1481
   * WND-5 (CLI semantics): normalize, Fisher scores, classify2      src/wndchrm_src/TrainingSet.cpp
 
 Every computation runs in the CUDA library (libwndcharm_gb300.so) through its
@@ -21,7 +24,54 @@ from . import _lib
 from ._lib import WndcharmError, check, lib
 
 __all__ = ["ImageMatrix", "FeatureComputationPlan", "StdFeatureComputationPlans", "FeatureComputationPlanExecutor",
-           "Engine", "extract_batch", "wnd_fit", "wnd_classify", "WndcharmError"]
+           "Engine", "Sampling", "extract_batch", "extract_samples", "wnd_fit", "wnd_classify", "WndcharmError"]
+
+
+class Sampling(object):
+    """Preprocessing and sampling options of wndchrm (its preproc_opts and
+    sampling_opts, src/wndchrm_src/wndchrm.cpp:750-770, 846-900):
+    bounding_rect (x, y, w, h) crops; downsample is a percentage (applied when
+    0 < downsample < 100, as ImageMatrix::OpenImage does); mean > 0 normalises
+    to that mean (and to stddev when > 0); rotations 1 or 4 (the -R switch);
+    tiles_x x tiles_y tiles per rotated image (-t).  ratio_x / ratio_y (explicit
+    Downsample ratios) and norm_min / norm_max / norm_range (normalize's range
+    branch) give the ImageMatrix methods' general forms."""
+
+    def __init__(self, bounding_rect=None, downsample=0, mean=0, stddev=0, rotations=1, tiles_x=1, tiles_y=1,
+                 ratio_x=None, ratio_y=None, norm_min=-1, norm_max=-1, norm_range=-1):
+        self.bounding_rect = bounding_rect
+        self.downsample = downsample
+        self.mean, self.stddev = mean, stddev
+        self.rotations, self.tiles_x, self.tiles_y = rotations, tiles_x, tiles_y
+        self.ratio_x, self.ratio_y = ratio_x, ratio_y
+        self.norm_min, self.norm_max, self.norm_range = norm_min, norm_max, norm_range
+
+    def struct(self):
+        s = _lib.wc_sampling()
+        lib().wc_sampling_default(ctypes.byref(s))
+        if self.bounding_rect is not None and self.bounding_rect[0] >= 0:
+            s.crop_x, s.crop_y, s.crop_w, s.crop_h = (int(v) for v in self.bounding_rect)
+        if self.ratio_x is not None or self.ratio_y is not None:
+            s.downsample_x = 1.0 if self.ratio_x is None else float(self.ratio_x)
+            s.downsample_y = 1.0 if self.ratio_y is None else float(self.ratio_y)
+        elif self.downsample and 0 < self.downsample < 100:
+            s.downsample_x = s.downsample_y = float(self.downsample) / 100.0
+        if self.mean > 0:
+            s.norm_mean, s.norm_std = float(self.mean), float(self.stddev)
+        s.norm_min, s.norm_max, s.norm_range = float(self.norm_min), float(self.norm_max), int(self.norm_range)
+        s.rotations, s.tiles_x, s.tiles_y = int(self.rotations), int(self.tiles_x), int(self.tiles_y)
+        return s
+
+    @property
+    def count(self):
+        """Samples per image."""
+        return check(lib().wc_sampling_count(ctypes.byref(self.struct())))
+
+    def sample_size(self, width, height, sample=0):
+        w, h = ctypes.c_int(), ctypes.c_int()
+        check(lib().wc_sample_size(ctypes.byref(self.struct()), int(width), int(height), int(sample),
+                                   ctypes.byref(w), ctypes.byref(h)))
+        return w.value, h.value
 
 
 class FeatureComputationPlan(object):
@@ -113,24 +163,60 @@ class ImageMatrix(object):
             self.bits = bits
         return self
 
-    def OpenImage(self, path, downsample=0, bounding_rect=None, mean=0, stddev=0):
+    def OpenImage(self, path, downsample=0, bounding_rect=None, mean=0, stddev=0, engine=None):
         """Read a grayscale 8/16-bit TIFF as ImageMatrix::OpenImage does
-        (src/cmatrix.cpp:252-294): optional crop to bounding_rect = (x, y, w, h).
+        (src/cmatrix.cpp:252-294): crop to bounding_rect = (x, y, w, h), area
+        downsampling to `downsample` percent (0 < downsample < 100), and
+        normalisation to `mean` (> 0) and `stddev`, on the GPU.  The pixel
+        plane is the file's integers when nothing is applied, else float64.
         Returns 1 on success, 0 when the file name has no ".tif"/".TIF" (as
-        the reference); downsampling and mean/stddev normalisation are not
-        supported here (WndcharmError)."""
+        the reference); a rectangle outside the image raises WndcharmError."""
         if ".tif" not in path and ".TIF" not in path:
             return 0
-        if (downsample and 0 < downsample < 100) or mean > 0:
-            raise WndcharmError("OpenImage: downsample / normalisation are not supported")
         pix, bits = read_tiff(path)
-        if bounding_rect is not None and bounding_rect[0] >= 0:
-            x, y, w, h = bounding_rect
-            if x + w > pix.shape[1] or y + h > pix.shape[0]:
-                raise WndcharmError("OpenImage: bounding_rect outside the image")
-            pix = pix[y:y + h, x:x + w]
+        opts = Sampling(bounding_rect=bounding_rect, downsample=downsample, mean=mean, stddev=stddev)
+        st = opts.struct()
+        if st.downsample_x < 1 or st.downsample_y < 1 or st.norm_mean > 0:
+            pix = (engine or default_engine()).preprocess(pix, opts, 0, bits)
+        elif st.crop_x >= 0:  # a crop alone copies pixels: the file's integers, no GPU needed
+            opts.sample_size(pix.shape[1], pix.shape[0])  # refuses a rectangle outside the image
+            pix = pix[st.crop_y:st.crop_y + st.crop_h, st.crop_x:st.crop_x + st.crop_w]
         self.set(np.ascontiguousarray(pix), bits)
         return 1
+
+    def _apply(self, matrix_IN, opts, sample=0, engine=None):
+        src = matrix_IN if matrix_IN is not None else self
+        pix = (engine or default_engine()).preprocess(src.pix_plane, opts, sample, src.bits)
+        self.set(pix, src.bits)
+
+    def submatrix(self, matrix_IN, x1, y1, x2, y2, engine=None):
+        """ImageMatrix::submatrix (src/cmatrix.cpp:414-470): rows y1..y2 and
+        columns x1..x2 of matrix_IN; returns 0 (self unchanged) when x2 or y2 is
+        outside it, else 1."""
+        if x2 >= matrix_IN.width or y2 >= matrix_IN.height or x2 < x1 or y2 < y1 or x1 < 0 or y1 < 0:
+            return 0
+        self._apply(matrix_IN, Sampling(bounding_rect=(x1, y1, x2 - x1 + 1, y2 - y1 + 1)), 0, engine)
+        return 1
+
+    def Downsample(self, matrix_IN, x_ratio, y_ratio, engine=None):
+        """ImageMatrix::Downsample (src/cmatrix.cpp:579-720): area averaging to
+        (unsigned)(ratio * size) along each axis; ratios above 1 count as 1."""
+        self._apply(matrix_IN, Sampling(ratio_x=x_ratio, ratio_y=y_ratio), 0, engine)
+
+    def normalize(self, n_min, n_max, n_range, n_mean, n_std, engine=None):
+        """ImageMatrix::normalize (src/cmatrix.cpp:836-888) in place: to [0,
+        n_range] between n_min and n_max (when all three are set), then to
+        n_mean / n_std (when n_mean > 0), clamped to [0, 2^bits - 1]."""
+        self._apply(None, Sampling(norm_min=n_min, norm_max=n_max, norm_range=n_range, mean=n_mean, stddev=n_std),
+                    0, engine)
+
+    def Rotate(self, matrix_IN, angle, engine=None):
+        """ImageMatrix::Rotate (src/cmatrix.cpp:727-769): 90 (transpose, rows
+        reversed), 180, or 270 (the transpose, as in the reference); other
+        angles leave self unchanged."""
+        if angle not in (90, 180, 270):
+            return
+        self._apply(matrix_IN, Sampling(rotations=4), int(angle) // 90, engine)
 
     @property
     def width(self):
@@ -202,6 +288,36 @@ class Engine(object):
         if out is None:
             out = np.zeros((n, plan.n_features))
         check(lib().wc_extract_batch(self._h, plan.handle, descs, n, out.ctypes.data, 0))
+        return out
+
+    def preprocess(self, pixels, sampling, sample=0, bits=16):
+        """One sample plane (float64) of a 2-D array: sampling's crop,
+        downsampling and normalisation, then sample `sample`'s rotation and
+        tile (rotation outermost, tile x, tile y innermost)."""
+        a = _as_input(pixels)
+        st = sampling.struct()
+        w, h = ctypes.c_int(), ctypes.c_int()
+        check(lib().wc_sample_size(ctypes.byref(st), a.shape[1], a.shape[0], int(sample), ctypes.byref(w),
+                                   ctypes.byref(h)))
+        out = np.zeros((h.value, w.value))
+        d = _lib.wc_image_desc(a.ctypes.data, _DT[a.dtype], a.shape[1], a.shape[0], int(bits), 0)
+        check(lib().wc_preprocess(self._h, ctypes.byref(d), ctypes.byref(st), int(sample), out.ctypes.data, out.size,
+                                  ctypes.byref(w), ctypes.byref(h), 0))
+        return out
+
+    def extract_samples(self, plan, images, sampling, bits=16, out=None):
+        """Features of every sample of every image ((n * sampling.count,
+        n_features), image-major), preprocessing and sampling on the GPU."""
+        imgs = [_as_input(a) for a in images]
+        n = len(imgs)
+        descs = (_lib.wc_image_desc * n)()
+        for i, a in enumerate(imgs):
+            descs[i] = _lib.wc_image_desc(a.ctypes.data, _DT[a.dtype], a.shape[1], a.shape[0], bits, 0)
+        st = sampling.struct()
+        per = check(lib().wc_sampling_count(ctypes.byref(st)))
+        if out is None:
+            out = np.zeros((n * per, plan.n_features))
+        check(lib().wc_extract_samples(self._h, plan.handle, descs, n, ctypes.byref(st), out.ctypes.data, 0))
         return out
 
     def extract_device(self, plan, descs, n, out_dev_ptr):
@@ -286,6 +402,10 @@ class FeatureComputationPlanExecutor(object):
 
 def extract_batch(plan, images, precision="fp64", bits=16):
     return default_engine(precision).extract(plan, images, bits=bits)
+
+
+def extract_samples(plan, images, sampling, precision="fp64", bits=16):
+    return default_engine(precision).extract_samples(plan, images, sampling, bits=bits)
 
 
 def wnd_fit(train, labels, n_classes, frac=0.15, precision="fp64"):

@@ -23,6 +23,14 @@ class wc_image_desc(ctypes.Structure):
                 ("height", ctypes.c_int), ("bits", ctypes.c_int), ("on_device", ctypes.c_int)]
 
 
+class wc_sampling(ctypes.Structure):
+    _fields_ = [("crop_x", ctypes.c_int), ("crop_y", ctypes.c_int), ("crop_w", ctypes.c_int), ("crop_h", ctypes.c_int),
+                ("downsample_x", ctypes.c_double), ("downsample_y", ctypes.c_double),
+                ("norm_min", ctypes.c_double), ("norm_max", ctypes.c_double), ("norm_range", ctypes.c_longlong),
+                ("norm_mean", ctypes.c_double), ("norm_std", ctypes.c_double),
+                ("rotations", ctypes.c_int), ("tiles_x", ctypes.c_int), ("tiles_y", ctypes.c_int)]
+
+
 class WndcharmError(RuntimeError):
     pass
 
@@ -58,6 +66,14 @@ def lib():
         L.wc_extract.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
         L.wc_extract_batch.argtypes = [vp, vp, ctypes.POINTER(wc_image_desc), ctypes.c_int, vp, ctypes.c_int]
         L.wc_transform.argtypes = [vp, ctypes.c_char_p, D, ctypes.c_int, ctypes.c_int, D, ctypes.c_longlong, I, I]
+        SP = ctypes.POINTER(wc_sampling)
+        L.wc_sampling_default.argtypes = [SP]
+        L.wc_sampling_default.restype = None
+        L.wc_sampling_count.argtypes = [SP]
+        L.wc_sample_size.argtypes = [SP, ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I]
+        L.wc_preprocess.argtypes = [vp, ctypes.POINTER(wc_image_desc), SP, ctypes.c_int, vp, ctypes.c_longlong, I, I,
+                                    ctypes.c_int]
+        L.wc_extract_samples.argtypes = [vp, vp, ctypes.POINTER(wc_image_desc), ctypes.c_int, SP, vp, ctypes.c_int]
         L.wc_wavelet_noalloc.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp]
         L.wc_tiff_info.argtypes = [ctypes.c_char_p, I, I, I]
         L.wc_tiff_read.argtypes = [ctypes.c_char_p, vp, ctypes.c_longlong]

@@ -129,6 +129,21 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
                     const double *weights, const double *mins, const double *maxs, const double *test, int T,
                     double *probs, int *pred);
 
+/* wc_wnd_classify_images: TrainingSet::ClassifyImage with WND-5
+ * (src/wndchrm_src/TrainingSet.cpp:1603-1800) for n_images images of `tiles`
+ * samples each: test holds n_images * tiles rows, an image's tiles consecutive.
+ * probs (n_images x C) are the tiles' marginal probabilities averaged in tile
+ * order (each added as p / tiles); pred is the class with the largest average
+ * (the first on ties; rank 1); norm_factors (may be NULL) the tiles' mean
+ * classify2 normalisation factor.  With max_tile set, the reference's
+ * "most similar tile" rule: a tile whose predicted-class probability divided
+ * by the other classes' sum is the largest so far replaces the sums with its
+ * own probabilities, and later tiles keep adding p / tiles.  Replaces the
+ * per-image loop of TrainingSet::Test (src/wndchrm_src/TrainingSet.cpp:1956-2000). */
+int wc_wnd_classify_images(wc_engine *engine, const double *train, int N, int F, const int *labels, int C,
+                           const double *weights, const double *mins, const double *maxs, const double *test,
+                           int n_images, int tiles, int max_tile, double *probs, int *pred, double *norm_factors);
+
 /* ---- image files ----
  * Grayscale TIFF as ImageMatrix::LoadTIFF reads it (src/cmatrix.cpp:85-203): one
  * image directory, one sample per pixel, 8 or 16 bits, strips uncompressed, LZW

@@ -141,6 +141,58 @@ int wcref_wnd(const double *train, int N, int F, const int *labels, int C, doubl
     return 0;
 }
 
+// TrainingSet::ClassifyImage (src/wndchrm_src/TrainingSet.cpp:1603-1800) with
+// WND, rank 1, no split, after the CLI's normalize + SetFisherScores, for
+// n_img images of `tiles` consecutive test rows each.  probs: n_img x C (the
+// `similarities` output, i.e. probabilities_sum); pred: n_img.
+extern int verbosity;
+int wcref_wnd_images(const double *train, int N, int F, const int *labels, int C, double frac, const double *test,
+                     int n_img, int tiles, int max_tile, double *probs, int *pred) {
+    const int old_verbosity = verbosity;
+    verbosity = 0;
+    TrainingSet *ts = new TrainingSet(N, C);
+    char lab[32];
+    for (int c = 1; c <= C; c++) {
+        snprintf(lab, sizeof lab, "c%04d", c);
+        ts->AddClass(lab);
+    }
+    const FeatureComputationPlan *plan = (F == 2919) ? std_plan(1) : nullptr;
+    char nm[256];
+    for (int s = 0; s < N; s++) {
+        signatures *sg = new signatures();
+        sg->NamesTrainingSet = ts;
+        sg->sample_class = (unsigned short)labels[s];
+        for (int f = 0; f < F; f++) {
+            if (plan) std::strncpy(nm, plan->getFeatureNameByIndex(f).c_str(), sizeof nm - 1), nm[sizeof nm - 1] = 0;
+            else snprintf(nm, sizeof nm, "Pixel Intensity Statistics () [%d]", f);
+            sg->Add(nm, train[(size_t)s * F + f]);
+        }
+        ts->AddSample(sg);
+    }
+    ts->normalize();
+    data_split split;
+    ts->SetFisherScores(frac, 0, &split);
+    const int T = n_img * tiles;
+    TrainingSet *test_set = new TrainingSet(T, C);
+    for (int t = 0; t < T; t++) {
+        signatures *sg = new signatures();
+        sg->sample_class = 0;
+        snprintf(sg->full_path, sizeof sg->full_path, "image%06d", t / tiles);
+        for (int f = 0; f < F; f++) sg->Add(nullptr, test[(size_t)t * F + f]);
+        test_set->AddSample(sg);
+    }
+    std::vector<double> sims(C + 1);
+    for (int g = 0; g < n_img; g++) {
+        const double c = ts->ClassifyImage(test_set, g * tiles, WND, tiles, 0, nullptr, max_tile, 1, nullptr, sims.data());
+        pred[g] = (int)c;
+        for (int k = 1; k <= C; k++) probs[(size_t)g * C + k - 1] = sims[k];
+    }
+    delete test_set;
+    delete ts;
+    verbosity = old_verbosity;
+    return 0;
+}
+
 // The reference's own preprocessing and sampling of one image: the steps of
 // ImageMatrix::OpenImage (src/cmatrix.cpp:252-294) after LoadTIFF, then the
 // Rotate and tile submatrix of TrainingSet::AddImageFile

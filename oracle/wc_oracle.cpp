@@ -1626,7 +1626,7 @@ static bool parse_group(const std::string &s, Group &g) {
 // ---------------------------------------------------------------- WND-5
 static void wnd_run(const double *train, int N, int F, const int *labels, int C, double frac,
                     const double *test, int T, double *weights, double *mins, double *maxs,
-                    double *probs, int *pred) {
+                    double *probs, int *pred, double *norms = nullptr) {
     // TrainingSet::normalize, src/wndchrm_src/TrainingSet.cpp:2090-2123
     std::vector<double> X(train, train + (size_t)N * F);
     for (int f = 0; f < F; f++) {
@@ -1704,6 +1704,59 @@ static void wnd_run(const double *train, int N, int F, const int *labels, int C,
         for (int c = 1; c <= C; c++) tot += csim[c];
         for (int c = 1; c <= C; c++) probs[(size_t)q * C + c - 1] = csim[c] / tot;
         pred[q] = (int)best;
+        if (norms) norms[q] = tot;
+    }
+}
+
+// TrainingSet::ClassifyImage, WND branch (src/wndchrm_src/TrainingSet.cpp:1603-1800),
+// rank 1, no ground truth: per image the `tiles` consecutive rows' marginal
+// probabilities accumulated as p / tiles in tile order; with max_tile a tile
+// whose share probabilities[pred] / (sum of the other entries 0..C) is the
+// largest so far overwrites the sums (entry 0, which classify2 never sets, is
+// taken as 0); the class of the largest sum; the mean normalisation factor.
+static void classify_images(const double *probs, const int *pred, const double *norms, int n_img, int tiles, int C,
+                            int max_tile, double *iprobs, int *ipred, double *inorm) {
+    std::vector<double> probabilities(C + 1), probabilities_sum(C + 1);
+    for (int g = 0; g < n_img; g++) {
+        int predicted_class = 0, most_similar_predicted_class = 0;
+        double max_tile_similarity = 0.0, sum_prob = 0.0, normalization_factor_avg = 0;
+        for (int c = 1; c <= C; c++) probabilities_sum[c] = 0.0;
+        for (int k = 0; k < tiles; k++) {
+            const size_t t = (size_t)g * tiles + k;
+            probabilities[0] = 0.0;
+            for (int c = 1; c <= C; c++) probabilities[c] = probs[t * C + c - 1];
+            predicted_class = pred[t];
+            if (predicted_class < 1) predicted_class = 0;
+            if (max_tile) {
+                sum_prob = 0.0;
+                for (int c = 0; c <= C; c++)
+                    if (c != predicted_class) sum_prob += probabilities[c];
+                if (probabilities[predicted_class] / sum_prob > max_tile_similarity) {
+                    max_tile_similarity = probabilities[predicted_class] / sum_prob;
+                    most_similar_predicted_class = predicted_class;
+                }
+            }
+            for (int c = 1; c <= C; c++) {
+                if (max_tile && max_tile_similarity == probabilities[predicted_class] / sum_prob)
+                    probabilities_sum[c] = probabilities[c];
+                else
+                    probabilities_sum[c] += (probabilities[c] / (double)tiles);
+            }
+            normalization_factor_avg += norms[t];
+        }
+        if (max_tile) predicted_class = most_similar_predicted_class;
+        normalization_factor_avg /= tiles;
+        if (C > 1) {
+            double max = 0.0;
+            for (int c = 1; c <= C; c++)
+                if (probabilities_sum[c] > max) {
+                    max = probabilities_sum[c];
+                    predicted_class = c;
+                }
+        }
+        for (int c = 1; c <= C; c++) iprobs[(size_t)g * C + c - 1] = probabilities_sum[c];
+        ipred[g] = predicted_class;
+        inorm[g] = normalization_factor_avg;
     }
 }
 
@@ -1778,6 +1831,16 @@ int wco_preprocess(const double *pix, int w, int h, int bits, const double *opt,
     *ow = o.w;
     *oh = o.h;
     std::memcpy(out, o.p.data(), sizeof(double) * o.n());
+    return 0;
+}
+
+int wco_wnd_images(const double *train, int N, int F, const int *labels, int C, double frac, const double *test,
+                   int n_img, int tiles, int max_tile, double *iprobs, int *ipred, double *inorm) {
+    const int T = n_img * tiles;
+    std::vector<double> w(F), mn(F), mx(F), p((size_t)T * C), nf(T);
+    std::vector<int> pr(T);
+    wnd_run(train, N, F, labels, C, frac, test, T, w.data(), mn.data(), mx.data(), p.data(), pr.data(), nf.data());
+    classify_images(p.data(), pr.data(), nf.data(), n_img, tiles, C, max_tile, iprobs, ipred, inorm);
     return 0;
 }
 

@@ -40,6 +40,12 @@ int wco_transform(const char *name, const double *pix, int w, int h, double *out
 int wco_preprocess(const double *pix, int w, int h, int bits, const double *opt, int sample, double *out,
                    long cap, int *ow, int *oh);
 
+// WND-5 over images of `tiles` consecutive test rows (TrainingSet::ClassifyImage):
+// per image the tile-averaged marginal probabilities (n_img x C), the class and
+// the mean normalisation factor.  max_tile: the reference's most-similar-tile rule.
+int wco_wnd_images(const double *train, int N, int F, const int *labels, int C, double frac, const double *test,
+                   int n_img, int tiles, int max_tile, double *iprobs, int *ipred, double *inorm);
+
 // Haralick per-angle tone count Ng of an image (diagnostic for cost models).
 int wco_haralick_tones(const double *pix, int w, int h);
 

@@ -8,7 +8,7 @@ Sources:
     (oracle/_ref/libwndref.so), run on those images and on small seeded
     synthetic images, for feature vectors, transform outputs and WND-5.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only preproc]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only preproc|wnd_images]
 """
 import ctypes
 import os
@@ -141,6 +141,25 @@ def preproc_fixtures():
     np.savez_compressed(os.path.join(HERE, "reference_preproc.npz"), **out)
 
 
+def wnd_image_fixtures():
+    """TrainingSet::ClassifyImage (WND-5, tiles averaged, and the most-similar-tile
+    rule) by the reference on seeded feature vectors: 12 test images of 4 tiles.
+    Inputs are regenerated by the tests: synth.feature_vectors(200, 48, 2919, 6, 7)."""
+    xtr, ytr, xte, yte = synth.feature_vectors(200, 48, 2919, 6, 7)
+    out = {}
+    for mt in (0, 1):
+        probs = np.zeros((12, 6))
+        pred = np.zeros(12, dtype=np.int32)
+        LIB.wcref_wnd_images(np.ascontiguousarray(xtr).ctypes.data_as(D), 200, 2919,
+                             np.ascontiguousarray(ytr, dtype=np.int32).ctypes.data_as(I), 6, ctypes.c_double(0.15),
+                             np.ascontiguousarray(xte).ctypes.data_as(D), 12, 4, mt, probs.ctypes.data_as(D),
+                             pred.ctypes.data_as(I))
+        out["probs_max_tile%d" % mt] = probs
+        out["pred_max_tile%d" % mt] = pred
+        print("wnd images, max_tile", mt, pred, flush=True)
+    np.savez_compressed(os.path.join(HERE, "reference_wnd_images.npz"), **out)
+
+
 def read_sig(path):
     lines = open(path).read().splitlines()[2:]
     return np.array([float(l.split("\t")[0]) for l in lines])
@@ -246,8 +265,12 @@ def main():
 
 
 if __name__ == "__main__":
-    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "preproc":
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "preproc":
         preproc_fixtures()
+    elif only == "wnd_images":
+        wnd_image_fixtures()
     else:
         main()
         preproc_fixtures()
+        wnd_image_fixtures()

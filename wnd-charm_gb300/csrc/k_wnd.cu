@@ -292,8 +292,9 @@ __global__ void __launch_bounds__(256) k_wnd_dist_df(const float2 *__restrict__ 
 }
 
 // per test row: sum the chunks in order, class means, argmax, probabilities
+// (norm: the sum of the class similarities, classify2's normalization_factor)
 __global__ void k_wnd_finish(const double *__restrict__ psim, const long long *__restrict__ pcnt, int T, int nchunk, int C,
-                             double *__restrict__ probs, int *__restrict__ pred) {
+                             double *__restrict__ probs, int *__restrict__ pred, double *__restrict__ norm) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
     double sim[16];
@@ -314,6 +315,59 @@ __global__ void k_wnd_finish(const double *__restrict__ psim, const long long *_
     for (int c = 0; c < C; c++) tot += sim[c];
     for (int c = 0; c < C; c++) probs[(long long)t * C + c] = sim[c] / tot;
     pred[t] = best;
+    norm[t] = tot;
+}
+
+// TrainingSet::ClassifyImage for WND-5 (src/wndchrm_src/TrainingSet.cpp:1603-1800),
+// one thread per image over its `tiles` consecutive rows, in tile order:
+// marginal probabilities summed as p / tiles (with max_tile, a tile whose
+// predicted-class share p[pred] / sum of the other classes' p is the largest so
+// far replaces the sums with its own p, the reference's rule), the mean
+// normalisation factor, and the class of the largest sum (first one on ties,
+// rank 1; a class below 1 from classify2 counts as 0).  The reference's share
+// also adds p[0], an element classify2 never sets; it counts as 0 here.
+__global__ void k_wnd_tiles(const double *__restrict__ probs, const int *__restrict__ pred,
+                            const double *__restrict__ norm, int n_img, int tiles, int C, int max_tile,
+                            double *__restrict__ iprobs, int *__restrict__ ipred, double *__restrict__ inorm) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_img) return;
+    double psum[17];
+    for (int c = 1; c <= C; c++) psum[c] = 0.0;
+    double best_share = 0.0, nf = 0.0;
+    int predicted = 0, best_pred = 0;
+    for (int k = 0; k < tiles; k++) {
+        const long long t = (long long)g * tiles + k;
+        const double *p = probs + t * C;  // class c at p[c - 1]
+        predicted = pred[t] < 1 ? 0 : pred[t];
+        const double pp = predicted ? p[predicted - 1] : 0.0;
+        double sum_prob = 0.0;
+        if (max_tile) {
+            for (int c = 0; c <= C; c++)
+                if (c != predicted) sum_prob += c ? p[c - 1] : 0.0;
+            if (pp / sum_prob > best_share) {
+                best_share = pp / sum_prob;
+                best_pred = predicted;
+            }
+        }
+        for (int c = 1; c <= C; c++) {
+            if (max_tile && best_share == pp / sum_prob) psum[c] = p[c - 1];
+            else psum[c] += p[c - 1] / (double)tiles;
+        }
+        nf += norm[t];
+    }
+    if (max_tile) predicted = best_pred;
+    nf /= tiles;
+    if (C > 1) {
+        double mx = 0.0;
+        for (int c = 1; c <= C; c++)
+            if (psum[c] > mx) {
+                mx = psum[c];
+                predicted = c;
+            }
+    }
+    for (int c = 1; c <= C; c++) iprobs[(long long)g * C + c - 1] = psum[c];
+    ipred[g] = predicted;
+    inorm[g] = nf;
 }
 
 }  // namespace wc
@@ -375,12 +429,11 @@ done:
     return rc;
 }
 
-extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
-                               const double *weights, const double *mins, const double *maxs, const double *test, int T,
-                               double *probs, int *pred) {
-    if (!E || !train || !labels || !weights || !mins || !maxs || !test || !probs || !pred || N < 1 || F < 1 || T < 1 ||
-        C < 1 || C > 16)
-        return set_err(WC_ERR_ARG, "wc_wnd_classify: bad arguments (C must be 1..16)");
+// classify2 for T test rows; with tiles > 0 the rows are n = T / tiles images'
+// tiles and ClassifyImage's per-image results are returned instead of the rows'.
+static int wnd_classify(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                        const double *weights, const double *mins, const double *maxs, const double *test, int T,
+                        double *probs, int *pred, int tiles, int max_tile, double *iprobs, int *ipred, double *inorm) {
     cudaStream_t st;
     long long *launches;
     int rc = engine_device(E, &st, &launches);
@@ -395,8 +448,10 @@ extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, 
     const int K = (int)keep.size();
     const int nchunk = std::max(1, std::min(64, (N + 4095) / 4096));
     const int per = ((N + nchunk - 1) / nchunk + WT - 1) / WT * WT;
+    const int n_img = tiles > 0 ? T / tiles : 0;
     double *dX = nullptr, *dT = nullptr, *dXc = nullptr, *dTc = nullptr, *dmin = nullptr, *dmax = nullptr, *dw2 = nullptr,
-           *dps = nullptr, *dprob = nullptr;
+           *dps = nullptr, *dprob = nullptr, *dnorm = nullptr, *diprob = nullptr, *dinorm = nullptr;
+    int *dipred = nullptr;
     long long *dpc = nullptr;
     int *dkeep = nullptr, *dy = nullptr, *dpred = nullptr;
     CKW(cudaMalloc(&dX, (size_t)N * F * 8));
@@ -412,6 +467,12 @@ extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, 
     CKW(cudaMalloc(&dpc, (size_t)T * nchunk * C * 8));
     CKW(cudaMalloc(&dprob, (size_t)T * C * 8));
     CKW(cudaMalloc(&dpred, (size_t)T * 4));
+    CKW(cudaMalloc(&dnorm, (size_t)T * 8));
+    if (n_img) {
+        CKW(cudaMalloc(&diprob, (size_t)n_img * C * 8));
+        CKW(cudaMalloc(&dipred, (size_t)n_img * 4));
+        CKW(cudaMalloc(&dinorm, (size_t)n_img * 8));
+    }
     CKW(cudaMemcpyAsync(dX, train, (size_t)N * F * 8, cudaMemcpyHostToDevice, st));
     CKW(cudaMemcpyAsync(dT, test, (size_t)T * F * 8, cudaMemcpyHostToDevice, st));
     CKW(cudaMemcpyAsync(dmin, mins, F * 8, cudaMemcpyHostToDevice, st));
@@ -446,10 +507,20 @@ extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, 
         k_wnd_dist<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, T, dXc, N, dy, dw2, K, C, per, dps, dpc);
     }
     ++*launches;
-    k_wnd_finish<<<(T + 127) / 128, 128, 0, st>>>(dps, dpc, T, nchunk, C, dprob, dpred);
+    k_wnd_finish<<<(T + 127) / 128, 128, 0, st>>>(dps, dpc, T, nchunk, C, dprob, dpred, dnorm);
     CKW(cudaGetLastError());
-    CKW(cudaMemcpyAsync(probs, dprob, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
-    CKW(cudaMemcpyAsync(pred, dpred, (size_t)T * 4, cudaMemcpyDeviceToHost, st));
+    if (n_img) {
+        ++*launches;
+        k_wnd_tiles<<<(n_img + 127) / 128, 128, 0, st>>>(dprob, dpred, dnorm, n_img, tiles, C, max_tile, diprob, dipred,
+                                                         dinorm);
+        CKW(cudaGetLastError());
+        CKW(cudaMemcpyAsync(iprobs, diprob, (size_t)n_img * C * 8, cudaMemcpyDeviceToHost, st));
+        CKW(cudaMemcpyAsync(ipred, dipred, (size_t)n_img * 4, cudaMemcpyDeviceToHost, st));
+        if (inorm) CKW(cudaMemcpyAsync(inorm, dinorm, (size_t)n_img * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+        CKW(cudaMemcpyAsync(probs, dprob, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
+        CKW(cudaMemcpyAsync(pred, dpred, (size_t)T * 4, cudaMemcpyDeviceToHost, st));
+    }
     CKW(cudaStreamSynchronize(st));
 done:
     cudaFree(dX);
@@ -465,5 +536,30 @@ done:
     cudaFree(dpc);
     cudaFree(dprob);
     cudaFree(dpred);
+    cudaFree(dnorm);
+    cudaFree(diprob);
+    cudaFree(dipred);
+    cudaFree(dinorm);
     return rc;
+}
+
+extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                               const double *weights, const double *mins, const double *maxs, const double *test, int T,
+                               double *probs, int *pred) {
+    if (!E || !train || !labels || !weights || !mins || !maxs || !test || !probs || !pred || N < 1 || F < 1 || T < 1 ||
+        C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_classify: bad arguments (C must be 1..16)");
+    return wnd_classify(E, train, N, F, labels, C, weights, mins, maxs, test, T, probs, pred, 0, 0, nullptr, nullptr,
+                        nullptr);
+}
+
+extern "C" int wc_wnd_classify_images(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                                      const double *weights, const double *mins, const double *maxs, const double *test,
+                                      int n_images, int tiles, int max_tile, double *probs, int *pred,
+                                      double *norm_factors) {
+    if (!E || !train || !labels || !weights || !mins || !maxs || !test || !probs || !pred || N < 1 || F < 1 ||
+        n_images < 1 || tiles < 1 || (long long)n_images * tiles > (1LL << 30) || C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_classify_images: bad arguments (C must be 1..16, tiles >= 1)");
+    return wnd_classify(E, train, N, F, labels, C, weights, mins, maxs, test, n_images * tiles, nullptr, nullptr, tiles,
+                        max_tile ? 1 : 0, probs, pred, norm_factors);
 }

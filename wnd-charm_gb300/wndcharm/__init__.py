@@ -359,6 +359,28 @@ class Engine(object):
                                     pred.ctypes.data_as(_lib.I)))
         return probs, pred
 
+    def wnd_classify_images(self, train, labels, n_classes, weights, mins, maxs, test, tiles, max_tile=False):
+        """TrainingSet::ClassifyImage with WND-5 for images of `tiles`
+        consecutive test rows: (probs (n_images, C), pred (n_images,),
+        normalisation factors (n_images,))."""
+        X = np.ascontiguousarray(train, dtype=np.float64)
+        y = np.ascontiguousarray(labels, dtype=np.int32)
+        T = np.ascontiguousarray(test, dtype=np.float64)
+        N, F = X.shape
+        if T.shape[0] % tiles:
+            raise WndcharmError("%d test rows are not whole images of %d tiles" % (T.shape[0], tiles))
+        n_img = T.shape[0] // tiles
+        w, mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (weights, mins, maxs))
+        probs = np.zeros((n_img, n_classes))
+        pred = np.zeros(n_img, dtype=np.int32)
+        norm = np.zeros(n_img)
+        check(lib().wc_wnd_classify_images(self._h, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I),
+                                           int(n_classes), w.ctypes.data_as(_lib.D), mn.ctypes.data_as(_lib.D),
+                                           mx.ctypes.data_as(_lib.D), T.ctypes.data_as(_lib.D), n_img, int(tiles),
+                                           1 if max_tile else 0, probs.ctypes.data_as(_lib.D),
+                                           pred.ctypes.data_as(_lib.I), norm.ctypes.data_as(_lib.D)))
+        return probs, pred, norm
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             lib().wc_engine_destroy(self._h)

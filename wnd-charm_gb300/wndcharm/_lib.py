@@ -79,6 +79,8 @@ def lib():
         L.wc_tiff_read.argtypes = [ctypes.c_char_p, vp, ctypes.c_longlong]
         L.wc_wnd_fit.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D, D, D]
         L.wc_wnd_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D, I]
+        L.wc_wnd_classify_images.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, D, I, D]
         _lib = L
     return _lib
 

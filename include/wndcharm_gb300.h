@@ -37,12 +37,16 @@ extern "C" {
 /* plan kinds: the reference's standard feature sets */
 #define WC_PLAN_SHORT 0 /* 1059 features, StdFeatureComputationPlans::getFeatureSet */
 #define WC_PLAN_LONG 1  /* 2919 features, StdFeatureComputationPlans::getFeatureSetLong */
+#define WC_PLAN_SHORT_COLOR 2 /* 2199 features, getFeatureSetColor (RGB images) */
+#define WC_PLAN_LONG_COLOR 3  /* 4059 features, getFeatureSetLongColor (RGB images) */
 
 /* pixel types accepted for input images */
 #define WC_U8 0
 #define WC_U16 1
 #define WC_F32 2
 #define WC_F64 3
+#define WC_RGB8 4  /* interleaved r, g, b bytes */
+#define WC_RGB16 5 /* interleaved r, g, b 16-bit samples (scaled to 8 bits over the image's range, as LoadTIFF does) */
 
 /* arithmetic form of an engine */
 #define WC_PREC_FP64 0  /* plain FP64 form: every family in double precision */
@@ -54,7 +58,10 @@ typedef struct wc_engine wc_engine; /* one GPU: device, stream, device memory po
 /* One input image.  `pixels` is a host pointer unless `on_device` is set, in
  * which case it is a device pointer on the engine's GPU.  Row-major, width
  * `width`, height `height`, elements of type `dtype`; `bits` is the image's
- * intensity depth (8 or 16), kept for the ImageMatrix::bits field. */
+ * intensity depth (8 or 16), kept for the ImageMatrix::bits field.  An RGB image
+ * (WC_RGB8 / WC_RGB16) becomes, as ImageMatrix::LoadTIFF reads a 3-sample TIFF,
+ * a grayscale plane 0.2989 r + 0.5870 g + 0.1140 b plus an HSV colour plane;
+ * the colour plans need RGB images, every other plan reads the grayscale plane. */
 typedef struct {
     const void *pixels;
     int dtype;

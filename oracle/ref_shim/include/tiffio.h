@@ -1,8 +1,9 @@
-/* TEST INFRASTRUCTURE ONLY: a do-nothing stand-in for libtiff's header so the
- * unmodified reference src/cmatrix.cpp compiles here.  Every open fails, so
- * ImageMatrix::LoadTIFF / SaveTiff return 0; the oracle build feeds pixels
- * through ImageMatrix::allocate + WriteablePixels instead (oracle/ref_shim/ref_capi.cpp),
- * and images are decoded in Python (tests/golden/make_golden.py). */
+/* TEST INFRASTRUCTURE ONLY: a stand-in for libtiff's header so the unmodified
+ * reference src/cmatrix.cpp compiles here.  Its definitions
+ * (oracle/ref_shim/tiff_stub.cpp) serve one in-memory image registered with
+ * wcref_tiff_set, so ImageMatrix::LoadTIFF can read RGB and grayscale pixels
+ * without files; with none registered every open fails.  Files themselves are
+ * decoded in Python (tests/golden/tiffread.py). */
 #ifndef WC_TIFF_STUB_H
 #define WC_TIFF_STUB_H
 #include <stddef.h>

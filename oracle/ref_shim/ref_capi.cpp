@@ -29,9 +29,24 @@ static void load_pixels(ImageMatrix &im, const double *pix, int w, int h, int bi
     im.finish();
 }
 
+// kind 0: short (1059), 1: long (2919), 2: short colour (2199), 3: long colour (4059)
 static const FeatureComputationPlan *std_plan(int kind) {
     if (kind == 1) return StdFeatureComputationPlans::getFeatureSetLong();
+    if (kind == 2) return StdFeatureComputationPlans::getFeatureSetColor();
+    if (kind == 3) return StdFeatureComputationPlans::getFeatureSetLongColor();
     return StdFeatureComputationPlans::getFeatureSet();
+}
+
+extern "C" void wcref_tiff_set(const void *data, int w, int h, int bits, int spp);
+
+// ImageMatrix::OpenImage on an in-memory image (the libtiff stand-in serves it
+// to the unmodified LoadTIFF): spp 3 = interleaved RGB, 8 or 16 bits.
+static int open_memory_image(ImageMatrix &im, const void *pix, int w, int h, int bits, int spp) {
+    wcref_tiff_set(pix, w, h, bits, spp);
+    char name[] = "memory.tif";
+    const int r = im.OpenImage(name, 0, nullptr, 0, 0);
+    wcref_tiff_set(nullptr, 0, 0, 0, 0);
+    return r;
 }
 
 extern "C" {
@@ -191,6 +206,66 @@ int wcref_wnd_images(const double *train, int N, int F, const int *labels, int C
     delete ts;
     verbosity = old_verbosity;
     return 0;
+}
+
+// LoadTIFF of an RGB image (spp 3): the grayscale plane (RGB2GRAY of the
+// 8-bit colour, 16-bit samples scaled to the image's RGB range first) and the
+// HSV colour plane (3 bytes per pixel), src/cmatrix.cpp:85-203.
+int wcref_load_rgb(const void *rgb, int w, int h, int bits, double *gray, unsigned char *hsv) {
+    ImageMatrix im;
+    if (open_memory_image(im, rgb, w, h, bits, 3) != 1) return -1;
+    readOnlyPixels rp = im.ReadablePixels();
+    readOnlyColors rc = im.ReadableColors();
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            gray[(size_t)y * w + x] = rp(y, x);
+            const HSVcolor c = rc(y, x);
+            unsigned char *o = hsv + 3 * ((size_t)y * w + x);
+            o[0] = c.h;
+            o[1] = c.s;
+            o[2] = c.v;
+        }
+    return 0;
+}
+
+// The reference's fuzzy colour tables need one fix to be well defined:
+// LoadColorsFunctions (src/colors/FuzzyCalc.cpp:582-623) returns when it
+// reaches the "rules:" line, before it writes the terminating entry (colour
+// -1) that color_value's loop (:625-650) stops at, so every membership lookup
+// that misses runs past the end of color_functions[] into whatever the linker
+// placed next (AddressSanitizer: global-buffer-overflow at FuzzyCalc.cpp:628).
+// After the first FindColor has loaded the tables, the entry after the last
+// loaded function is given colour -1, as the loader intends; everything else
+// runs unmodified.
+extern trapez_function color_functions[50];
+static void terminate_colour_functions() {
+    static bool done = false;
+    if (done) return;
+    FindColor(0, 0, 0, nullptr);
+    int k = 0;
+    while (k < 49 && color_functions[k].name[0]) k++;
+    color_functions[k].color = (TColor)-1;
+    done = true;
+}
+
+// FindColor (src/colors/FuzzyCalc.cpp:802-834) of one h, s, v.
+int wcref_find_colour(int h, int s, int v) {
+    terminate_colour_functions();
+    return (int)FindColor((short)h, (short)s, (short)v, nullptr);
+}
+
+// A standard plan (kinds as std_plan) on an RGB (spp 3) or grayscale (spp 1)
+// image read through LoadTIFF.
+int wcref_extract_image(int kind, const void *pix, int w, int h, int bits, int spp, double *out) {
+    terminate_colour_functions();
+    ImageMatrix im;
+    if (open_memory_image(im, pix, w, h, bits, spp) != 1) return -1;
+    const FeatureComputationPlan *plan = std_plan(kind);
+    std::vector<double> row(plan->n_features, 0.0);
+    FeatureComputationPlanExecutor ex(plan);
+    ex.run(&im, row, 0);
+    std::memcpy(out, row.data(), row.size() * sizeof(double));
+    return (int)row.size();
 }
 
 // The reference's own preprocessing and sampling of one image: the steps of

@@ -84,6 +84,7 @@ struct Moments4 {
 struct Img {
     int w = 0, h = 0;
     std::vector<double> p;
+    std::vector<unsigned char> hsv;  // colour plane (h, s, v per pixel) of an RGB image, else empty
     Img() {}
     Img(int w_, int h_) : w(w_), h(h_), p((size_t)w_ * h_, 0.0) {}
     double &at(int y, int x) { return p[(size_t)y * w + x]; }
@@ -1375,22 +1376,235 @@ static void f_gabor(const Img &im, double *out) {
     }
 }
 
+// ---------------------------------------------------------------- colour
+// RGB2HSV and RGB2GRAY (src/cmatrix.h:95-160).
+static void rgb2hsv(unsigned char R, unsigned char G, unsigned char B, unsigned char *hsv) {
+    double r = (double)R / 255, g = (double)G / 255, b = (double)B / 255;
+    double mx = std::max(r, std::max(g, b)), mn = std::min(r, std::min(g, b));
+    double delta = mx - mn;
+    unsigned char hh = 0, s = 0, v = (unsigned char)(mx * 240.0);
+    if (mx != 0.0) s = (unsigned char)((delta / mx) * 240.0);
+    if (s != 0) {
+        double h = 0;
+        if (r == mx) h = (g - b) / delta;
+        else if (g == mx) h = 2 + (b - r) / delta;
+        else if (b == mx) h = 4 + (r - g) / delta;
+        h *= 60.0;
+        if (h >= 360) h -= 360.0;
+        if (h < 0.0) h += 360.0;
+        hh = (unsigned char)(h * (240.0 / 360.0));
+    }
+    hsv[0] = hh;
+    hsv[1] = s;
+    hsv[2] = v;
+}
+static double rgb2gray(unsigned char r, unsigned char g, unsigned char b) {
+    return 0.2989 * r + 0.5870 * g + 0.1140 * b;
+}
+
+// ImageMatrix::LoadTIFF for 3 samples per pixel (src/cmatrix.cpp:128-199):
+// 16-bit samples scaled to bytes over the image's min..max of all channels.
+static Img make_rgb_img(const void *pix, int w, int h, int bits) {
+    Img im(w, h);
+    im.hsv.resize((size_t)3 * w * h);
+    const size_t n = (size_t)w * h;
+    double lo = 0, scale = 0;
+    if (bits > 8) {
+        const unsigned short *p = (const unsigned short *)pix;
+        double mn = DBL_MAX, mx = -DBL_MAX;
+        for (size_t i = 0; i < 3 * n; i++) {
+            mn = std::min(mn, (double)p[i]);
+            mx = std::max(mx, (double)p[i]);
+        }
+        lo = mn;
+        scale = 255.0 / (mx - mn);
+    }
+    for (size_t i = 0; i < n; i++) {
+        unsigned char c[3];
+        for (int k = 0; k < 3; k++) {
+            if (bits > 8) {
+                double t = ((double)((const unsigned short *)pix)[3 * i + k] - lo) * scale;
+                c[k] = std::isnan(t) ? 0 : (unsigned char)t;  // a flat image: 0 * inf
+            } else {
+                c[k] = ((const unsigned char *)pix)[3 * i + k];
+            }
+        }
+        im.p[i] = rgb2gray(c[0], c[1], c[2]);
+        rgb2hsv(c[0], c[1], c[2], &im.hsv[3 * i]);
+    }
+    return im;
+}
+
+// The fuzzy colour classifier (src/colors/FuzzyCalc.cpp:625-834, constants
+// src/colors/FuzzyCalc.h:42-148).  Colours: 1 white, 2 light grey, 3 dark
+// grey, 4 black, 5 red, 6 pink, 7 dark brown, 8 light brown, 9 dark orange,
+// 10 light orange, 11 yellow, 12 olive, 13 light green, 14 dark green, 15 teal,
+// 16 aqua, 17 blue, 18 dark fuchsia, 19 light fuchsia.
+namespace fuzzy {
+struct Trapezoid { int colour; double start, max1, max2, end; };
+static const Trapezoid kHueFunctions[11] = {
+    {5, 0, 0, 0, 11},       {9, 0, 17, 17, 27},       {10, 20, 27, 27, 37},  {11, 27, 39, 39, 47},
+    {13, 40, 50, 50, 80},   {14, 50, 80, 80, 120},    {16, 80, 120, 120, 160}, {17, 120, 160, 160, 200},
+    {18, 160, 200, 200, 220}, {19, 200, 220, 220, 230}, {5, 220, 240, 240, 240}};
+// the rule base, one rule per (hue colour, saturation class 1..6, value class
+// 1..5) in this order; the output colour 0 marks the two rules whose colour
+// name the reference misspells (no colour sums them)
+static const int kHueColour[10] = {5, 9, 10, 11, 13, 14, 16, 17, 18, 19};
+struct Rule { int hue, sat, val, colour; };
+static std::vector<Rule> rules() {
+    static const unsigned char grid[300] = {
+        4, 4, 3, 2, 1, 4, 3, 3, 19, 6, 4, 7, 18, 6, 6, 4, 7, 8, 19, 6, 4, 7, 7, 5, 5, 4, 4, 5, 5, 5,
+        4, 3, 3, 2, 1, 4, 3, 3, 2, 1, 4, 7, 3, 8, 6, 4, 7, 7, 8, 10, 4, 7, 7, 8, 9, 4, 7, 7, 8, 9,
+        4, 3, 3, 2, 1, 4, 3, 3, 2, 1, 4, 3, 3, 2, 10, 4, 7, 8, 8, 10, 4, 7, 8, 8, 10, 4, 7, 8, 8, 10,
+        4, 3, 3, 2, 1, 4, 3, 3, 2, 1, 4, 3, 12, 12, 11, 4, 12, 12, 12, 11, 4, 12, 12, 12, 11, 4, 12, 12, 12, 11,
+        4, 3, 3, 2, 1, 4, 3, 3, 2, 1, 4, 12, 12, 13, 13, 4, 14, 14, 13, 13, 4, 14, 14, 13, 13, 4, 14, 14, 13, 13,
+        4, 3, 3, 2, 1, 4, 3, 3, 13, 13, 4, 14, 14, 13, 13, 4, 14, 14, 13, 13, 4, 14, 14, 13, 13, 4, 14, 14, 13, 13,
+        4, 3, 3, 2, 1, 4, 3, 3, 15, 16, 4, 15, 17, 17, 16, 4, 15, 17, 16, 16, 4, 15, 17, 16, 16, 4, 15, 15, 16, 16,
+        4, 3, 3, 2, 1, 4, 3, 0, 16, 16, 4, 18, 0, 19, 16, 4, 17, 17, 17, 17, 4, 17, 17, 17, 17, 4, 17, 17, 17, 17,
+        4, 3, 3, 2, 1, 4, 3, 18, 19, 19, 4, 18, 18, 19, 19, 4, 18, 18, 19, 19, 4, 18, 18, 19, 19, 4, 7, 18, 18, 19,
+        4, 3, 3, 2, 1, 4, 3, 2, 19, 19, 4, 18, 18, 19, 19, 4, 18, 18, 19, 19, 4, 7, 18, 19, 19, 4, 7, 18, 18, 19};
+    std::vector<Rule> r;
+    for (int k = 0; k < 300; k++) r.push_back({kHueColour[k / 30], (k / 5) % 6 + 1, k % 5 + 1, grid[k]});
+    return r;
+}
+// color_value: the first trapezoid of the colour giving a positive membership
+static double colour_value(int colour, double x) {
+    double res = 0;
+    for (const Trapezoid &t : kHueFunctions) {
+        if (t.colour != colour) continue;
+        if (x < t.start || x > t.end) res = 0;
+        else if (x >= t.max1 && x <= t.max2) res = 1;
+        else if (x < t.max1) res = (x - t.start) / (t.max1 - t.start);
+        else res = 1 - (x - t.max2) / (t.end - t.max2);
+        if (res > 0) return res;
+    }
+    return res;
+}
+// saturation classes 1..6: grey, almost grey, tend grey, medium grey, tend clear, clear
+static double saturation_value(int cls, double x) {
+    switch (cls) {
+        case 1:
+            if (x < 0) return 0;  // MIN_GREY
+            if (x < -0.1 || x > 40) return 0;
+            if (x < 0) return (x - -0.1) / (0 - -0.1);
+            return 1 - ((x - 0) / (40 - 0));
+        case 2:
+            if (x < 10 || x > 70) return 0;
+            if (x < 30) return (x - 10) / (30.0 - 10);
+            return 1 - ((x - 30) / (70.0 - 30));
+        case 3:
+            if (x < 30 || x > 120) return 0;
+            if (x < 70) return (x - 30) / (70.0 - 30);
+            return 1 - ((x - 70) / (120.0 - 70));
+        case 4:
+            if (x < 60 || x > 180) return 0;
+            if (x < 120) return (x - 60) / (120.0 - 60);
+            return 1 - ((x - 120) / (180.0 - 120));
+        case 5:
+            if (x < 120 || x > 240) return 0;
+            if (x < 180) return (x - 120) / (180.0 - 120);
+            return 1 - ((x - 180) / (240.0 - 180));
+        default:
+            if (x < 180 || x > 240.1) return 0;
+            if (x <= 240) return (x - 180) / (240.0 - 180);
+            return 1 - ((x - 240) / (240.1 - 240));
+    }
+}
+// value classes 1..5: dark, almost dark, tend dark, tend light, light
+static double value_value(int cls, double x) {
+    switch (cls) {
+        case 1:
+            if (x < 0) return 0;  // MIN_DARK
+            if (x < -0.1 || x > 60) return 0;
+            if (x < 0) return (x - -0.1) / (0 - -0.1);
+            return 1 - ((x - 0) / (60 - 0));
+        case 2:
+            if (x < 0 || x > 120) return 0;
+            if (x < 60) return (x - 0) / (60.0 - 0);
+            return 1 - ((x - 60) / (120.0 - 60));
+        case 3:
+            if (x < 60 || x > 180) return 0;
+            if (x < 120) return (x - 60) / (120.0 - 60);
+            return 1 - ((x - 120) / (180.0 - 120));
+        case 4:
+            if (x < 120 || x > 240) return 0;
+            if (x < 180) return (x - 120) / (180.0 - 120);
+            return 1 - ((x - 180) / (240.0 - 180));
+        default:
+            if (x < 200 || x > 240.1) return 0;
+            if (x <= 240) return (x - 200) / (240.0 - 200);
+            return 1 - ((x - 240) / (240.1 - 240));
+    }
+}
+// CalculateRules2 + FindColor: per colour, the rule products in rule order
+static int find_colour(int h, int s, int v) {
+    static const std::vector<Rule> R = rules();
+    double best = 0;
+    int res = 2;
+    for (int colour = 1; colour <= 19; colour++) {
+        double sum = 0;
+        for (const Rule &r : R) {
+            if (r.colour != colour) continue;
+            double ret = colour_value(r.hue, h);
+            if (ret == 0) continue;
+            ret = ret * saturation_value(r.sat, s);
+            if (ret == 0) continue;
+            ret = ret * value_value(r.val, v);
+            sum = sum + ret;
+        }
+        if (sum > best) {
+            best = sum;
+            res = colour;
+        }
+    }
+    return res;
+}
+}  // namespace fuzzy
+
+// HueTransform / ColorTransform (src/cmatrix.cpp:1023-1066)
+static Img hue_plane(const Img &in) {
+    Img o(in.w, in.h);
+    for (size_t i = 0; i < o.n(); i++) o.p[i] = in.hsv[3 * i];
+    return o;
+}
+static Img colour_plane(const Img &in) {
+    Img o(in.w, in.h);
+    const double max_range = std::pow((double)2, 8) - 1;
+    for (size_t i = 0; i < o.n(); i++) {
+        unsigned long c = fuzzy::find_colour(in.hsv[3 * i], in.hsv[3 * i + 1], in.hsv[3 * i + 2]);
+        o.p[i] = int((max_range * c) / 19);
+    }
+    return o;
+}
+// ColorHistogram::execute (src/FeatureAlgorithms.cpp:506-531)
+static void f_color_hist(const Img &im, double *out) {
+    for (int c = 0; c < 20; c++) out[c] = 0;
+    for (size_t i = 0; i < im.n(); i++) out[fuzzy::find_colour(im.hsv[3 * i], im.hsv[3 * i + 1], im.hsv[3 * i + 2])]++;
+    for (int c = 0; c < 20; c++) out[c] /= (unsigned)(im.w * im.h);
+}
+
 // ---------------------------------------------------------------- plans
 enum Alg { A_CHEBFOURIER, A_CHEB, A_ZERNIKE, A_HARALICK, A_MSHIST, A_TAMURA, A_COMB, A_RADON,
-           A_FRACTAL, A_PIXSTATS, A_EDGEF, A_OBJ, A_INVOBJ, A_GABOR, A_GINI, A_COUNT };
+           A_FRACTAL, A_PIXSTATS, A_EDGEF, A_OBJ, A_INVOBJ, A_GABOR, A_GINI, A_COLORHIST, A_COUNT };
 static const char *kAlgName[A_COUNT] = {
     "Chebyshev-Fourier Coefficients", "Chebyshev Coefficients", "Zernike Coefficients",
     "Haralick Textures", "Multiscale Histograms", "Tamura Textures", "Comb Moments",
     "Radon Coefficients", "Fractal Features", "Pixel Intensity Statistics", "Edge Features",
-    "Otsu Object Features", "Inverse-Otsu Object Features", "Gabor Textures", "Gini Coefficient"};
-static const int kAlgN[A_COUNT] = {32, 32, 72, 28, 24, 6, 48, 12, 20, 5, 28, 34, 34, 7, 1};
+    "Otsu Object Features", "Inverse-Otsu Object Features", "Gabor Textures", "Gini Coefficient", "Color Histogram"};
+static const int kAlgN[A_COUNT] = {32, 32, 72, 28, 24, 6, 48, 12, 20, 5, 28, 34, 34, 7, 1, 20};
 
 typedef void (*AlgFn)(const Img &, double *);
 static const AlgFn kAlgFn[A_COUNT] = {f_cheb_fourier, f_cheb_coeffs, f_zernike, f_haralick, f_mshist,
     f_tamura, f_comb, f_radon, f_fractal, f_pixstats, f_edge_features, f_objects, f_inv_objects,
-    f_gabor, f_gini};
+    f_gabor, f_gini, f_color_hist};
 
-struct Group { int alg; std::string chain; };  // chain: transforms in application order, "F W" etc.
+// chain: transforms in application order, space-separated tokens ("Fourier Wavelet");
+// the reference's "Color Transform" is the token "ColorTransform"
+struct Group { int alg; std::string chain; };
+
+static std::string display_name(const std::string &token) {
+    return token == "ColorTransform" ? "Color Transform" : token;
+}
 
 static std::string chain_text(const std::string &chain) {
     // "Fourier Wavelet" (Fourier first) -> "(Wavelet (Fourier ()))"
@@ -1403,7 +1617,7 @@ static std::string chain_text(const std::string &chain) {
         p = q + 1;
     }
     std::string s = "()";
-    for (auto &x : t) s = "(" + x + " " + s + ")";
+    for (auto &x : t) s = "(" + display_name(x) + " " + s + ")";
     return s;
 }
 
@@ -1420,8 +1634,17 @@ static std::vector<Group> make_plan(int kind) {
         for (int a : {A_COMB, A_HARALICK, A_MSHIST, A_TAMURA, A_RADON, A_FRACTAL, A_PIXSTATS, A_GINI})
             g.push_back({a, c});
     };
-    if (kind == 1) {
+    // StdFeatureComputationPlans::addColorFeatures, src/Tasks.cpp:445-459
+    auto colour = [&]() {
+        g.push_back({A_COLORHIST, ""});
+        B("ColorTransform"); C("ColorTransform");
+        B("Hue"); C("Hue");
+        B("Hue Fourier"); C("Hue Fourier");
+        B("Hue Chebyshev"); C("Hue Chebyshev");
+    };
+    if (kind == 1 || kind == 3) {
         A(""); B(""); C("");
+        if (kind == 3) colour();
         B("Fourier"); C("Fourier");
         B("Wavelet"); C("Wavelet");
         B("Chebyshev"); C("Chebyshev");
@@ -1446,6 +1669,7 @@ static std::vector<Group> make_plan(int kind) {
             {A_TAMURA, "Fourier Chebyshev"}, {A_TAMURA, "Fourier"}, {A_TAMURA, "Wavelet"},
             {A_TAMURA, "Fourier Wavelet"}, {A_ZERNIKE, ""}, {A_ZERNIKE, "Fourier"}};
         for (auto &x : s) g.push_back(x);
+        if (kind == 2) colour();
     }
     return g;
 }
@@ -1457,10 +1681,11 @@ struct PlanInfo {
     int n = 0;
 };
 
+// kind 0: short, 1: long, 2: short colour, 3: long colour
 static const PlanInfo &plan_info(int kind) {
-    static PlanInfo P[2];
-    static std::once_flag once[2];
-    kind = kind ? 1 : 0;
+    static PlanInfo P[4];
+    static std::once_flag once[4];
+    if (kind < 0 || kind > 3) kind = 0;
     std::call_once(once[kind], [kind]() {
         PlanInfo &pi = P[kind];
         pi.groups = make_plan(kind);
@@ -1475,6 +1700,9 @@ static const PlanInfo &plan_info(int kind) {
 }
 
 static Img apply_transform(const std::string &t, const Img &in) {
+    if (t == "ColorTransform") return in;  // the reference's EmptyTransform: a copy (colour plane included)
+    if (t == "Hue") return hue_plane(in);
+    if (t == "Color") return colour_plane(in);
     if (t == "Fourier") return fourier(in);
     if (t == "Chebyshev") return chebyshev(in, 0);
     if (t == "Wavelet") return wavelet(in);
@@ -1614,6 +1842,11 @@ static bool parse_group(const std::string &s, Group &g) {
     std::vector<std::string> t;
     std::string rest = s.substr(p + 1);
     while (rest.size() > 2 && rest[0] == '(' && rest[1] != ')') {
+        if (rest.compare(0, 17, "(Color Transform ") == 0) {
+            t.push_back("ColorTransform");
+            rest = rest.substr(17);
+            continue;
+        }
         size_t q = rest.find(' ');
         t.push_back(rest.substr(1, q - 1));
         rest = rest.substr(q + 1);
@@ -1801,6 +2034,23 @@ int wco_extract_std_batch(int kind, const double *pix, const long *offs, const i
     for (auto &t : th) t.join();
     return pi.n;
 }
+
+// Colour: an RGB image (interleaved 8- or 16-bit samples) through a plan.
+int wco_extract_rgb(int kind, const void *rgb, int w, int h, int bits, double *out) {
+    const PlanInfo &pi = plan_info(kind);
+    Img root = make_rgb_img(rgb, w, h, bits);
+    run_groups(pi.groups, pi.offset, root, out);
+    return pi.n;
+}
+
+int wco_load_rgb(const void *rgb, int w, int h, int bits, double *gray, unsigned char *hsv) {
+    Img im = make_rgb_img(rgb, w, h, bits);
+    std::memcpy(gray, im.p.data(), sizeof(double) * im.n());
+    std::memcpy(hsv, im.hsv.data(), im.hsv.size());
+    return 0;
+}
+
+int wco_find_colour(int h, int s, int v) { return fuzzy::find_colour(h, s, v); }
 
 int wco_extract_group(const char *group, const double *pix, int w, int h, int bits, double *out) {
     (void)bits;

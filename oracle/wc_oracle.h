@@ -26,6 +26,14 @@ int wco_extract_std_batch(int kind, const double *pix, const long *pix_offsets,
                           const int *ws, const int *hs, int n, int bits,
                           double *out, int nthreads);
 
+// Colour: an RGB image (interleaved r, g, b; bits 8 or 16) read as LoadTIFF
+// reads a 3-sample TIFF (gray plane + HSV colour plane), then a plan (kinds 0-3;
+// 2 = short colour, 3 = long colour).  wco_load_rgb gives the two planes
+// (hsv: 3 bytes per pixel); wco_find_colour the fuzzy colour (1..19) of h, s, v.
+int wco_extract_rgb(int kind, const void *rgb, int w, int h, int bits, double *out);
+int wco_load_rgb(const void *rgb, int w, int h, int bits, double *gray, unsigned char *hsv);
+int wco_find_colour(int h, int s, int v);
+
 // One group by reference name, e.g. "Zernike Coefficients (Fourier ())".
 int wco_extract_group(const char *group, const double *pix, int w, int h, int bits, double *out);
 

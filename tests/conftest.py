@@ -45,8 +45,16 @@ def golden(name):
 
 
 def golden_names(kind):
-    fn = "names_long.txt" if kind == 1 else "names_short.txt"
+    fn = {0: "names_short.txt", 1: "names_long.txt", 2: "names_color_short.txt", 3: "names_color_long.txt"}[kind]
     return open(os.path.join(GOLDEN, fn)).read().splitlines()
+
+
+def oracle_features_rgb(lib, img, bits, kind):
+    """The oracle's plan `kind` on an RGB image ((h, w, 3) uint8 / uint16)."""
+    a = np.ascontiguousarray(img)
+    out = np.zeros(lib.wco_plan_n_features(kind))
+    lib.wco_extract_rgb(kind, ctypes.c_void_p(a.ctypes.data), a.shape[1], a.shape[0], bits, out.ctypes.data_as(D))
+    return out
 
 
 def oracle_features(lib, img, bits=16, kind=1):

@@ -8,7 +8,7 @@ Sources:
     (oracle/_ref/libwndref.so), run on those images and on small seeded
     synthetic images, for feature vectors, transform outputs and WND-5.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only preproc|wnd_images]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--only preproc|wnd_images|colour]
 """
 import ctypes
 import os
@@ -160,6 +160,47 @@ def wnd_image_fixtures():
     np.savez_compressed(os.path.join(HERE, "reference_wnd_images.npz"), **out)
 
 
+def colour_image(rng, w, h, bits):
+    """Seeded synthetic RGB image: three blob images (different classes) as
+    the channels; 8-bit, or 12-bit values in 16-bit samples."""
+    ch = [synth.blob_image(rng, c, w, h, mean=60 + 40 * c, sd=30, scale=1 if bits == 8 else 16,
+                           maxval=255 if bits == 8 else 4095) for c in range(3)]
+    return np.ascontiguousarray(np.stack(ch, axis=-1).astype(np.uint8 if bits == 8 else np.uint16))
+
+
+def colour_fixtures():
+    """Colour images through the reference's LoadTIFF (gray + HSV planes) and
+    its colour plans (with the terminator its fuzzy-colour loader omits,
+    supplied by oracle/ref_shim/ref_capi.cpp); FindColor on random h, s, v."""
+    rng = np.random.default_rng(4242)
+    rgb8 = colour_image(rng, 64, 48, 8)
+    rgb16 = colour_image(rng, 40, 56, 16)
+    y, x = np.mgrid[0:256, 0:256]
+    grid = np.ascontiguousarray(np.stack([x, y, (7 * x + 13 * y) % 256], axis=-1).astype(np.uint8))
+    out = {"img_rgb8": rgb8, "img_rgb16": rgb16, "img_grid": grid}
+    for key, img, bits in (("rgb8", rgb8, 8), ("rgb16", rgb16, 16)):
+        h, w = img.shape[:2]
+        gray, hsv = np.zeros(w * h), np.zeros(3 * w * h, dtype=np.uint8)
+        LIB.wcref_load_rgb(img.ctypes.data, w, h, bits, gray.ctypes.data_as(D), hsv.ctypes.data)
+        out["gray_" + key] = gray.reshape(h, w)
+        out["hsv_" + key] = hsv.reshape(h, w, 3)
+        for kind in (2, 3):
+            f = np.zeros(LIB.wcref_plan_n_features(kind))
+            LIB.wcref_extract_image(kind, img.ctypes.data, w, h, bits, 3, f.ctypes.data_as(D))
+            out["plan%d_%s" % (kind, key)] = f
+        print("colour", key, flush=True)
+    f = np.zeros(LIB.wcref_plan_n_features(2))
+    LIB.wcref_extract_image(2, grid.ctypes.data, 256, 256, 8, 3, f.ctypes.data_as(D))
+    out["plan2_grid"] = f
+    hsv = rng.integers(0, 256, size=(20000, 3)).astype(np.int32)
+    out["fc_hsv"] = hsv
+    out["fc_colour"] = np.array([LIB.wcref_find_colour(int(a), int(b), int(c)) for a, b, c in hsv], dtype=np.int32)
+    np.savez_compressed(os.path.join(HERE, "reference_colour.npz"), **out)
+    for kind, fn in ((2, "names_color_short.txt"), (3, "names_color_long.txt")):
+        with open(os.path.join(HERE, fn), "w") as fh:
+            fh.write("\n".join(names(kind)) + "\n")
+
+
 def read_sig(path):
     lines = open(path).read().splitlines()[2:]
     return np.array([float(l.split("\t")[0]) for l in lines])
@@ -270,7 +311,10 @@ if __name__ == "__main__":
         preproc_fixtures()
     elif only == "wnd_images":
         wnd_image_fixtures()
+    elif only == "colour":
+        colour_fixtures()
     else:
         main()
         preproc_fixtures()
         wnd_image_fixtures()
+        colour_fixtures()

@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # files whose arithmetic restates a CPU order of operations bit for bit: no
 # multiply-add contraction anywhere in them
 EXTRA = {"k_haralick.cu": ["-fmad=false"], "k_groupa.cu": ["-fmad=false"], "k_fft.cu": ["-fmad=false"],
-         "k_pre.cu": ["-fmad=false"]}
+         "k_pre.cu": ["-fmad=false"], "k_color.cu": ["-fmad=false"]}
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + CSRC, "-I" + os.path.join(os.path.dirname(HERE), "include")]
 

@@ -103,10 +103,24 @@ struct Node {
     std::vector<int> chain;
 };
 
+static size_t pixel_bytes(int dtype) {
+    switch (dtype) {
+        case WC_U8: return 1;
+        case WC_U16: return 2;
+        case WC_F32: return 4;
+        case WC_RGB8: return 3;
+        case WC_RGB16: return 6;
+        default: return 8;
+    }
+}
+
 static int out_shape(int xf, int w, int h, int &ow, int &oh) {
     switch (xf) {
         case X_FOURIER: ow = w; oh = h; return 0;
-        case X_EDGE: ow = w; oh = h; return 0;
+        case X_EDGE:
+        case X_COLOR:
+        case X_HUE:
+        case X_CTCOPY: ow = w; oh = h; return 0;
         case X_WAVELET: ow = 2 * ((w + 9) / 2); oh = 2 * ((h + 9) / 2); return 0;
         case X_CHEBYSHEV: {
             int N = w < h ? w : h;
@@ -147,12 +161,41 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     int maxdepth = 0;
     for (auto &nd : nodes) maxdepth = std::max(maxdepth, nd.depth);
 
+    // ---- colour: only the root plane and its "Color Transform" copies carry
+    // the HSV plane that Color, Hue and the Color Histogram read
+    std::vector<char> colour_node(NN, 0);
+    colour_node[0] = 1;
+    bool needs_colour = false;
+    for (int k = 1; k < NN; k++) {  // parents precede children
+        if (nodes[k].xf == X_CTCOPY) colour_node[k] = colour_node[nodes[k].parent];
+        if (nodes[k].xf == X_COLOR || nodes[k].xf == X_HUE) {
+            if (!colour_node[nodes[k].parent])
+                return set_err(WC_ERR_UNSUPPORTED, "the %s transform reads the colour plane, which only the image "
+                               "itself (or a Color Transform copy) has", kXfName[nodes[k].xf]);
+            needs_colour = true;
+        }
+    }
+    for (size_t g = 0; g < plan.groups.size(); g++)
+        if (plan.groups[g].alg == A_COLORHIST) {
+            if (!colour_node[group_node[g]])
+                return set_err(WC_ERR_UNSUPPORTED, "Color Histogram reads the colour plane: only of the image itself");
+            needs_colour = true;
+        }
+    bool any_rgb = false;
+    for (int b = 0; b < n; b++) {
+        const bool rgb = imgs[b].dtype == WC_RGB8 || imgs[b].dtype == WC_RGB16;
+        if (needs_colour && !rgb) return set_err(WC_ERR_ARG, "image %d: the plan's colour features need an RGB image", b);
+        any_rgb |= rgb;
+    }
+
     // ---- planes
     std::vector<Plane> planes((size_t)n * NN);
     size_t arena_elems = 0;
     for (int b = 0; b < n; b++) {
         if (imgs[b].width < 1 || imgs[b].height < 1 || !imgs[b].pixels)
             return set_err(WC_ERR_ARG, "image %d: bad size or null pixels", b);
+        if (imgs[b].dtype < WC_U8 || imgs[b].dtype > WC_RGB16)
+            return set_err(WC_ERR_ARG, "image %d: unknown pixel type %d", b, imgs[b].dtype);
         for (int k = 0; k < NN; k++) {
             Plane &P = planes[(size_t)b * NN + k];
             if (k == 0) {
@@ -205,6 +248,17 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     };
     const size_t m_planes = put_vec(planes);
     const size_t m_stats = meta.take(sizeof(PlaneStats) * planes.size());
+    // colour planes (HSV bytes) of the RGB images, and the fuzzy classifier's table
+    std::vector<long long> clr_off(n, 0);
+    size_t clr_bytes = 0;
+    long long fuzzy_tab = 0;
+    for (int b = 0; b < n; b++)
+        if (imgs[b].dtype == WC_RGB8 || imgs[b].dtype == WC_RGB16) {
+            clr_off[b] = (long long)clr_bytes;
+            clr_bytes += ((size_t)3 * imgs[b].width * imgs[b].height + 255) & ~(size_t)255;
+        }
+    const size_t m_clr = put_vec(clr_off);
+    if (any_rgb) fuzzy_tab = E->tabs.add_lazy("fuzzy colours", [] { return fuzzy_membership_table(); });
 
     struct TL { size_t jobs, aux1, aux2, aux3; size_t ws; };
     std::vector<std::vector<TL>> tl(maxdepth + 1, std::vector<TL>(X_COUNT));
@@ -283,13 +337,14 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     std::vector<size_t> in_off(n);
     for (int b = 0; b < n; b++) {
         if (imgs[b].on_device) continue;
-        size_t es = imgs[b].dtype == WC_U8 ? 1 : imgs[b].dtype == WC_U16 ? 2 : imgs[b].dtype == WC_F32 ? 4 : 8;
+        size_t es = pixel_bytes(imgs[b].dtype);
         in_off[b] = in_bytes;
         in_bytes += ((size_t)imgs[b].width * imgs[b].height * es + 255) & ~(size_t)255;
     }
     if ((r = E->meta.ensure(meta.used + 256))) return r;
     if ((r = E->ws.ensure(ws.used + 256))) return r;
     if ((r = E->stage.ensure(in_bytes + 256))) return r;
+    if ((r = E->clr.ensure(clr_bytes + 256))) return r;
     if ((r = E->tabs.sync(E->st))) return r;
     E->hmeta.resize(meta.used + 256);
     for (auto &bl : blobs)
@@ -299,7 +354,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     CK(cudaMemcpyAsync(dm, E->hmeta.data(), meta.used, cudaMemcpyHostToDevice, E->st));
     for (int b = 0; b < n; b++) {
         const wc_image_desc &I = imgs[b];
-        size_t es = I.dtype == WC_U8 ? 1 : I.dtype == WC_U16 ? 2 : I.dtype == WC_F32 ? 4 : 8;
+        size_t es = pixel_bytes(I.dtype);
         const void *src = I.pixels;
         if (!I.on_device) {
             CK(cudaMemcpyAsync((char *)E->stage.p + in_off[b], I.pixels, (size_t)I.width * I.height * es,
@@ -307,7 +362,11 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
             src = (char *)E->stage.p + in_off[b];
         }
         ProfScope ps(ctx, "convert");
-        launch_convert(ctx, src, I.dtype, arena + planes[(size_t)b * NN].off, (long long)I.width * I.height);
+        if (I.dtype == WC_RGB8 || I.dtype == WC_RGB16)
+            launch_rgb_ingest(ctx, src, I.dtype, (long long)I.width * I.height, arena + planes[(size_t)b * NN].off,
+                              (unsigned char *)E->clr.p + clr_off[b]);
+        else
+            launch_convert(ctx, src, I.dtype, arena + planes[(size_t)b * NN].off, (long long)I.width * I.height);
     }
     const Plane *dplanes = (const Plane *)(dm + m_planes);
     PlaneStats *dstats = (PlaneStats *)(dm + m_stats);
@@ -321,6 +380,9 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     fr.ws = dw;
     fr.tabs = E->tabs.d();
     fr.feat = dfeat;
+    fr.clr = (const unsigned char *)E->clr.p;
+    fr.clr_off = (const long long *)(dm + m_clr);
+    fr.fuzzy = E->tabs.d() + fuzzy_tab;
     Ctx lc[WC_LANES];
     for (int k = 0; k < WC_LANES; k++) {
         lc[k] = ctx;
@@ -354,7 +416,10 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
             const TJob *dj = (const TJob *)(dm + L.jobs);
             const int nj = (int)G.jobs.size();
             ProfScope ps(ctx, kXfName[x]);
-            if (x == X_EDGE) launch_edge(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh);
+            if (x == X_COLOR || x == X_HUE || x == X_CTCOPY)
+                launch_color_xf(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh, x, NN, (const unsigned char *)E->clr.p,
+                                (const long long *)(dm + m_clr), E->tabs.d() + fuzzy_tab);
+            else if (x == X_EDGE) launch_edge(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh);
             else if (x == X_WAVELET)
                 launch_wavelet(ctx, arena, dplanes, dj, nj, G.maxw, G.maxh, (double *)(dw + L.ws),
                                (const long long *)(dm + L.aux1));
@@ -435,7 +500,7 @@ const char *wc_last_error(void) { return g_err.c_str(); }
 const char *wc_version(void) { return "wndcharm-gb300 0.1 (sm_103a)"; }
 
 int wc_plan_get(int kind, const wc_plan **out) {
-    if (!out || (kind != WC_PLAN_SHORT && kind != WC_PLAN_LONG)) return set_err(WC_ERR_ARG, "wc_plan_get: bad kind");
+    if (!out || kind < WC_PLAN_SHORT || kind > WC_PLAN_LONG_COLOR) return set_err(WC_ERR_ARG, "wc_plan_get: bad kind");
     *out = static_cast<const wc_plan *>(standard_plan(kind));
     return WC_OK;
 }

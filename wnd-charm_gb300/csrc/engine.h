@@ -93,6 +93,7 @@ struct wc_engine {
     long long launches = 0;
     wc::DevBuf arena, feat, ws, meta, stage;
     wc::DevBuf pre, pre_meta;  // preprocessing: images, opened and sample planes; jobs and positions
+    wc::DevBuf clr;            // HSV colour planes of the batch's RGB images
     wc::Tables tabs;
     std::vector<char> hmeta, hpre;
     std::mutex mu;

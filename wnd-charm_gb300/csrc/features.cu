@@ -458,6 +458,11 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early) {
                         (const int *)(fr.meta + fs.off["slots" + std::to_string(A_GINI)]), keys, koff, fr.feat);
     }
     {
+        ProfScope ps(c, "Color Histogram");
+        if (nj(A_COLORHIST)) launch_color_hist(c, fr.planes, jobs(A_COLORHIST), nj(A_COLORHIST), fr.clr, fr.clr_off,
+                                               fr.fuzzy, fr.feat);
+    }
+    {
         ProfScope ps(c, "Multiscale Histograms");
         if (nj(A_MSHIST)) launch_mshist(c, fr.arena, fr.planes, fr.stats, jobs(A_MSHIST), nj(A_MSHIST), fr.feat);
     }

@@ -105,6 +105,17 @@ void launch_objects(Ctx &c, const double *arena, const Plane *planes, const Plan
                     long long maxpix, const OBJob *oj, double *ws, const Plane *inv_planes, PlaneStats *inv_stats,
                     double *thr, unsigned long long *acc, double *feat);
 
+// k_color.cu: RGB ingest, the fuzzy colour classifier's membership table
+// (host-made), the Color / Hue / Color Transform transforms and the Color
+// Histogram family.  clr: HSV bytes (3 per pixel) of each image at
+// clr_off[image] bytes.
+std::vector<double> fuzzy_membership_table();
+void launch_rgb_ingest(Ctx &c, const void *src, int dtype, long long n, double *gray, unsigned char *hsv);
+void launch_color_xf(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh, int xf,
+                     int nn, const unsigned char *clr, const long long *clr_off, const double *tab);
+void launch_color_hist(Ctx &c, const Plane *planes, const FJob *jobs, int njobs, const unsigned char *clr,
+                       const long long *clr_off, const double *tab, double *feat);
+
 // k_pre.cu: preprocessing (crop, Downsample, normalize) of each image into its
 // opened plane, then one rotated / tiled plane per sample.  Offsets are in
 // doubles into the preprocessing arena (tables: into the position table).

@@ -18,9 +18,9 @@ const char *const kAlgName[A_COUNT] = {
     "Chebyshev-Fourier Coefficients", "Chebyshev Coefficients", "Zernike Coefficients",
     "Haralick Textures", "Multiscale Histograms", "Tamura Textures", "Comb Moments",
     "Radon Coefficients", "Fractal Features", "Pixel Intensity Statistics", "Edge Features",
-    "Otsu Object Features", "Inverse-Otsu Object Features", "Gabor Textures", "Gini Coefficient"};
-const int kAlgN[A_COUNT] = {32, 32, 72, 28, 24, 6, 48, 12, 20, 5, 28, 34, 34, 7, 1};
-const char *const kXfName[X_COUNT] = {"Fourier", "Chebyshev", "Wavelet", "Edge"};
+    "Otsu Object Features", "Inverse-Otsu Object Features", "Gabor Textures", "Gini Coefficient", "Color Histogram"};
+const int kAlgN[A_COUNT] = {32, 32, 72, 28, 24, 6, 48, 12, 20, 5, 28, 34, 34, 7, 1, 20};
+const char *const kXfName[X_COUNT] = {"Fourier", "Chebyshev", "Wavelet", "Edge", "Color", "Hue", "Color Transform"};
 
 static std::string chain_text(const std::vector<int> &chain) {
     std::string s = "()";
@@ -51,15 +51,19 @@ bool parse_group(const std::string &s, int &alg, std::vector<int> &chain) {
     std::vector<int> outer;
     std::string rest = s.substr(p + 1);
     while (rest.size() > 2 && rest[0] == '(' && rest[1] != ')') {
-        size_t q = rest.find(' ');
-        if (q == std::string::npos) return false;
-        std::string t = rest.substr(1, q - 1);
+        // "(Name (" : the longest transform name followed by " ("
         int x = -1;
-        for (int i = 0; i < X_COUNT; i++)
-            if (t == kXfName[i]) x = i;
+        size_t len = 0;
+        for (int i = 0; i < X_COUNT; i++) {
+            const size_t n = strlen(kXfName[i]);
+            if (rest.compare(1, n, kXfName[i]) == 0 && rest.compare(1 + n, 2, " (") == 0 && n > len) {
+                x = i;
+                len = n;
+            }
+        }
         if (x < 0) return false;
         outer.push_back(x);
-        rest = rest.substr(q + 1);
+        rest = rest.substr(len + 2);
     }
     if (rest.compare(0, 2, "()") != 0) return false;
     chain.assign(outer.rbegin(), outer.rend());
@@ -81,8 +85,18 @@ static Plan make_standard(int kind) {
         for (int a : {A_COMB, A_HARALICK, A_MSHIST, A_TAMURA, A_RADON, A_FRACTAL, A_PIXSTATS, A_GINI})
             add_group(p, a, c);
     };
-    if (kind == 1) {  // StdFeatureComputationPlans::addLongFeatures, src/Tasks.cpp:354-400
+    // StdFeatureComputationPlans::addColorFeatures, src/Tasks.cpp:445-459
+    auto colour = [&]() {
+        const std::vector<int> CT = {X_CTCOPY}, H = {X_HUE};
+        add_group(p, A_COLORHIST, R);
+        B(CT); Cg(CT);
+        B(H); Cg(H);
+        B(cat(H, X_FOURIER)); Cg(cat(H, X_FOURIER));
+        B(cat(H, X_CHEBYSHEV)); Cg(cat(H, X_CHEBYSHEV));
+    };
+    if (kind == 1 || kind == 3) {  // addLongFeatures(plan, colour), src/Tasks.cpp:354-400
         A(R); B(R); Cg(R);
+        if (kind == 3) colour();
         B(F); Cg(F);
         B(W); Cg(W);
         B(C); Cg(C);
@@ -117,14 +131,16 @@ static Plan make_standard(int kind) {
             parse_group(n, alg, ch);
             add_group(p, alg, ch);
         }
+        if (kind == 2) colour();  // getFeatureSetColor, src/Tasks.cpp:323-332
     }
     return p;
 }
 
+// kind 0: short (1059), 1: long (2919), 2: short colour (2199), 3: long colour (4059)
 const Plan *standard_plan(int kind) {
-    static wc_plan P[2];
-    static std::once_flag once[2];
-    kind = kind ? 1 : 0;
+    static wc_plan P[4];
+    static std::once_flag once[4];
+    if (kind < 0 || kind > 3) kind = 0;
     std::call_once(once[kind], [kind]() { static_cast<Plan &>(P[kind]) = make_standard(kind); });
     return &P[kind];
 }

@@ -142,6 +142,9 @@ static int prepare_samples(wc_engine *E, const wc_image_desc *imgs, int n, const
     };
     for (int b = 0; b < n; b++) {
         const wc_image_desc &I = imgs[b];
+        if (I.dtype == WC_RGB8 || I.dtype == WC_RGB16)
+            return set_err(WC_ERR_UNSUPPORTED, "image %d: colour images are not preprocessed (the reference's Rotate "
+                           "and Downsample leave or rebuild the colour plane differently from the gray one)", b);
         if (!I.pixels || I.dtype < WC_U8 || I.dtype > WC_F64)
             return set_err(WC_ERR_ARG, "image %d: null pixels or unknown pixel type %d", b, I.dtype);
         Opened o;

@@ -38,6 +38,9 @@ struct FeatureRun {
     char *ws;
     const double *tabs;
     double *feat;
+    const unsigned char *clr;  // HSV colour planes of RGB images, at clr_off[image] bytes
+    const long long *clr_off;
+    const double *fuzzy;  // the fuzzy colour classifier's membership table
 };
 
 void features_init();

@@ -13,10 +13,13 @@ namespace wc {
 // grayscale FeatureAlgorithm singletons, in this project's numbering.
 enum Alg {
     A_CHEBFOURIER = 0, A_CHEB, A_ZERNIKE, A_HARALICK, A_MSHIST, A_TAMURA, A_COMB, A_RADON,
-    A_FRACTAL, A_PIXSTATS, A_EDGEF, A_OBJ, A_INVOBJ, A_GABOR, A_GINI, A_COUNT
+    A_FRACTAL, A_PIXSTATS, A_EDGEF, A_OBJ, A_INVOBJ, A_GABOR, A_GINI, A_COLORHIST, A_COUNT
 };
-// Image transforms (src/ImageTransforms.h): Fourier, Chebyshev, Wavelet, Edge.
-enum Xf { X_FOURIER = 0, X_CHEBYSHEV, X_WAVELET, X_EDGE, X_COUNT };
+// Image transforms (src/ImageTransforms.h): Fourier, Chebyshev, Wavelet, Edge,
+// and for colour images Color (the fuzzy colour index), Hue, and "Color
+// Transform", the name the reference's colour plans use, which its lookup
+// resolves to an EmptyTransform (a copy of the source plane).
+enum Xf { X_FOURIER = 0, X_CHEBYSHEV, X_WAVELET, X_EDGE, X_COLOR, X_HUE, X_CTCOPY, X_COUNT };
 
 extern const char *const kAlgName[A_COUNT];
 extern const int kAlgN[A_COUNT];

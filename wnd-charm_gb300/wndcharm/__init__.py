@@ -144,6 +144,16 @@ class StdFeatureComputationPlans(object):
     def getFeatureSetLong():
         return FeatureComputationPlan._standard(_lib.WC_PLAN_LONG, "Long Feature Set")
 
+    @staticmethod
+    def getFeatureSetColor():
+        """2199 features: the short set plus the colour features (RGB images)."""
+        return FeatureComputationPlan._standard(_lib.WC_PLAN_SHORT_COLOR, "Color Feature Set")
+
+    @staticmethod
+    def getFeatureSetLongColor():
+        """4059 features: the long set with the colour features (RGB images)."""
+        return FeatureComputationPlan._standard(_lib.WC_PLAN_LONG_COLOR, "Long Color Feature Set")
+
 
 class ImageMatrix(object):
     """Grayscale pixel plane (row-major, height x width) with its bit depth."""
@@ -231,11 +241,23 @@ _DT = {np.dtype(np.uint8): _lib.WC_U8, np.dtype(np.uint16): _lib.WC_U16, np.dtyp
        np.dtype(np.float64): _lib.WC_F64}
 
 
+_RGB = {np.dtype(np.uint8): _lib.WC_RGB8, np.dtype(np.uint16): _lib.WC_RGB16}
+
+
 def _as_input(a):
+    """A 2-D grayscale array, or an RGB array (height, width, 3) of uint8 / uint16."""
     a = np.asarray(a)
+    if a.ndim == 3:
+        if a.shape[2] != 3 or a.dtype not in _RGB:
+            raise WndcharmError("an RGB image is a (height, width, 3) uint8 or uint16 array")
+        return np.ascontiguousarray(a)
     if a.dtype not in _DT:
         a = a.astype(np.float64)
     return np.ascontiguousarray(a)
+
+
+def _dtype_code(a):
+    return _RGB[a.dtype] if a.ndim == 3 else _DT[a.dtype]
 
 
 class Engine(object):
@@ -284,7 +306,7 @@ class Engine(object):
         n = len(imgs)
         descs = (_lib.wc_image_desc * n)()
         for i, a in enumerate(imgs):
-            descs[i] = _lib.wc_image_desc(a.ctypes.data, _DT[a.dtype], a.shape[1], a.shape[0], bits, 0)
+            descs[i] = _lib.wc_image_desc(a.ctypes.data, _dtype_code(a), a.shape[1], a.shape[0], bits, 0)
         if out is None:
             out = np.zeros((n, plan.n_features))
         check(lib().wc_extract_batch(self._h, plan.handle, descs, n, out.ctypes.data, 0))
@@ -300,7 +322,7 @@ class Engine(object):
         check(lib().wc_sample_size(ctypes.byref(st), a.shape[1], a.shape[0], int(sample), ctypes.byref(w),
                                    ctypes.byref(h)))
         out = np.zeros((h.value, w.value))
-        d = _lib.wc_image_desc(a.ctypes.data, _DT[a.dtype], a.shape[1], a.shape[0], int(bits), 0)
+        d = _lib.wc_image_desc(a.ctypes.data, _dtype_code(a), a.shape[1], a.shape[0], int(bits), 0)
         check(lib().wc_preprocess(self._h, ctypes.byref(d), ctypes.byref(st), int(sample), out.ctypes.data, out.size,
                                   ctypes.byref(w), ctypes.byref(h), 0))
         return out
@@ -312,7 +334,7 @@ class Engine(object):
         n = len(imgs)
         descs = (_lib.wc_image_desc * n)()
         for i, a in enumerate(imgs):
-            descs[i] = _lib.wc_image_desc(a.ctypes.data, _DT[a.dtype], a.shape[1], a.shape[0], bits, 0)
+            descs[i] = _lib.wc_image_desc(a.ctypes.data, _dtype_code(a), a.shape[1], a.shape[0], bits, 0)
         st = sampling.struct()
         per = check(lib().wc_sampling_count(ctypes.byref(st)))
         if out is None:

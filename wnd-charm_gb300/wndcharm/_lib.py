@@ -10,8 +10,8 @@ HERE = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(HERE, "build", "libwndcharm_gb300.so")
 
 WC_OK = 0
-WC_PLAN_SHORT, WC_PLAN_LONG = 0, 1
-WC_U8, WC_U16, WC_F32, WC_F64 = 0, 1, 2, 3
+WC_PLAN_SHORT, WC_PLAN_LONG, WC_PLAN_SHORT_COLOR, WC_PLAN_LONG_COLOR = 0, 1, 2, 3
+WC_U8, WC_U16, WC_F32, WC_F64, WC_RGB8, WC_RGB16 = 0, 1, 2, 3, 4, 5
 WC_PREC_FP64, WC_PREC_MIXED = 0, 1
 
 D = ctypes.POINTER(ctypes.c_double)

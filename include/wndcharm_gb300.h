@@ -152,13 +152,16 @@ int wc_wnd_classify_images(wc_engine *engine, const double *train, int N, int F,
                            int n_images, int tiles, int max_tile, double *probs, int *pred, double *norm_factors);
 
 /* ---- image files ----
- * Grayscale TIFF as ImageMatrix::LoadTIFF reads it (src/cmatrix.cpp:85-203): one
- * image directory, one sample per pixel, 8 or 16 bits, strips uncompressed, LZW
- * (optionally with the horizontal predictor) or PackBits, either byte order.
- * wc_tiff_info gives the size and bit depth; wc_tiff_read writes the samples
- * row-major (uint8, or uint16 in native byte order) into `pixels` (capacity in
- * bytes).  Colour and multi-directory files give WC_ERR_UNSUPPORTED. */
+ * TIFF as ImageMatrix::LoadTIFF reads it (src/cmatrix.cpp:85-203): one image
+ * directory, one sample per pixel (grayscale) or three interleaved (RGB; hand
+ * them to the engine as WC_RGB8 / WC_RGB16), 8 or 16 bits, strips
+ * uncompressed, LZW (optionally with the horizontal predictor) or PackBits,
+ * either byte order.  wc_tiff_info gives the size and bit depth, wc_tiff_layout
+ * also the samples per pixel; wc_tiff_read writes the samples row-major and
+ * interleaved (uint8, or uint16 in native byte order) into `pixels` (capacity
+ * in bytes).  Other layouts and multi-directory files give WC_ERR_UNSUPPORTED. */
 int wc_tiff_info(const char *path, int *width, int *height, int *bits);
+int wc_tiff_layout(const char *path, int *width, int *height, int *bits, int *samples);
 int wc_tiff_read(const char *path, void *pixels, long long capacity);
 
 /* ---- preprocessing and sampling ----

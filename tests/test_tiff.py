@@ -47,9 +47,10 @@ def _packbits(row):
 
 
 def _write_tiff(path, a, compression=1, predictor=1, order="<"):
-    h, w = a.shape
+    h, w = a.shape[:2]
+    spp = 1 if a.ndim == 2 else a.shape[2]
     bps = 8 * a.dtype.itemsize
-    if predictor == 2:
+    if predictor == 2:  # each sample minus the same sample of the pixel to its left
         d = a.astype(np.int64)
         d[:, 1:] = d[:, 1:] - d[:, :-1]
         a = (d % (1 << bps)).astype(a.dtype)
@@ -57,9 +58,9 @@ def _write_tiff(path, a, compression=1, predictor=1, order="<"):
     strips = [b"".join(rows[y:y + 3]) for y in range(0, h, 3)]  # 3 rows per strip
     if compression == 32773:
         strips = [b"".join(_packbits(r) for r in rows[y:y + 3]) for y in range(0, h, 3)]
-    entries = [(256, 3, 1, w), (257, 3, 1, h), (258, 3, 1, bps), (259, 3, 1, compression), (262, 3, 1, 1),
-               (273, 4, len(strips), None), (277, 3, 1, 1), (278, 3, 1, 3), (279, 4, len(strips), None),
-               (317, 3, 1, predictor)]
+    entries = [(256, 3, 1, w), (257, 3, 1, h), (258, 3, spp, bps), (259, 3, 1, compression),
+               (262, 3, 1, 1 if spp == 1 else 2), (273, 4, len(strips), None), (277, 3, 1, spp), (278, 3, 1, 3),
+               (279, 4, len(strips), None), (284, 3, 1, 1), (317, 3, 1, predictor)]
     head = 8
     data = b"".join(strips)
     offs, o = [], head
@@ -67,17 +68,21 @@ def _write_tiff(path, a, compression=1, predictor=1, order="<"):
         offs.append(o)
         o += len(s_)
     arrays = head + len(data)
-    ifd = arrays + 8 * len(strips)
+    bps_at = arrays + 8 * len(strips)  # BitsPerSample per sample (6 bytes for 3 samples: stored out of line)
+    ifd = bps_at + 8
     out = bytearray((b"II" if order == "<" else b"MM") + struct.pack(order + "HI", 42, ifd))
     out += data
     out += struct.pack(order + "%dI" % len(strips), *offs)
     out += struct.pack(order + "%dI" % len(strips), *[len(s_) for s_ in strips])
+    out += struct.pack(order + "4H", bps, bps, bps, 0)
     out += struct.pack(order + "H", len(entries))
     for tag, typ, cnt, val in entries:
         if tag == 273:
             out += struct.pack(order + "HHII", tag, typ, cnt, arrays)
         elif tag == 279:
             out += struct.pack(order + "HHII", tag, typ, cnt, arrays + 4 * len(strips))
+        elif tag == 258 and spp > 2:
+            out += struct.pack(order + "HHII", tag, typ, cnt, bps_at)
         else:
             out += struct.pack(order + "HHIHH", tag, typ, cnt, val, 0)
     out += struct.pack(order + "I", 0)
@@ -95,6 +100,22 @@ def test_written_tiffs(tmp_path, dtype, compression, predictor, order):
     pix, bits = wndcharm.read_tiff(str(p))
     assert bits == 8 * a.dtype.itemsize
     np.testing.assert_array_equal(pix, a)
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
+@pytest.mark.parametrize("compression,predictor,order", [(1, 1, "<"), (32773, 1, ">"), (1, 2, "<")])
+def test_written_rgb_tiffs(tmp_path, dtype, compression, predictor, order):
+    rng = np.random.default_rng(2)
+    a = rng.integers(0, np.iinfo(dtype).max, size=(9, 14, 3)).astype(dtype)
+    a[3, 1:12] = a[3, 1]  # a run of one colour
+    p = tmp_path / "rgb.tif"
+    _write_tiff(p, a, compression, predictor, order)
+    pix, bits = wndcharm.read_tiff(str(p))
+    assert bits == 8 * a.dtype.itemsize and pix.shape == (9, 14, 3)
+    np.testing.assert_array_equal(pix, a)
+    im = wndcharm.ImageMatrix()
+    assert im.OpenImage(str(p), bounding_rect=(2, 1, 5, 6)) == 1
+    np.testing.assert_array_equal(im.pix_plane, a[1:7, 2:7])
 
 
 def test_tiff_errors(tmp_path):

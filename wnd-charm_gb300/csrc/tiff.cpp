@@ -1,9 +1,11 @@
-// Grayscale TIFF reading for the images wndchrm opens (ImageMatrix::LoadTIFF,
+// TIFF reading for the images wndchrm opens (ImageMatrix::LoadTIFF,
 // src/cmatrix.cpp:85-203, which goes through libtiff): one image directory,
-// one sample per pixel, 8 or 16 bits, strips stored uncompressed, LZW (with or
-// without the horizontal-differencing predictor) or PackBits, either byte
-// order.  Pixel values are the stored samples (LoadTIFF ignores the
-// photometric interpretation).  Written from the TIFF 6.0 specification.
+// one sample per pixel (grayscale) or three interleaved (RGB, which LoadTIFF
+// turns into a gray and an HSV plane), 8 or 16 bits, strips stored
+// uncompressed, LZW (with or without the horizontal-differencing predictor) or
+// PackBits, either byte order.  Pixel values are the stored samples (LoadTIFF
+// ignores the photometric interpretation).  Written from the TIFF 6.0
+// specification.
 #include <cstdint>
 #include <cstdio>
 #include <algorithm>
@@ -20,8 +22,8 @@ int set_err(int code, const char *fmt, ...);
 namespace {
 
 struct TiffImage {
-    int w = 0, h = 0, bits = 0;
-    std::vector<uint8_t> pix;  // row-major, native-order uint8 / uint16
+    int w = 0, h = 0, bits = 0, spp = 1;
+    std::vector<uint8_t> pix;  // row-major, native-order uint8 / uint16, samples interleaved
 };
 
 struct Reader {
@@ -178,13 +180,15 @@ int read_tiff(const char *path, TiffImage &img) {
     if (!r.ok) return wc::set_err(WC_ERR_IO, "'%s': truncated directory", path);
     if (next_ifd != 0) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': more than one image directory", path);
     if (bps != 8 && bps != 16) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u bits per sample (8 or 16 only)", path, bps);
-    if (spp != 1 || planar != 1) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u samples per pixel (grayscale only)", path, spp);
+    if ((spp != 1 && spp != 3) || (spp == 3 && planar != 1))
+        return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u samples per pixel, planar configuration %u (grayscale or "
+                           "interleaved RGB only)", path, spp, planar);
     if (tiled) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': tiled TIFF", path);
     if (comp != 1 && comp != 5 && comp != 32773)
         return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': compression %u (none, LZW or PackBits only)", path, comp);
     if (w == 0 || h == 0 || offs.empty() || offs.size() != counts.size())
         return wc::set_err(WC_ERR_IO, "'%s': missing image size or strips", path);
-    const size_t es = bps / 8, row = (size_t)w * es, total = row * h;
+    const size_t es = bps / 8, row = (size_t)w * spp * es, total = row * h;
     if (rps > h) rps = h;
     std::vector<uint8_t> raw;
     raw.reserve(total);
@@ -207,19 +211,21 @@ int read_tiff(const char *path, TiffImage &img) {
     img.w = (int)w;
     img.h = (int)h;
     img.bits = (int)bps;
+    img.spp = (int)spp;
     img.pix.assign(total, 0);
+    const size_t ns = (size_t)w * spp;  // samples per row; the predictor differences each sample with its left neighbour
     for (size_t y = 0; y < h; y++) {
         const uint8_t *s = raw.data() + y * row;
         if (es == 1) {
             uint8_t *d = img.pix.data() + y * row;
             memcpy(d, s, row);
             if (pred == 2)
-                for (size_t x = 1; x < w; x++) d[x] = (uint8_t)(d[x] + d[x - 1]);
+                for (size_t x = spp; x < ns; x++) d[x] = (uint8_t)(d[x] + d[x - spp]);
         } else {
             uint16_t *d = (uint16_t *)(img.pix.data() + y * row);
-            for (size_t x = 0; x < w; x++) d[x] = r.le ? (uint16_t)(s[2 * x] | (s[2 * x + 1] << 8)) : (uint16_t)((s[2 * x] << 8) | s[2 * x + 1]);
+            for (size_t x = 0; x < ns; x++) d[x] = r.le ? (uint16_t)(s[2 * x] | (s[2 * x + 1] << 8)) : (uint16_t)((s[2 * x] << 8) | s[2 * x + 1]);
             if (pred == 2)
-                for (size_t x = 1; x < w; x++) d[x] = (uint16_t)(d[x] + d[x - 1]);
+                for (size_t x = spp; x < ns; x++) d[x] = (uint16_t)(d[x] + d[x - spp]);
         }
     }
     return WC_OK;
@@ -237,6 +243,18 @@ int wc_tiff_info(const char *path, int *width, int *height, int *bits) {
     *width = img.w;
     *height = img.h;
     *bits = img.bits;
+    return WC_OK;
+}
+
+int wc_tiff_layout(const char *path, int *width, int *height, int *bits, int *samples) {
+    if (!path || !width || !height || !bits || !samples) return wc::set_err(WC_ERR_ARG, "wc_tiff_layout: null argument");
+    TiffImage img;
+    const int r = read_tiff(path, img);
+    if (r) return r;
+    *width = img.w;
+    *height = img.h;
+    *bits = img.bits;
+    *samples = img.spp;
     return WC_OK;
 }
 

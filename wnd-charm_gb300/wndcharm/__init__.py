@@ -166,19 +166,20 @@ class ImageMatrix(object):
 
     def set(self, pixels, bits=None):
         a = np.asarray(pixels)
-        if a.ndim != 2:
-            raise WndcharmError("ImageMatrix needs a 2-D array")
+        if not (a.ndim == 2 or (a.ndim == 3 and a.shape[2] == 3)):
+            raise WndcharmError("ImageMatrix needs a 2-D (grayscale) or (height, width, 3) RGB array")
         self.pix_plane = a
         if bits is not None:
             self.bits = bits
         return self
 
     def OpenImage(self, path, downsample=0, bounding_rect=None, mean=0, stddev=0, engine=None):
-        """Read a grayscale 8/16-bit TIFF as ImageMatrix::OpenImage does
+        """Read an 8/16-bit grayscale or RGB TIFF as ImageMatrix::OpenImage does
         (src/cmatrix.cpp:252-294): crop to bounding_rect = (x, y, w, h), area
         downsampling to `downsample` percent (0 < downsample < 100), and
-        normalisation to `mean` (> 0) and `stddev`, on the GPU.  The pixel
-        plane is the file's integers when nothing is applied, else float64.
+        normalisation to `mean` (> 0) and `stddev`, on the GPU (grayscale
+        only).  The pixel plane is the file's integers ((height, width, 3)
+        for RGB) when nothing is applied, else float64.
         Returns 1 on success, 0 when the file name has no ".tif"/".TIF" (as
         the reference); a rectangle outside the image raises WndcharmError."""
         if ".tif" not in path and ".TIF" not in path:
@@ -476,12 +477,14 @@ def tiles(pixels, tiles_x, tiles_y):
 
 
 def read_tiff(path):
-    """(pixels, bits) of a grayscale 8/16-bit TIFF (uint8 or uint16 array, height x
-    width), read as ImageMatrix::LoadTIFF reads it."""
+    """(pixels, bits) of an 8/16-bit grayscale or RGB TIFF, read as
+    ImageMatrix::LoadTIFF reads it: a uint8 / uint16 array of (height, width),
+    or (height, width, 3) for RGB."""
     L = lib()
-    w, h, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    w, h, b, spp = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     p = path.encode()
-    check(L.wc_tiff_info(p, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b)))
-    out = np.empty((h.value, w.value), dtype=np.uint8 if b.value == 8 else np.uint16)
+    check(L.wc_tiff_layout(p, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b), ctypes.byref(spp)))
+    shape = (h.value, w.value) if spp.value == 1 else (h.value, w.value, spp.value)
+    out = np.empty(shape, dtype=np.uint8 if b.value == 8 else np.uint16)
     check(L.wc_tiff_read(p, out.ctypes.data_as(ctypes.c_void_p), out.nbytes))
     return out, b.value

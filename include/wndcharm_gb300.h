@@ -102,7 +102,10 @@ long long wc_engine_launch_count(const wc_engine *engine);
  * TIME line at verbosity > 4, src/Tasks.cpp:208-253): while on, every
  * transform and feature-family stage is bracketed by CUDA events on the
  * engine's stream (this serialises nothing but adds events); the report lists
- * "stage<TAB>milliseconds<TAB>calls" lines accumulated since the last switch. */
+ * "stage<TAB>milliseconds<TAB>calls<TAB>start<TAB>end" lines accumulated since
+ * the last switch (start / end: the stage's earliest start and latest end in ms
+ * after the batch's first stage; -1 for the host-side stages, "host: ...",
+ * which are wall-clock milliseconds of the calling thread). */
 int wc_engine_profile(wc_engine *engine, int on);
 int wc_engine_profile_report(wc_engine *engine, char *buf, int buflen);
 
@@ -111,10 +114,10 @@ int wc_engine_profile_report(wc_engine *engine, char *buf, int buflen);
  * doubles to out_row (host memory).  Synchronous. */
 int wc_extract(wc_engine *engine, const wc_plan *plan, const void *pixels, int dtype, int width, int height,
                int bits, double *out_row);
-/* Batched form: n images of any sizes, out is n x n_features row-major.  If
- * out_on_device is set, `out` is a device pointer and the call returns once the
- * work is queued on the engine's stream; otherwise it is host memory and the
- * call returns when the rows are written. */
+/* Batched form: n images of any sizes, out is n x n_features row-major, host
+ * memory unless out_on_device is set (then a device pointer on the engine's
+ * GPU).  Either way the call returns when the rows are written: it reads the
+ * kernels' error word at the end, which waits for the engine's stream. */
 int wc_extract_batch(wc_engine *engine, const wc_plan *plan, const wc_image_desc *images, int n, double *out,
                      int out_on_device);
 /* One transform ("Fourier", "Chebyshev", "Wavelet", "Edge"), host buffers; out

@@ -7,6 +7,7 @@
 // is a plane in one HBM arena, each transform runs as one launch over all
 // (source, destination) plane pairs of its depth, and each feature family runs
 // as one launch over all (plane, output column) jobs of the batch.
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -135,6 +136,8 @@ static int out_shape(int xf, int w, int h, int &ow, int &oh) {
 // Runs `plan` over `n` images; `dfeat` receives n x n_features on the device.
 int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, double *dfeat,
               std::vector<Plane> *planes_out) {
+    const auto h0 = std::chrono::steady_clock::now();
+    auto host_ms = [&h0]() { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count(); };
     Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof};
     // ---- nodes: every prefix of every group's transform chain
     std::vector<Node> nodes(1);
@@ -351,6 +354,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
         if (bl.bytes) memcpy(E->hmeta.data() + bl.off, bl.src, bl.bytes);
     char *dm = (char *)E->meta.p;
     char *dw = (char *)E->ws.p;
+    E->prof.host("host: plan the batch", host_ms());
     CK(cudaMemcpyAsync(dm, E->hmeta.data(), meta.used, cudaMemcpyHostToDevice, E->st));
     for (int b = 0; b < n; b++) {
         const wc_image_desc &I = imgs[b];
@@ -446,6 +450,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
         CK(cudaEventRecord(E->join_ev[k], E->lanes[k]));
         CK(cudaStreamWaitEvent(ctx.st, E->join_ev[k], 0));
     }
+    E->prof.host("host: plan and queue the batch", host_ms());
     if (r_early) return r_early;
     if (r) return r;
     CK(cudaGetLastError());
@@ -572,6 +577,7 @@ int wc_engine_create(int device, int precision, wc_engine **out) {
     }
     CK(cudaEventCreateWithFlags(&E->fork_ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&E->early_ev, cudaEventDisableTiming));
+
     *out = E;
     return WC_OK;
 }

@@ -76,6 +76,21 @@ struct Prof {
         if (!on || idx < 0 || idx >= (long long)pending.size()) return;
         cudaEventRecord(pending[idx].b, st);
     }
+    // a host-side stage (wall milliseconds); it has no place on the device timeline (start, end -1)
+    void host(const std::string &name, double t) {
+        if (!on) return;
+        size_t k = 0;
+        while (k < order.size() && order[k] != name) k++;
+        if (k == order.size()) {
+            order.push_back(name);
+            ms.push_back(0);
+            calls.push_back(0);
+            t0.push_back(-1);
+            t1.push_back(-1);
+        }
+        ms[k] += t;
+        calls[k] += 1;
+    }
     void collect() {  // after the stream has been synchronised
         cudaEvent_t ref = pending.empty() ? nullptr : pending[0].a;
         for (auto &m : pending) {

@@ -345,7 +345,7 @@ class Engine(object):
 
     def extract_device(self, plan, descs, n, out_dev_ptr):
         """Device-resident form: descs is a wc_image_desc array with on_device set;
-        features land at out_dev_ptr (device); returns once queued."""
+        features land at out_dev_ptr (device); returns when they are written."""
         check(lib().wc_extract_batch(self._h, plan.handle, descs, n, ctypes.c_void_p(out_dev_ptr), 1))
 
     def transform(self, name, pixels):

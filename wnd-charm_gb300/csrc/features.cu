@@ -314,7 +314,6 @@ int features_prepare(FeatureSetup &fs) {
             o.keys_ws = (long long)(fs.ws_take(2 * n * 8) / 8);
             o.tmp_ws = (long long)(fs.ws_take(n * 8) / 8);
             o.dist_ws = (long long)(fs.ws_take(n * 8) / 8);
-            o.cnt_ws = (long long)(fs.ws_take(256 * 512 * 4) / 8);
             oj.push_back(o);
             inv.push_back({o.src_ws, Q.w, Q.h});
         }

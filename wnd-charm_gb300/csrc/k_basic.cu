@@ -7,7 +7,6 @@
 
 #include "kcommon.cuh"
 #include "kernels.h"
-#include "ksort.cuh"
 
 namespace wc {
 
@@ -186,31 +185,6 @@ void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs
     k_wavelet_y<<<dim3((maxw + 31) / 32, (oy + 7) / 8, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp, tmp_off);
     WC_LAUNCH(c);
     k_wavelet_x<<<dim3((ox + 31) / 32, (oy + 7) / 8, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp, tmp_off);
-}
-
-// ---------------------------------------------------------------- radix sort
-// Each plane's values as orderable 64-bit keys, sorted by one CTA (ksort.cuh).
-#define SORT_THREADS 512
-__global__ void __launch_bounds__(SORT_THREADS) k_plane_sort(const double *__restrict__ arena, const Plane *__restrict__ planes,
-                                                             const int *__restrict__ plane_ids,
-                                                             unsigned long long *__restrict__ keys,
-                                                             unsigned long long *__restrict__ tmp,
-                                                             const long long *__restrict__ key_off,
-                                                             unsigned int *__restrict__ counts) {
-    const Plane P = planes[plane_ids[blockIdx.x]];
-    const long long n = (long long)P.w * P.h;
-    unsigned long long *A = keys + key_off[blockIdx.x], *B = tmp + key_off[blockIdx.x];
-    const double *src = arena + P.off;
-    for (long long i = threadIdx.x; i < n; i += blockDim.x) A[i] = dkey(src[i]);
-    cta_radix_sort_u64(A, B, n, counts + (size_t)blockIdx.x * 256 * SORT_THREADS);
-}
-
-void launch_plane_sort(Ctx &c, const double *arena, const Plane *planes, const int *plane_ids, int n,
-                       unsigned long long *keys, unsigned long long *tmp, const long long *key_off,
-                       unsigned int *counts) {
-    if (n <= 0) return;
-    WC_LAUNCH(c);
-    k_plane_sort<<<n, SORT_THREADS, 0, c.st>>>(arena, planes, plane_ids, keys, tmp, key_off, counts);
 }
 
 // ---------------------------------------------------------------- pixel statistics + Gini

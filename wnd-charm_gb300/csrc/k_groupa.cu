@@ -294,26 +294,38 @@ __global__ void __launch_bounds__(512) k_ob_final(const Plane *__restrict__ plan
         s_gy = mass ? (double)a[2] / mass : 0;
     }
     __syncthreads();
-    // compaction of the roots (L[i] == i) in raster order
+    // compaction of the roots (L[i] == i) in raster order: every warp counts the
+    // roots of its own contiguous segment, a scan over the warps gives each its
+    // first slot, then every warp writes its roots in order
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (long long t0 = 0; t0 < n; t0 += blockDim.x) {
-        const long long i = t0 + threadIdx.x;
-        const int f = (i < n && L[i] == (int)i) ? 1 : 0;
-        const unsigned bal = __ballot_sync(0xffffffffu, f);
-        const int pre = __popc(bal & ((1u << lane) - 1));
-        if (lane == 0) wsum[wid] = __popc(bal);
-        __syncthreads();
-        int off = 0;
-        for (int w = 0; w < wid; w++) off += wsum[w];
-        if (f) roots[s_count + off + pre] = (int)i;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int w = 0; w < nw; w++) tot += wsum[w];
-            s_count += tot;
-        }
-        __syncthreads();
+    const unsigned lt = (1u << lane) - 1;
+    const long long seg = (n + nw - 1) / nw, s0 = min(n, (long long)wid * seg), s1 = min(n, s0 + seg);
+    int mine = 0;
+    for (long long b = s0; b < s1; b += 32) {
+        const long long i = b + lane;
+        mine += __popc(__ballot_sync(0xffffffffu, i < s1 && L[i] == (int)i));
     }
+    if (lane == 0) wsum[wid] = mine;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int w = 0; w < nw; w++) {
+            const int v = wsum[w];
+            wsum[w] = run;
+            run += v;
+        }
+        s_count = run;
+    }
+    __syncthreads();
+    long long slot = wsum[wid];
+    for (long long b = s0; b < s1; b += 32) {
+        const long long i = b + lane;
+        const bool f = i < s1 && L[i] == (int)i;
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        if (f) roots[slot + __popc(bal & lt)] = (int)i;
+        slot += __popc(bal);
+    }
+    __syncthreads();
     const long long count = s_count;
     const double gx = s_gx, gy = s_gy;
     unsigned long long *ka = (unsigned long long *)(ws + O.keys_ws), *kd = ka + count;
@@ -330,9 +342,8 @@ __global__ void __launch_bounds__(512) k_ob_final(const Plane *__restrict__ plan
         kd[k] = dkey(d);
     }
     __syncthreads();
-    unsigned int *cnt = (unsigned int *)(ws + O.cnt_ws);
-    cta_radix_sort_u64(ka, tmp, count, cnt);
-    cta_radix_sort_u64(kd, tmp, count, cnt);
+    cta_sort_u64(ka, tmp, count);
+    cta_sort_u64(kd, tmp, count);
     if (threadIdx.x == 0) {
         double ahist[10] = {0}, dhist[10] = {0};
         double amin = 0, amax = 0, amean = 0, amed = 0, avar = 0, dmin = 0, dmax = 0, dmean = 0, dmed = 0, dvar = 0;
@@ -350,8 +361,8 @@ __global__ void __launch_bounds__(512) k_ob_final(const Plane *__restrict__ plan
             double ss = 0;
             if (amax - amin > 0)
                 for (long long k = 0; k < count; k++) {
-                    const double v = (double)ka[k];
-                    ss = __dadd_rn(ss, pow(v - amean, 2));
+                    const double v = (double)ka[k], e = v - amean;
+                    ss = __dadd_rn(ss, __dmul_rn(e, e));  // pow(e, 2): the correctly rounded square
                     ahist[hist_bin(v, amin, sc, 10)] += 1;
                 }
             avar = (count > 1) ? ss / (count - 1) : ss;
@@ -362,8 +373,8 @@ __global__ void __launch_bounds__(512) k_ob_final(const Plane *__restrict__ plan
             const double dsc = (dmax - dmin > 0) ? 10.0 / double(dmax - dmin) : 0;
             double sdv = 0;
             for (long long k = 0; k < count; k++) {
-                const double v = dkey_inv(kd[k]);
-                sdv = __dadd_rn(sdv, pow(v - dmean, 2));
+                const double v = dkey_inv(kd[k]), e = v - dmean;
+                sdv = __dadd_rn(sdv, __dmul_rn(e, e));
                 dhist[hist_bin(v, dmin, dsc, 10)] += 1;
             }
             dvar = (count > 1) ? sdv / (count - 1) : sdv;

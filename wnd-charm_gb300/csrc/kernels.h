@@ -13,9 +13,6 @@ void launch_plane_stats(Ctx &c, const double *arena, const Plane *planes, int np
 void launch_edge(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh);
 void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
                     double *tmp, const long long *tmp_off);
-void launch_plane_sort(Ctx &c, const double *arena, const Plane *planes, const int *plane_ids, int n,
-                       unsigned long long *keys, unsigned long long *tmp, const long long *key_off,
-                       unsigned int *counts);
 void launch_pixstats(Ctx &c, const Plane *planes, const PlaneStats *stats, const FJob *jobs, int njobs,
                      const int *sort_slot, const unsigned long long *keys, const long long *key_off, double *feat);
 void launch_gini(Ctx &c, const Plane *planes, const FJob *jobs, int njobs, const int *sort_slot,
@@ -99,7 +96,7 @@ void launch_edgefeat(Ctx &c, const double *arena, const Plane *planes, const FJo
 struct OBJob {
     int inverse;  // 1: Inverse-Otsu (source = inverted plane at src_ws)
     int pad_;
-    long long src_ws, lab_ws, area_ws, xm_ws, ym_ws, roots_ws, keys_ws, tmp_ws, dist_ws, cnt_ws;  // doubles offsets
+    long long src_ws, lab_ws, area_ws, xm_ws, ym_ws, roots_ws, keys_ws, tmp_ws, dist_ws;  // doubles offsets
 };
 void launch_objects(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs, int njobs,
                     long long maxpix, const OBJob *oj, double *ws, const Plane *inv_planes, PlaneStats *inv_stats,

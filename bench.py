@@ -171,6 +171,51 @@ def fp64_peak_tflops(dev):
     return 2 * 4096 ** 3 / best / 1e12
 
 
+def run_tiles(args):
+    """The batched uneven-size workload: images with independent sides from
+    {64, 96, ..., 1024} (seed 2), each cut into 4 x 4 tiles as wndchrm samples
+    them, all tiles of a step's images through the long plan in one call
+    (wc_extract_samples: images go to the GPU once, tiles are cut there).
+    Host images in, host rows out, CUDA events around each call."""
+    import torch
+    import wndcharm
+    from wndcharm import synth
+    B = min(args.batch, 32)
+    n = B * (args.steps + args.warmup)
+    sizes = synth.uneven_sizes(n, seed=2)
+    rng = np.random.default_rng(2)
+    imgs = [synth.blob_image(rng, i % 8, w, h, mean=320, sd=80, scale=16, maxval=4095).astype(np.uint16)
+            for i, (w, h) in enumerate(sizes)]
+    plan = wndcharm.StdFeatureComputationPlans.getFeatureSetLong()
+    eng = wndcharm.Engine(0, args.precision)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    s = wndcharm.Sampling(tiles_x=4, tiles_y=4)
+    t = 0.0
+    l0 = 0
+    for k in range(args.warmup + args.steps):
+        batch = imgs[k * B:(k + 1) * B]
+        if k == args.warmup:
+            l0 = eng.launches
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        rows = eng.extract_samples(plan, batch, s)
+        b.record(stream)
+        b.synchronize()
+        if k >= args.warmup:
+            t += a.elapsed_time(b) / 1000.0
+    tiles = 16 * B * args.steps
+    px = sum(w * h for w, h in sizes[args.warmup * B:])
+    print(json.dumps({"metric": "tiles/sec, 2919-feature set, 4x4 ROI tiles of uneven 64..1024 px uint16 images",
+                      "value": tiles / t, "unit": "tiles/s", "images_per_s": B * args.steps / t,
+                      "megapixels_per_s": px / t / 1e6, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1000 * t / args.steps, "higher_is_better": True, "dtype": "f32+f64",
+                      "data": "synthetic", "gpu_launches": eng.launches - l0, "rows_per_step": int(rows.shape[0]),
+                      "config": {"workload": "uneven sides {64..1024} (seed 2), blob+grating, 8 classes, 4x4 tiles "
+                                             "cut on the GPU", "images_per_step": B, "precision_form": args.precision,
+                                 "io": "host images in, host rows out (inside the timed region)"}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -183,11 +228,16 @@ def main():
     ap.add_argument("--per-image", type=int, default=8, help="images timed one per call in the FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP64 comparison forms")
+    ap.add_argument("--workload", default="512", choices=["512", "tiles"],
+                    help="512: the 512x512 images (the headline line); tiles: uneven images "
+                         "(sides 64..1024) cut into 4 x 4 tiles on the GPU, one line of its own")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "tiles":
+        return run_tiles(args)
 
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -37,3 +37,20 @@ def test_uneven_tiles_one_batch():
         fails = compare(got[k], exp, names, rtol=1e-7, atol=1e-9, count_moves=2)
         assert not fails, (k, tl[k].shape, list(fails.items())[:3])
         np.testing.assert_array_equal(eng.extract(plan, [np.ascontiguousarray(tl[k])])[0], got[k])
+
+
+def test_device_tiles_equal_host_tiles():
+    """Tiles cut on the GPU (wc_extract_samples) give the same rows, bit for
+    bit, as the same tiles cut on the host and extracted as images."""
+    import wndcharm
+    from wndcharm import synth
+    rng = np.random.default_rng(21)
+    imgs = [synth.blob_image(rng, i, w, h, mean=320, sd=80, scale=16, maxval=4095).astype(np.uint16)
+            for i, (w, h) in enumerate([(130, 97), (64, 200), (257, 66)])]
+    plan = wndcharm.StdFeatureComputationPlans.getFeatureSetLong()
+    for prec in ("fp64", "mixed"):
+        eng = wndcharm.Engine(0, prec)
+        dev = eng.extract_samples(plan, imgs, wndcharm.Sampling(tiles_x=4, tiles_y=4))
+        host = eng.extract(plan, [t for im in imgs for t in wndcharm.tiles(im, 4, 4)])
+        assert dev.shape == host.shape == (48, 2919)
+        np.testing.assert_array_equal(dev, host)

@@ -610,19 +610,40 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                     failed = true;
                     break;
                 }
-                // initFrancisQRStep
+                // initFrancisQRStep: the first im from iu-2 down to il where the bulge may
+                // start (il at the latest), with its first reflector column fv.  The
+                // candidates are independent, so 32 are evaluated at once, one per lane,
+                // each with the sequential search's own operations; the ballot keeps the
+                // highest one that qualifies.
                 double fv0 = 0, fv1 = 0, fv2 = 0;
-                int im;
-                for (im = iu - 2; im >= il; --im) {
-                    const double Tmm = T_(im, im), r = __dsub_rn(sh0, Tmm), s = __dsub_rn(sh1, Tmm);
-                    fv0 = __dadd_rn(__dsub_rn(__dmul_rn(r, s), sh2) / T_(im + 1, im), T_(im, im + 1));
-                    fv1 = __dsub_rn(__dsub_rn(__dsub_rn(T_(im + 1, im + 1), Tmm), r), s);
-                    fv2 = T_(im + 2, im + 1);
-                    if (im == il) break;
-                    const double lhs = __dmul_rn(T_(im, im - 1), __dadd_rn(fabs(fv1), fabs(fv2)));
-                    const double rhs = __dmul_rn(fv0, __dadd_rn(__dadd_rn(fabs(T_(im - 1, im - 1)), fabs(Tmm)),
-                                                                fabs(T_(im + 1, im + 1))));
-                    if (fabs(lhs) < __dmul_rn(eps, rhs)) break;
+                int im = il;
+                for (int top = iu - 2; top >= il; top -= 32) {
+                    const int cand = top - lane;
+                    bool hit = false;
+                    double a0 = 0, a1 = 0, a2 = 0;
+                    if (cand >= il) {
+                        const double Tmm = T_(cand, cand), r = __dsub_rn(sh0, Tmm), s = __dsub_rn(sh1, Tmm);
+                        a0 = __dadd_rn(__dsub_rn(__dmul_rn(r, s), sh2) / T_(cand + 1, cand), T_(cand, cand + 1));
+                        a1 = __dsub_rn(__dsub_rn(__dsub_rn(T_(cand + 1, cand + 1), Tmm), r), s);
+                        a2 = T_(cand + 2, cand + 1);
+                        if (cand == il) {
+                            hit = true;
+                        } else {
+                            const double lhs = __dmul_rn(T_(cand, cand - 1), __dadd_rn(fabs(a1), fabs(a2)));
+                            const double rhs = __dmul_rn(a0, __dadd_rn(__dadd_rn(fabs(T_(cand - 1, cand - 1)), fabs(Tmm)),
+                                                                       fabs(T_(cand + 1, cand + 1))));
+                            hit = fabs(lhs) < __dmul_rn(eps, rhs);
+                        }
+                    }
+                    const unsigned b = __ballot_sync(0xffffffffu, hit);
+                    if (b) {
+                        const int src = __ffs(b) - 1;
+                        im = top - src;
+                        fv0 = __shfl_sync(0xffffffffu, a0, src);
+                        fv1 = __shfl_sync(0xffffffffu, a1, src);
+                        fv2 = __shfl_sync(0xffffffffu, a2, src);
+                        break;
+                    }
                 }
                 // performFrancisQRStep, restricted to the window
                 for (int k = im; k <= iu - 2; ++k) {

@@ -452,6 +452,9 @@ __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b)
 // the exact FP64 position whenever the estimate lies within 4e-3 of a bin
 // boundary (the estimate's error is below 1e-3 for images up to 2048 px), so
 // every sub-pixel lands in the bin the FP64 form gives it.
+// x == 0.0 (either sign) from the bits, off the FP64 pipe
+__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
 template <typename R>
 __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                         double *__restrict__ feat, int rsize_max) {
@@ -501,7 +504,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 const R fr = (R)__dadd_rn(__dsub_rn(1.0, ra), (double)rl);
                 for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
                     const double pd = p[(long long)(m / 2) * W + n / 2];
-                    if (pd == 0.0) continue;
+                    if (is_zero(pd)) continue;
                     const R pix = (R)pd * (R)0.25;
                     const R pl = rmul(pix, fr);  // no contraction into the sum (the FP64 form's rounding)
                     lo += pl;
@@ -517,14 +520,15 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
         const float csf = (float)cs, snf = (float)sn, rff = (float)rFirst;
         for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
             const double pd = p[(long long)(m / 2) * W + n / 2];
-            if (pd == 0.0) continue;
-            const double xT = -xo - 0.25 + 0.5 * n;              // exact: multiples of 0.25
-            const double yT = -yo - 0.25 + 0.5 * (NY - 1 - m);   // exact
+            if (is_zero(pd)) continue;
+            // sub-pixel centre -xo - 0.25 + 0.5 n (and likewise y): a multiple of 0.25,
+            // exact as k / 4 with an integer k in float and in double alike
+            const int kx = 2 * n - 4 * xo - 1, ky = 2 * (NY - 1 - m) - 4 * yo - 1;
             int rl;
             R pix, pl;
             bool exact = sizeof(R) == 8;
             if (!exact) {
-                const float rif = fmaf((float)yT, snf, fmaf((float)xT, csf, -rff));
+                const float rif = fmaf((float)ky * 0.25f, snf, fmaf((float)kx * 0.25f, csf, -rff));
                 const float fl = floorf(rif), fr = rif - fl;
                 if (fr < 4e-3f || fr > 1.f - 4e-3f) exact = true;
                 else {
@@ -534,6 +538,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 }
             }
             if (exact) {
+                const double xT = (double)kx * 0.25, yT = (double)ky * 0.25;
                 const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
                 rl = (int)ri;
                 const double pdq = pd * 0.25;

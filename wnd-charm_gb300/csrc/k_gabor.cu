@@ -32,6 +32,9 @@ __global__ void k_cfft_lines(R *__restrict__ data, long long js, int nl, int n, 
     C *base = (C *)data + (long long)blockIdx.y * js;
     C *b0 = (C *)fsm, *b1 = b0 + (long long)lpc * n;
     const cplx *tw = (const cplx *)(twd + P.tw_off);
+    // the twiddles in the element type, rounded once per block (after the two line buffers)
+    C *twr = b1 + (long long)lpc * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) twr[i] = {(R)tw[i].x, (R)tw[i].y};
     if (es == 1) {
         for (int i = threadIdx.x; i < lines * n; i += blockDim.x) {
             const int l = i / n, k = i - l * n;
@@ -44,7 +47,7 @@ __global__ void k_cfft_lines(R *__restrict__ data, long long js, int nl, int n, 
         }
     }
     __syncthreads();
-    const C *r = stockham<R>(b0, b1, lines, P, tw) ? b1 : b0;
+    const C *r = stockham<R, R>(b0, b1, lines, P, twr) ? b1 : b0;
     if (es == 1) {
         for (int i = threadIdx.x; i < lines * n; i += blockDim.x) {
             const int l = i / n, k = i - l * n;
@@ -73,12 +76,12 @@ static void cfft2(Ctx &c, double *data, int na, int fh, int fw, const FFTPlan *p
     int lpc = 96 * 1024 / (2 * es * fw);
     lpc = lpc < 1 ? 1 : (lpc > 8 ? 8 : lpc);
     WC_LAUNCH(c);
-    k_cfft_lines<R><<<dim3((fh + lpc - 1) / lpc, na), 256, (size_t)lpc * fw * 2 * es, c.st>>>((R *)data, js, fh, fw, fw, 1,
+    k_cfft_lines<R><<<dim3((fh + lpc - 1) / lpc, na), 256, ((size_t)lpc * 2 + 1) * fw * es, c.st>>>((R *)data, js, fh, fw, fw, 1,
                                                                                             plan_w, tw, lpc);
     int lpc2 = 96 * 1024 / (2 * es * fh);
     lpc2 = lpc2 < 1 ? 1 : (lpc2 > 8 ? 8 : lpc2);
     WC_LAUNCH(c);
-    k_cfft_lines<R><<<dim3((fw + lpc2 - 1) / lpc2, na), 256, (size_t)lpc2 * fh * 2 * es, c.st>>>((R *)data, js, fw, fh, 1, fw,
+    k_cfft_lines<R><<<dim3((fw + lpc2 - 1) / lpc2, na), 256, ((size_t)lpc2 * 2 + 1) * fh * es, c.st>>>((R *)data, js, fw, fh, 1, fw,
                                                                                                plan_h, tw, lpc2);
 }
 

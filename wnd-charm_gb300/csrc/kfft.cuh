@@ -2,7 +2,8 @@
 // length; radix-p stages with host-computed FP64 twiddles
 // tw[k] = exp(-2 pi i k / n)).  Shared by the Fourier transform node and the
 // Gabor FFT convolution; templated on the element type (FP64 form, and FP32
-// for the mixed form's Gabor filtering, which rounds the twiddles on load).
+// for the mixed form's Gabor filtering) and on the twiddles' type (FP64, or
+// the FP64 twiddles rounded to FP32 once, in shared memory).
 #pragma once
 #include "kernels.h"
 
@@ -21,16 +22,16 @@ template <typename R>
 __device__ __forceinline__ cpx<R> cadd(cpx<R> a, cpx<R> b) {
     return {a.x + b.x, a.y + b.y};
 }
-template <typename R>
-__device__ __forceinline__ cpx<R> twid(const cplx *tw, long long i) {
-    const cplx t = tw[i];
+template <typename R, typename T>
+__device__ __forceinline__ cpx<R> twid(const cpx<T> *tw, long long i) {
+    const cpx<T> t = tw[i];
     return {(R)t.x, (R)t.y};
 }
 
 // One Stockham pass over `lines` lines of length n held in src (line-major),
 // writing dst.  Ns = product of the radices already applied.
-template <typename R>
-static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines, int n, int p, int Ns, const cplx *tw) {
+template <typename R, typename T>
+static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines, int n, int p, int Ns, const cpx<T> *tw) {
     typedef cpx<R> C;
     const int m = n / p;
     const int total = lines * m;
@@ -48,13 +49,13 @@ static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines,
             for (int r = 0; r < 8; r++) {
                 if (r < p) {
                     C a = s[j + r * m];
-                    if (r > 0 && k > 0) a = cmul(a, twid<R>(tw, (long long)r * k * twstep_k % n));
+                    if (r > 0 && k > 0) a = cmul(a, twid<R, T>(tw, (long long)r * k * twstep_k % n));
                     v[r] = a;
                 }
             }
             for (int q = 0; q < p; q++) {
                 C acc = v[0];
-                for (int r = 1; r < p; r++) acc = cadd(acc, cmul(v[r], twid<R>(tw, (long long)((r * q) % p) * twstep_q)));
+                for (int r = 1; r < p; r++) acc = cadd(acc, cmul(v[r], twid<R, T>(tw, (long long)((r * q) % p) * twstep_q)));
                 d[obase + q * Ns] = acc;
             }
         } else {
@@ -62,8 +63,8 @@ static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines,
                 C acc = s[j];
                 for (int r = 1; r < p; r++) {
                     C a = s[j + r * m];
-                    if (k > 0) a = cmul(a, twid<R>(tw, (long long)r * k * twstep_k % n));
-                    acc = cadd(acc, cmul(a, twid<R>(tw, (long long)((r * q) % p) * twstep_q)));
+                    if (k > 0) a = cmul(a, twid<R, T>(tw, (long long)r * k * twstep_k % n));
+                    acc = cadd(acc, cmul(a, twid<R, T>(tw, (long long)((r * q) % p) * twstep_q)));
                 }
                 d[obase + q * Ns] = acc;
             }
@@ -72,8 +73,8 @@ static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines,
 }
 
 // returns which buffer (0 or 1) holds the result
-template <typename R>
-static __device__ int stockham(cpx<R> *b0, cpx<R> *b1, int lines, const FFTPlan &P, const cplx *tw) {
+template <typename R, typename T>
+static __device__ int stockham(cpx<R> *b0, cpx<R> *b1, int lines, const FFTPlan &P, const cpx<T> *tw) {
     cpx<R> *src = b0, *dst = b1;
     int Ns = 1, cur = 0;
     for (int s = 0; s < P.nstages; s++) {

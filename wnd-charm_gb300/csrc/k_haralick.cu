@@ -152,14 +152,16 @@ __global__ void __launch_bounds__(256) k_har_stats(const FJob *__restrict__ jobs
     for (long long q = threadIdx.x; q < (long long)Ng * Ng; q += blockDim.x) {
         const int i = (int)(q / Ng), j = (int)(q - (long long)i * Ng);
         const double p = P[q];
+        const double pp = px[i] * py[j];
+        const double lpp = log10(pp + EPS);
+        hxy2 -= pp * lpp / l2;
+        if (p == 0.0) continue;  // every other term is then a zero: the sums stay as they are
         f1 += p * p;
         tmp3 += i * j * p;
         mean4 += i * p;
         f5 += p / (1 + (i - j) * (i - j));
         e9 += p * log10(p + EPS) / l2;
-        const double pp = px[i] * py[j];
-        hxy1 -= p * log10(pp + EPS) / l2;
-        hxy2 -= pp * log10(pp + EPS) / l2;
+        hxy1 -= p * lpp / l2;
     }
     f1 = block_sum(f1, sh);
     tmp3 = block_sum(tmp3, sh);
@@ -657,21 +659,22 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                             if (first && k > il) T_(k, k - 1) = -T_(k, k - 1);
                             else if (!first) T_(k, k - 1) = beta;
                         }
+                        const double te0 = __dmul_rn(tau, ess[0]), te1 = __dmul_rn(tau, ess[1]);  // per column alike
                         for (int cc = k + tid; cc <= iu; cc += GS) {  // left: rows k..k+2
                             const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
                             if (FUSED) {
                                 const double t = __dadd_rn(__fma_rn(ess[1], a2, __dmul_rn(ess[0], a1)), a0);
                                 T_(k, cc) = __fma_rn(-tau, t, a0);
-                                T_(k + 1, cc) = __fma_rn(-__dmul_rn(tau, ess[0]), t, a1);
-                                T_(k + 2, cc) = __fma_rn(-__dmul_rn(tau, ess[1]), t, a2);
+                                T_(k + 1, cc) = __fma_rn(-te0, t, a1);
+                                T_(k + 2, cc) = __fma_rn(-te1, t, a2);
                                 continue;
                             }
                             double t = plus_zero(__dmul_rn(ess[0], a1));
                             t = __dadd_rn(t, __dmul_rn(ess[1], a2));
                             t = __dadd_rn(t, a0);
                             T_(k, cc) = __dsub_rn(a0, __dmul_rn(tau, t));
-                            T_(k + 1, cc) = __dsub_rn(a1, __dmul_rn(__dmul_rn(tau, ess[0]), t));
-                            T_(k + 2, cc) = __dsub_rn(a2, __dmul_rn(__dmul_rn(tau, ess[1]), t));
+                            T_(k + 1, cc) = __dsub_rn(a1, __dmul_rn(te0, t));
+                            T_(k + 2, cc) = __dsub_rn(a2, __dmul_rn(te1, t));
                         }
                         QR_SYNC();
                         const int rend = min(iu, k + 3);
@@ -701,12 +704,13 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                     QR_SYNC();
                     if (beta != 0) {
                         if (tid == 0) T_(iu - 1, iu - 2) = beta;
+                        const double te0 = __dmul_rn(tau, ess[0]);
                         for (int cc = iu - 1 + tid; cc <= iu; cc += GS) {
                             const double a0 = T_(iu - 1, cc), a1 = T_(iu, cc);
                             double t = __dadd_rn(__dmul_rn(ess[0], a1), 0.0);
                             t = __dadd_rn(t, a0);
                             T_(iu - 1, cc) = __dsub_rn(a0, __dmul_rn(tau, t));
-                            T_(iu, cc) = __dsub_rn(a1, __dmul_rn(__dmul_rn(tau, ess[0]), t));
+                            T_(iu, cc) = __dsub_rn(a1, __dmul_rn(te0, t));
                         }
                         QR_SYNC();
                         for (int rr = il + tid; rr <= iu; rr += GS) {

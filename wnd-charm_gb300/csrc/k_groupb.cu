@@ -15,6 +15,7 @@
 #include <cmath>
 
 #include "kcommon.cuh"
+#include "kdf32.cuh"
 #include "kernels.h"
 
 namespace wc {
@@ -67,7 +68,7 @@ __global__ void k_zern_moments(const double *__restrict__ arena, const Plane *__
 #define ZCHUNK 2048
 // second pass: per (chunk of pixels, half, job): per-CTA partial AR/AI.
 // HALF 0 covers n = 0..10, HALF 1 covers n = 11..15 (36 (n, m) pairs each).
-// (FP64 form, the reference's operations; the mixed form uses k_zern_cmom.)
+// (FP64 form, the reference's operations; the mixed form uses k_zern_cmom_df.)
 template <int HALF>
 __global__ void __launch_bounds__(256) k_zern_accum(const double *__restrict__ arena, const Plane *__restrict__ planes,
                                                     const FJob *__restrict__ jobs, const double *__restrict__ mom,
@@ -170,57 +171,75 @@ __global__ void k_zern_finish(const FJob *__restrict__ jobs, const double *__res
 // the first harmonic, zernike.cpp:287-296) and R_nm(r) = sum_s c_nms r^(n-2s),
 //   R_nm e^{-i(m+1) phi} = sum_s c_nms (r^2)^j zbar^(m+1) / r,   j = (n-m)/2 - s,
 // zbar = x - i y; so A_nm = (n+1)/pi sum_s c_nms M(j, m+1) with the 72 complex
-// moments M(j, m') = sum f (r^2)^j zbar^m' / r (FP64, about half the FP64
-// instructions per pixel of the q-recursion), and the exact integer
+// moments M(j, m') = sum f (r^2)^j zbar^m' / r, and the exact integer
 // coefficients c_nms = (-1)^s (n-s)! / (s! ((n+m)/2-s)! ((n-m)/2-s)!) applied once
-// per job in FP64.  HALF 0: m' = 1..5, HALF 1: m' = 6..16 (36 moments each,
-// m' ascending, j = 0..(16-m')/2 ascending).
+// per job in FP64 (k_zern_finish_cmom).  HALF 0: m' = 1..5, HALF 1: m' = 6..16
+// (36 moments each, m' ascending, j = 0..(16-m')/2 ascending).
+// The moments are summed in pairs of floats (about 48 bits, on the FP32
+// pipe instead of the FP64 one).  Whether a pixel lies
+// in the unit disc is decided as the FP64 kernel decides it: the pair estimate
+// of r^2 decides away from 1 and 0, the FP64 test within 1e-6 of them.  Chunks
+// of ZCHUNK_DF pixels per block; the block's sums are reduced in pairs within
+// each warp and in FP64 across the warps.
+#define ZCHUNK_DF 16384
 template <int HALF>
-__global__ void __launch_bounds__(256) k_zern_cmom(const double *__restrict__ arena, const Plane *__restrict__ planes,
-                                                   const FJob *__restrict__ jobs, const double *__restrict__ mom,
-                                                   double *__restrict__ part, int nchunk) {
+__global__ void __launch_bounds__(256) k_zern_cmom_df(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                      const FJob *__restrict__ jobs, const double *__restrict__ mom,
+                                                      double *__restrict__ part, int nchunk) {
     constexpr int M0 = HALF ? 6 : 1, M1 = HALF ? 16 : 5, JMAX = (16 - M0) / 2;
     __shared__ double red[8][72];
     const FJob J = jobs[blockIdx.z];
     const Plane P = planes[J.plane];
     const long long npix = (long long)P.w * P.h;
-    const long long c0 = (long long)blockIdx.x * ZCHUNK;
-    double acc[72];
+    const long long c0 = (long long)blockIdx.x * ZCHUNK_DF;
+    df acc[72];
 #pragma unroll
-    for (int q = 0; q < 72; q++) acc[q] = 0.0;
+    for (int q = 0; q < 72; q++) acc[q] = {0.f, 0.f};
     if (c0 < npix) {
         const double sum = mom[3 * blockIdx.z], cx = mom[3 * blockIdx.z + 1], cy = mom[3 * blockIdx.z + 2];
         const double inv_rad = 1.0 / (double)(P.w < P.h ? P.w : P.h), inv_sum = 1.0 / sum;
+        const df cxd = df_from_double(cx), cyd = df_from_double(cy), ird = df_from_double(inv_rad),
+                 isd = df_from_double(inv_sum);
         const double *p = arena + P.off;
-        const long long c1 = min(npix, c0 + ZCHUNK);
+        const long long c1 = min(npix, c0 + ZCHUNK_DF);
         for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
             const long long yy = i / P.w, xx = i - yy * P.w;
-            const double x = __dsub_rn((double)(xx + 1), cx) * inv_rad, y = __dsub_rn((double)(yy + 1), cy) * inv_rad;
-            const double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), r = sqrt(r2);
-            if (r < DBL_EPSILON || r > 1.0) continue;
-            double q[JMAX + 1];
-            q[0] = p[i] * inv_sum / r;
+            const df x = df_mul(df_sub({(float)(xx + 1), 0.f}, cxd), ird);
+            const df y = df_mul(df_sub({(float)(yy + 1), 0.f}, cyd), ird);
+            const df r2 = df_add(df_mul(x, x), df_mul(y, y));
+            bool in;
+            if (fabsf(r2.hi - 1.f) < 1e-6f || r2.hi < 1e-20f) {
+                const double xe = __dsub_rn((double)(xx + 1), cx) * inv_rad, ye = __dsub_rn((double)(yy + 1), cy) * inv_rad;
+                const double r = sqrt(__dadd_rn(__dmul_rn(xe, xe), __dmul_rn(ye, ye)));
+                in = !(r < DBL_EPSILON || r > 1.0);
+            } else {
+                in = r2.hi < 1.f;
+            }
+            if (!in) continue;
+            const df r = df_sqrt(r2);
+            df q[JMAX + 1];
+            q[0] = df_div(df_mul(df_from_double(p[i]), isd), r);
 #pragma unroll
-            for (int j = 1; j <= JMAX; j++) q[j] = q[j - 1] * r2;
-            double zr = x, zi = -y;  // zbar^1
+            for (int j = 1; j <= JMAX; j++) q[j] = df_mul(q[j - 1], r2);
+            df zr = x, zi = df_neg(y);  // zbar^1
 #pragma unroll
             for (int mp = 2; mp <= M0; mp++) {
-                const double t = zr * x + zi * y;  // (zr + i zi)(x - i y)
-                zi = zi * x - zr * y;
+                const df t = df_add(df_mul(zr, x), df_mul(zi, y));
+                zi = df_sub(df_mul(zi, x), df_mul(zr, y));
                 zr = t;
             }
             int slot = 0;
 #pragma unroll
             for (int mp = M0; mp <= M1; mp++) {
                 if (mp > M0) {
-                    const double t = zr * x + zi * y;
-                    zi = zi * x - zr * y;
+                    const df t = df_add(df_mul(zr, x), df_mul(zi, y));
+                    zi = df_sub(df_mul(zi, x), df_mul(zr, y));
                     zr = t;
                 }
 #pragma unroll
                 for (int j = 0; j <= (16 - mp) / 2; j++) {
-                    acc[2 * slot] += q[j] * zr;
-                    acc[2 * slot + 1] += q[j] * zi;
+                    acc[2 * slot] = df_add(acc[2 * slot], df_mul(q[j], zr));
+                    acc[2 * slot + 1] = df_add(acc[2 * slot + 1], df_mul(q[j], zi));
                     slot++;
                 }
             }
@@ -229,8 +248,10 @@ __global__ void __launch_bounds__(256) k_zern_cmom(const double *__restrict__ ar
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int qq = 0; qq < 72; qq++) {
-        double v = warp_sum(acc[qq]);
-        if (lane == 0) red[wid][qq] = v;
+        df v = acc[qq];
+        for (int o = 16; o > 0; o >>= 1)
+            v = df_add(v, {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+        if (lane == 0) red[wid][qq] = df_to_double(v);
     }
     __syncthreads();
     if (threadIdx.x < 72) {
@@ -293,12 +314,13 @@ void launch_zernike(Ctx &c, const double *arena, const Plane *planes, const FJob
     WC_LAUNCH(c);
     k_zern_moments<<<njobs, 512, 0, c.st>>>(arena, planes, jobs, mom);
     if (c.prec == WC_PREC_MIXED) {
+        const int nch = (int)((maxpix + ZCHUNK_DF - 1) / ZCHUNK_DF);
         WC_LAUNCH(c);
-        k_zern_cmom<0><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+        k_zern_cmom_df<0><<<dim3(nch, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nch);
         WC_LAUNCH(c);
-        k_zern_cmom<1><<<dim3(nchunk, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nchunk);
+        k_zern_cmom_df<1><<<dim3(nch, 1, njobs), 256, 0, c.st>>>(arena, planes, jobs, mom, part, nch);
         WC_LAUNCH(c);
-        k_zern_finish_cmom<<<njobs, 160, 0, c.st>>>(jobs, part, nchunk, feat);
+        k_zern_finish_cmom<<<njobs, 160, 0, c.st>>>(jobs, part, nch, feat);
         return;
     }
     WC_LAUNCH(c);

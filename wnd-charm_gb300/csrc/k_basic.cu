@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "kcommon.cuh"
+#include "kdf32.cuh"
 #include "kernels.h"
 
 namespace wc {
@@ -452,6 +453,12 @@ __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b)
 // the exact FP64 position whenever the estimate lies within 4e-3 of a bin
 // boundary (the estimate's error is below 1e-3 for images up to 2048 px), so
 // every sub-pixel lands in the bin the FP64 form gives it.
+// a pixel in the projection's type; to float from the bits (the conversion
+// instruction issues on the FP64 pipe)
+template <typename R> __device__ __forceinline__ R to_r(double x);
+template <> __device__ __forceinline__ float to_r<float>(double x) { return f32_of(x); }
+template <> __device__ __forceinline__ double to_r<double>(double x) { return x; }
+
 // x == 0.0 (either sign) from the bits, off the FP64 pipe
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
@@ -505,7 +512,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 for (; n >= 0 && n < NX && m >= 0 && m < NY; n += dn, m += dm) {
                     const double pd = p[(long long)(m / 2) * W + n / 2];
                     if (is_zero(pd)) continue;
-                    const R pix = (R)pd * (R)0.25;
+                    const R pix = to_r<R>(pd) * (R)0.25;
                     const R pl = rmul(pix, fr);  // no contraction into the sum (the FP64 form's rounding)
                     lo += pl;
                     hi += pix - pl;
@@ -533,7 +540,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 if (fr < 4e-3f || fr > 1.f - 4e-3f) exact = true;
                 else {
                     rl = (int)fl;
-                    pix = (R)pd * (R)0.25;
+                    pix = to_r<R>(pd) * (R)0.25;
                     pl = rmul(pix, (R)(1.f - fr));
                 }
             }
@@ -542,7 +549,7 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
                 rl = (int)ri;
                 const double pdq = pd * 0.25;
-                pix = (R)pdq;
+                pix = to_r<R>(pdq);
                 pl = (R)__dmul_rn(pdq, __dadd_rn(__dsub_rn(1.0, ri), (double)rl));
             }
             if (rl != cur) {

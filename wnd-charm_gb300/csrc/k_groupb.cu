@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256) k_zern_cmom_df(const double *__restrict__
             if (!in) continue;
             const df r = df_sqrt(r2);
             df q[JMAX + 1];
-            q[0] = df_div(df_mul(df_from_double(p[i]), isd), r);
+            q[0] = df_div(df_mul(df_split(p[i]), isd), r);
 #pragma unroll
             for (int j = 1; j <= JMAX; j++) q[j] = df_mul(q[j - 1], r2);
             df zr = x, zi = df_neg(y);  // zbar^1

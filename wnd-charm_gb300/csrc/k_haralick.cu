@@ -14,6 +14,7 @@
 #include <cmath>
 
 #include "kcommon.cuh"
+#include "kdf32.cuh"
 #include "kernels.h"
 
 namespace wc {
@@ -758,6 +759,319 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
 #undef T_
 }
 
+// The mixed form's real Schur iteration: the same algorithm, windows and
+// decisions as har_schur, with the matrix held and updated in pairs of floats
+// (about 48 significant bits, on the FP32 pipe instead of the FP64 one).  The
+// deflation threshold is eps = 2^-46 (a few units of the pairs' rounding, as
+// Eigen's epsilon is for doubles), relative to the two diagonal entries as
+// there, or eps times the matrix's norm: clusters of eigenvalues near 1e-18
+// (Q is close to singular) cannot reach the relative threshold within float's
+// exponent range, and without the normwise one ran to the iteration limit.
+// The choices between candidates compare the leading floats.  The Hessenberg matrix arrives in FP64 and is converted
+// in place on the integer pipe (a double and a pair are both 8 bytes; zeros are
+// zero bits in both).
+// The vector is first scaled by a power of two that brings its largest entry
+// into [0.5, 1): exact, leaves ess and tau unchanged and beta scaled back, and
+// keeps the squares within float's exponent range (FP64's wider range needs no
+// such step; unscaled, bulges of 1e-20 underflowed to 0 / 0).
+__device__ __forceinline__ void hh_scale(float m, float &down, float &up) {
+    const int eb = (int)((__float_as_uint(m) >> 23) & 0xff);  // m > 0, eb <= 252 for these matrices
+    down = __uint_as_float((unsigned)(253 - min(eb, 252)) << 23);
+    up = __uint_as_float((unsigned)(min(eb, 252) + 1) << 23);
+}
+__device__ __forceinline__ void hh_make3_df(const df v0, const df v1, const df v2, int lane, df &e0, df &e1, df &tau,
+                                            df &beta) {
+    const float m = fmaxf(fabsf(v0.hi), fmaxf(fabsf(v1.hi), fabsf(v2.hi)));
+    tau = {0.f, 0.f};
+    beta = v0;
+    e0 = e1 = {0.f, 0.f};
+    if (m == 0.f) return;
+    float down, up;
+    hh_scale(m, down, up);
+    const df w0 = df_scale(v0, down), w1 = df_scale(v1, down), w2 = df_scale(v2, down);
+    const df wl = lane == 2 ? w2 : w1;
+    const df sq = df_mul(wl, wl);
+    const df tail = df_add(df_shfl(sq, 1), df_shfl(sq, 2));
+    if (tail.hi == 0.f) return;
+    df bb = df_sqrt(df_fma(w0, w0, tail));
+    if (w0.hi >= 0.f) bb = df_neg(bb);
+    const df den = df_sub(w0, bb);
+    const df num = lane == 0 ? w1 : (lane == 1 ? w2 : df_sub(bb, w0));
+    const df q = df_div(num, lane < 2 ? den : bb);
+    e0 = df_shfl(q, 0);
+    e1 = df_shfl(q, 1);
+    tau = df_shfl(q, 2);
+    beta = df_scale(bb, up);
+}
+
+template <int NW>
+__device__ void har_schur_df(df *__restrict__ A, const int n, float *__restrict__ rowsum, double *__restrict__ res,
+                             const int tid) {
+    const int lane = tid & 31;
+    constexpr int GS = 32 * NW;
+    if (n < 3) {
+        if (tid == 0) res[13] = 0.0;
+        return;
+    }
+#define T_(r, c) A[(long long)(r) * n + (c)]
+    for (int r = 0; r < n; r++)
+        for (int c = (r > 0 ? r - 1 : 0) + tid; c < n; c += GS) {
+            T_(r, c) = df_split(*(const double *)&T_(r, c));
+        }
+    QR_SYNC();
+    for (int j = tid; j < n; j += GS) {
+        float s = 0.f;
+        for (int c = (j > 0 ? j - 1 : 0); c < n; c++) s = __fadd_rn(s, fabsf(T_(j, c).hi));
+        rowsum[j] = s;
+    }
+    QR_SYNC();
+    float norm = 0.f;
+    for (int j = 0; j < n; j++) norm = __fadd_rn(norm, rowsum[j]);
+    const float eps = 0x1p-46f, nthr = __fmul_rn(eps, norm);
+    const int maxIter = 40 * n;
+    int iu = n - 1, iter = 0, totalIter = 0;
+    df exshift = {0.f, 0.f};
+    bool failed = false;
+    const df zero = {0.f, 0.f};
+    if (norm != 0.f) {
+        while (iu >= 0) {
+            int il = 0;
+            for (int base = iu; base > 0; base -= 32) {
+                const int r = base - lane;
+                bool hit = false;
+                if (r > 0) {
+                    float sm = __fadd_rn(fabsf(T_(r - 1, r - 1).hi), fabsf(T_(r, r).hi));
+                    if (sm == 0.f) sm = norm;
+                    const float sub = fabsf(T_(r, r - 1).hi);
+                    hit = sub < __fmul_rn(eps, sm) || sub < nthr;
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, hit);
+                if (b) {
+                    il = base - (__ffs(b) - 1);
+                    break;
+                }
+            }
+            if (il == iu) {
+                QR_SYNC();
+                if (tid == 0) {
+                    T_(iu, iu) = df_add(T_(iu, iu), exshift);
+                    if (iu > 0) T_(iu, iu - 1) = zero;
+                }
+                QR_SYNC();
+                iu--;
+                iter = 0;
+            } else if (il == iu - 1) {
+                const df p = df_scale(df_sub(T_(iu - 1, iu - 1), T_(iu, iu)), 0.5f);
+                const df q = df_fma(p, p, df_mul(T_(iu, iu - 1), T_(iu - 1, iu)));
+                QR_SYNC();
+                if (tid == 0) {
+                    T_(iu, iu) = df_add(T_(iu, iu), exshift);
+                    T_(iu - 1, iu - 1) = df_add(T_(iu - 1, iu - 1), exshift);
+                }
+                QR_SYNC();
+                if (q.hi >= 0.f) {
+                    const df z = q.hi == 0.f ? zero : df_sqrt(q);
+                    const df gp = (p.hi >= 0.f) ? df_add(p, z) : df_sub(p, z), gq = T_(iu, iu - 1);
+                    df c, s;
+                    const df one = {1.f, 0.f};
+                    if (gq.hi == 0.f) { c = {gp.hi < 0.f ? -1.f : 1.f, 0.f}; s = zero; }
+                    else if (gp.hi == 0.f) { c = zero; s = {gq.hi < 0.f ? 1.f : -1.f, 0.f}; }
+                    else if (df_lt(df_abs(gq), df_abs(gp))) {
+                        const df t = df_div(gq, gp);
+                        df u = df_sqrt(df_fma(t, t, one));
+                        if (gp.hi < 0.f) u = df_neg(u);
+                        c = df_div(one, u);
+                        s = df_neg(df_mul(t, c));
+                    } else {
+                        const df t = df_div(gp, gq);
+                        df u = df_sqrt(df_fma(t, t, one));
+                        if (gq.hi < 0.f) u = df_neg(u);
+                        s = df_neg(df_div(one, u));
+                        c = df_neg(df_mul(t, s));
+                    }
+                    QR_SYNC();
+                    if (tid == 0) {
+                        for (int col = iu - 1; col <= iu; col++) {
+                            const df xi = T_(iu - 1, col), yi = T_(iu, col);
+                            T_(iu - 1, col) = df_fma(c, xi, df_mul(df_neg(s), yi));
+                            T_(iu, col) = df_fma(s, xi, df_mul(c, yi));
+                        }
+                        for (int row = iu - 1; row <= iu; row++) {
+                            const df xi = T_(row, iu - 1), yi = T_(row, iu);
+                            T_(row, iu - 1) = df_fma(c, xi, df_mul(df_neg(s), yi));
+                            T_(row, iu) = df_fma(s, xi, df_mul(c, yi));
+                        }
+                        T_(iu, iu - 1) = zero;
+                    }
+                }
+                if (tid == 0 && iu > 1) T_(iu - 1, iu - 2) = zero;
+                QR_SYNC();
+                iu -= 2;
+                iter = 0;
+            } else {
+                df sh0 = T_(iu, iu), sh1 = T_(iu - 1, iu - 1), sh2 = df_mul(T_(iu, iu - 1), T_(iu - 1, iu));
+                if (iter == 10) {
+                    exshift = df_add(exshift, sh0);
+                    QR_SYNC();
+                    for (int i = tid; i <= iu; i += GS) T_(i, i) = df_sub(T_(i, i), sh0);
+                    QR_SYNC();
+                    const df s = df_add(df_abs(T_(iu, iu - 1)), df_abs(T_(iu - 1, iu - 2)));
+                    sh0 = df_mul(s, {0.75f, 0.f});
+                    sh1 = sh0;
+                    sh2 = df_mul(df_mul(s, {-0.4375f, 0.f}), s);
+                }
+                if (iter == 30) {
+                    df s = df_scale(df_sub(sh1, sh0), 0.5f);
+                    s = df_fma(s, s, sh2);
+                    if (s.hi > 0.f) {
+                        s = df_sqrt(s);
+                        if (df_lt(sh1, sh0)) s = df_neg(s);
+                        s = df_add(s, df_scale(df_sub(sh1, sh0), 0.5f));
+                        s = df_sub(sh0, df_div(sh2, s));
+                        exshift = df_add(exshift, s);
+                        QR_SYNC();
+                        for (int i = tid; i <= iu; i += GS) T_(i, i) = df_sub(T_(i, i), s);
+                        QR_SYNC();
+                        sh0 = sh1 = sh2 = df{0.964f, 0.f};
+                    }
+                }
+                iter++;
+                totalIter++;
+                if (totalIter > maxIter) {
+                    failed = true;
+                    break;
+                }
+                df fv0 = zero, fv1 = zero, fv2 = zero;
+                int im = il;
+                for (int top = iu - 2; top >= il; top -= 32) {
+                    const int cand = top - lane;
+                    bool hit = false;
+                    df a0 = zero, a1 = zero, a2 = zero;
+                    if (cand >= il) {
+                        const df Tmm = T_(cand, cand), r = df_sub(sh0, Tmm), s = df_sub(sh1, Tmm);
+                        a0 = df_add(df_div(df_sub(df_mul(r, s), sh2), T_(cand + 1, cand)), T_(cand, cand + 1));
+                        a1 = df_sub(df_sub(df_sub(T_(cand + 1, cand + 1), Tmm), r), s);
+                        a2 = T_(cand + 2, cand + 1);
+                        if (cand == il) {
+                            hit = true;
+                        } else {
+                            const float lhs = __fmul_rn(T_(cand, cand - 1).hi, __fadd_rn(fabsf(a1.hi), fabsf(a2.hi)));
+                            const float rhs = __fmul_rn(a0.hi, __fadd_rn(__fadd_rn(fabsf(T_(cand - 1, cand - 1).hi), fabsf(Tmm.hi)),
+                                                                         fabsf(T_(cand + 1, cand + 1).hi)));
+                            hit = fabsf(lhs) < __fmul_rn(eps, rhs);
+                        }
+                    }
+                    const unsigned b = __ballot_sync(0xffffffffu, hit);
+                    if (b) {
+                        const int src = __ffs(b) - 1;
+                        im = top - src;
+                        fv0 = df_shfl(a0, src);
+                        fv1 = df_shfl(a1, src);
+                        fv2 = df_shfl(a2, src);
+                        break;
+                    }
+                }
+                for (int k = im; k <= iu - 2; ++k) {
+                    const bool first = (k == im);
+                    df e0, e1, tau, beta;
+                    if (first) hh_make3_df(fv0, fv1, fv2, lane, e0, e1, tau, beta);
+                    else hh_make3_df(T_(k, k - 1), T_(k + 1, k - 1), T_(k + 2, k - 1), lane, e0, e1, tau, beta);
+                    QR_SYNC();
+                    if (beta.hi != 0.f) {
+                        if (tid == 0) {
+                            if (first && k > il) T_(k, k - 1) = df_neg(T_(k, k - 1));
+                            else if (!first) T_(k, k - 1) = beta;
+                        }
+                        const df ntau = df_neg(tau), nte0 = df_neg(df_mul(tau, e0)), nte1 = df_neg(df_mul(tau, e1));
+                        for (int cc = k + tid; cc <= iu; cc += GS) {  // left: rows k..k+2
+                            const df a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
+                            const df t = df_add(df_fma(e1, a2, df_mul(e0, a1)), a0);
+                            T_(k, cc) = df_fma(ntau, t, a0);
+                            T_(k + 1, cc) = df_fma(nte0, t, a1);
+                            T_(k + 2, cc) = df_fma(nte1, t, a2);
+                        }
+                        QR_SYNC();
+                        const int rend = min(iu, k + 3);
+                        for (int rr = il + tid; rr <= rend; rr += GS) {  // right: cols k..k+2
+                            const df b0 = T_(rr, k), b1 = T_(rr, k + 1), b2 = T_(rr, k + 2);
+                            const df ntt = df_neg(df_mul(tau, df_add(df_fma(b2, e1, df_mul(b1, e0)), b0)));
+                            T_(rr, k) = df_add(b0, ntt);
+                            T_(rr, k + 1) = df_fma(ntt, e0, b1);
+                            T_(rr, k + 2) = df_fma(ntt, e1, b2);
+                        }
+                    }
+                    QR_SYNC();
+                }
+                {
+                    const df v0 = T_(iu - 1, iu - 2), v1 = T_(iu, iu - 2);
+                    df e0 = zero, tau = zero, beta = v0;
+                    const float m = fmaxf(fabsf(v0.hi), fabsf(v1.hi));
+                    if (m != 0.f) {
+                        float down, up;
+                        hh_scale(m, down, up);
+                        const df w0 = df_scale(v0, down), w1 = df_scale(v1, down);
+                        const df tail = df_mul(w1, w1);
+                        if (tail.hi != 0.f) {
+                            df bb = df_sqrt(df_fma(w0, w0, tail));
+                            if (w0.hi >= 0.f) bb = df_neg(bb);
+                            e0 = df_div(w1, df_sub(w0, bb));
+                            tau = df_div(df_sub(bb, w0), bb);
+                            beta = df_scale(bb, up);
+                        }
+                    }
+                    QR_SYNC();
+                    if (beta.hi != 0.f) {
+                        if (tid == 0) T_(iu - 1, iu - 2) = beta;
+                        const df ntau = df_neg(tau), nte0 = df_neg(df_mul(tau, e0));
+                        for (int cc = iu - 1 + tid; cc <= iu; cc += GS) {
+                            const df a0 = T_(iu - 1, cc), a1 = T_(iu, cc);
+                            const df t = df_fma(e0, a1, a0);
+                            T_(iu - 1, cc) = df_fma(ntau, t, a0);
+                            T_(iu, cc) = df_fma(nte0, t, a1);
+                        }
+                        QR_SYNC();
+                        for (int rr = il + tid; rr <= iu; rr += GS) {
+                            const df b0 = T_(rr, iu - 1), b1 = T_(rr, iu);
+                            const df ntt = df_neg(df_mul(tau, df_fma(b1, e0, b0)));
+                            T_(rr, iu - 1) = df_add(b0, ntt);
+                            T_(rr, iu) = df_fma(ntt, e0, b1);
+                        }
+                    }
+                    QR_SYNC();
+                }
+                for (int i = im + 2 + tid; i <= iu; i += GS) {
+                    T_(i, i - 2) = zero;
+                    if (i > im + 2) T_(i, i - 3) = zero;
+                }
+                QR_SYNC();
+            }
+        }
+    }
+    if (tid == 0) {
+        double f = 0;
+        if (!failed) {
+            // eigenvalue #2 in Schur order (EigenSolver::compute, EigenSolver.h:363-381), in FP64 from the pairs
+            int i = 0;
+            double re2 = 0, im2 = 1;
+            while (i < n && i <= 2) {
+                if (i == n - 1 || T_(i + 1, i).hi == 0.f) {
+                    if (i == 2) { re2 = df_to_double(T_(i, i)); im2 = 0; }
+                    ++i;
+                } else {
+                    const double tii = df_to_double(T_(i, i)), tjj = df_to_double(T_(i + 1, i + 1));
+                    const double p = 0.5 * (tii - tjj);
+                    const double z = sqrt(fabs(p * p + df_to_double(T_(i + 1, i)) * df_to_double(T_(i, i + 1))));
+                    if (i == 2 || i + 1 == 2) { re2 = tjj + p; im2 = (i == 2) ? z : -z; }
+                    i += 2;
+                }
+            }
+            if (im2 == 0) f = sqrt(fmax(re2, 0.0));
+        }
+        res[13] = f;  // no convergence: 0, as the oracle
+    }
+#undef T_
+}
+
 // Matrices with at least QR_BIG tones (the long chains) get 4 warps each, one
 // per SM sub-partition, which quarters the reflector updates on the critical
 // path, as long as there are no more of them than max_groups; the rest (and
@@ -786,8 +1100,14 @@ __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, c
     const int n = ((const int *)(wsb + H.lut_b))[256];
     double *res = (double *)(wsb + H.res_b) + ang * 14;
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
-    if ((int)blockIdx.x < nbig) har_schur<4, FUSED>(A, n, rowsum[0], res, threadIdx.x);
-    else har_schur<1, FUSED>(A, n, rowsum[wq], res, threadIdx.x & 31);
+    if (FUSED) {
+        float *rs = (float *)rowsum[(int)blockIdx.x < nbig ? 0 : wq];
+        if ((int)blockIdx.x < nbig) har_schur_df<4>((df *)A, n, rs, res, threadIdx.x);
+        else har_schur_df<1>((df *)A, n, rs, res, threadIdx.x & 31);
+        return;
+    }
+    if ((int)blockIdx.x < nbig) har_schur<4, false>(A, n, rowsum[0], res, threadIdx.x);
+    else har_schur<1, false>(A, n, rowsum[wq], res, threadIdx.x & 31);
 }
 
 // mean and range over the angles, permuted into the output order

@@ -59,12 +59,26 @@ __device__ __forceinline__ double local_mean(const double *__restrict__ S, int W
     const long long cnt = (ey - sy + 1) * (ex - sx + 1);
     const double v = __dadd_rn(__dsub_rn(__dsub_rn(unten, links), oben), ol);
     // an unclipped window holds a power-of-two count: dividing by 2^e and
-    // multiplying by the exact 2^-e round identically, and spare the FP64 pipe
+    // multiplying by the exact 2^-e round identically; while the quotient stays
+    // normal that is an exponent decrement on the integer pipe
     if ((cnt & (cnt - 1)) == 0) {
         const int e = __ffsll(cnt) - 1;
+        const long long b = __double_as_longlong(v);
+        const int E = (int)((b >> 52) & 0x7ff);
+        if (E > e && E != 0x7ff) return __longlong_as_double(b - ((long long)e << 52));
+        if ((b & 0x7fffffffffffffffLL) == 0) return v;
         return __dmul_rn(v, __longlong_as_double((long long)(1023 - e) << 52));
     }
     return v / (double)cnt;
+}
+
+// |a - b| as bits (a nonnegative double orders as its bit pattern)
+__device__ __forceinline__ long long absdiff_bits(double a, double b) {
+    return __double_as_longlong(__dsub_rn(a, b)) & 0x7fffffffffffffffLL;
+}
+// a finite double below 2^1022 in magnitude (2x is exact and finite)
+__device__ __forceinline__ bool tame(double v) {
+    return ((__double_as_longlong(v) >> 52) & 0x7ff) < 0x7fd;
 }
 
 #define TAM_TILE 1024
@@ -84,22 +98,26 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
     double *phi = ws + T.phi_ws;
     long long ksum = 0;
     int kmin = 1 << 30, kmax = -1;
-    double pmn = DBL_MAX, pmx = -DBL_MAX, sr = 0;
+    // pmn from DBL_MAX; pmx from -DBL_MAX, whose pattern is negative as a signed integer
+    long long pmnb = __double_as_longlong(DBL_MAX), pmxb = __double_as_longlong(-DBL_MAX);
+    double sr = 0;
     const long long i0 = (long long)blockIdx.x * TAM_TILE, i1 = min(n, i0 + TAM_TILE);
     for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int y = (int)(i / W), x = (int)(i - (long long)y * W);
-        // coarseness: first strict maximum over k = 1..7, horizontal before vertical
-        double maxE = 0;
+        // coarseness: first strict maximum over k = 1..7, horizontal before vertical.
+        // E values are |differences| (+0 or more, or NaN): compared as bit
+        // patterns, NaN never greater, exactly as the double comparison
+        long long maxE = 0;
         int maxk = 0, k2 = 1;
         for (int k = 1; k <= 7; k++, k2 *= 2) {
             const long long len = 2 * k2;
-            double eh = 0, ev = 0;
+            long long eh = 0, ev = 0;
             if (x + k2 < W && x - k2 >= 0)
-                eh = fabs(__dsub_rn(local_mean(S, W, H, x + k2, y, len), local_mean(S, W, H, x - k2, y, len)));
+                eh = absdiff_bits(local_mean(S, W, H, x + k2, y, len), local_mean(S, W, H, x - k2, y, len));
             if (y + k2 < H && y - k2 >= 0)
-                ev = fabs(__dsub_rn(local_mean(S, W, H, x, y + k2, len), local_mean(S, W, H, x, y - k2, len)));
-            if (eh > maxE) { maxE = eh; maxk = k; }
-            if (ev > maxE) { maxE = ev; maxk = k; }
+                ev = absdiff_bits(local_mean(S, W, H, x, y + k2, len), local_mean(S, W, H, x, y - k2, len));
+            if (eh > maxE && eh <= 0x7ff0000000000000LL) { maxE = eh; maxk = k; }
+            if (ev > maxE && ev <= 0x7ff0000000000000LL) { maxE = ev; maxk = k; }
         }
         sb[i] = (unsigned char)maxk;
         ksum += maxk;
@@ -107,29 +125,57 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
         kmax = max(kmax, maxk);
         // directionality: H = [[-1,2,1],[-2,0,2],[-1,-2,-1]], V = [[1,0,0],[0,0,0],[-1,0,0]],
         // accumulated x offset outer, y offset inner, zero outside the image
+        // When the neighbourhood is finite and below 2^1022, the zero-coefficient
+        // terms add +-0 to sums that are never -0 (they start at +0), the +-1
+        // products are exact and x + 2v is one rounding, so the same sums take
+        // fused multiply-adds over the nonzero taps, in the same order.
         const double fH[3][3] = {{-1, 2, 1}, {-2, 0, 2}, {-1, -2, -1}};
         const double fV[3][3] = {{1, 0, 0}, {0, 0, 0}, {-1, 0, 0}};
-        double dH = 0, dV = 0;
-        for (int a = -1; a <= 1; a++) {
-            const int xx = x + a;
-            if (xx < 0 || xx >= W) continue;
+        double nb[3][3];
+        bool fast = true;
+        for (int a = -1; a <= 1; a++)
             for (int b = -1; b <= 1; b++) {
-                const int yy = y + b;
-                if (yy < 0 || yy >= H) continue;
-                const double v = nrm[(long long)yy * W + xx];
-                dH = __dadd_rn(dH, __dmul_rn(fH[b + 1][a + 1], v));
-                dV = __dadd_rn(dV, __dmul_rn(fV[b + 1][a + 1], v));
+                const int xx = x + a, yy = y + b;
+                const bool in = xx >= 0 && xx < W && yy >= 0 && yy < H;
+                nb[b + 1][a + 1] = in ? nrm[(long long)yy * W + xx] : 0.0;
+                fast = fast && tame(nb[b + 1][a + 1]);
+            }
+        double dH = 0, dV = 0;
+        if (fast) {
+            // out-of-image taps hold +0 and add nothing (x + 0 = x for x != -0)
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++)
+                    if (fH[b][a] != 0) dH = __fma_rn(fH[b][a], nb[b][a], dH);
+            dV = __dsub_rn(nb[0][0], nb[2][0]);
+        } else {
+            for (int a = -1; a <= 1; a++) {
+                const int xx = x + a;
+                if (xx < 0 || xx >= W) continue;
+                for (int b = -1; b <= 1; b++) {
+                    const int yy = y + b;
+                    if (yy < 0 || yy >= H) continue;
+                    const double v = nb[b + 1][a + 1];
+                    dH = __dadd_rn(dH, __dmul_rn(fH[b + 1][a + 1], v));
+                    dV = __dadd_rn(dV, __dmul_rn(fV[b + 1][a + 1], v));
+                }
             }
         }
+        // dH >= 1e-4 and the running min / max of phi (phi is +0 or positive, or
+        // NaN, which fmin / fmax skip) as comparisons of bit patterns
+        const long long dHb = __double_as_longlong(dH);
         double ph = 0.0;
-        if (dH >= 0.0001) {
+        if (dHb >= 0x3f1a36e2eb1c432dLL && dHb <= 0x7ff0000000000000LL) {
             ph = atan(dV / dH) + (M_PI / 2.0 + 0.001);
             sr += __dadd_rn(__dadd_rn(__dmul_rn(dH, dH), __dmul_rn(dV, dV)), __dmul_rn(ph, ph));
         }
         phi[i] = ph;
-        pmn = fmin(pmn, ph);
-        pmx = fmax(pmx, ph);
+        const long long phb = __double_as_longlong(ph);
+        if ((phb & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL) {
+            pmnb = min(pmnb, phb);
+            pmxb = max(pmxb, phb);
+        }
     }
+    double pmn = __longlong_as_double(pmnb), pmx = __longlong_as_double(pmxb);
     ksum = block_sum_ll(ksum, shl);
     const double dkmin = block_min((double)kmin, sh), dkmax = block_max((double)kmax, sh);
     pmn = block_min(pmn, sh);

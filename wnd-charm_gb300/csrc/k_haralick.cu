@@ -291,15 +291,72 @@ __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict
     }
 }
 
+// The mixed form's Q, in pairs of floats: the GLCM (no longer read by f1..f13)
+// is converted in place on the integer pipe, then each term is
+// P(i,k) P(j,k) times the pair reciprocal of px_i py_k + 1e-13, summed in the
+// same k order.  Q is written in pairs for k_har_hess_df.
+__global__ void __launch_bounds__(256) k_har_p_df(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    const int ang = blockIdx.y;
+    const HarJob H = hj[blockIdx.x];
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    if (n < 3) return;
+    df *P = (df *)((double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256);
+    for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) P[q] = df_split(*(const double *)&P[q]);
+}
+
+__global__ void __launch_bounds__(32 * Q_WARPS) k_har_q_df(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    __shared__ df qrow[Q_WARPS][256];
+    __shared__ df py[256];
+    const int ang = blockIdx.y;
+    const HarJob H = hj[blockIdx.x];
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    if (n < 3) return;
+    const df *P = (const df *)((const double *)(wsb + H.glcm_b) + (long long)ang * 256 * 256);
+    df *A = (df *)((double *)(wsb + H.q_b) + (long long)ang * 256 * 256);
+    const double *mar = (const double *)(wsb + H.mar_b + (long long)ang * HAR_MAR_BYTES);
+    const int *lo = (const int *)(wsb + H.mar_b + (long long)ang * HAR_MAR_BYTES + 4096), *hi = lo + 256;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) py[k] = df_split(mar[256 + k]);
+    __syncthreads();
+    const df one = {1.f, 0.f}, eps13 = df_from_double(0.0000000000001);
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    df *q = qrow[wq];
+    for (int i = blockIdx.z * Q_WARPS + wq; i < n; i += gridDim.z * Q_WARPS) {
+        for (int j = lane; j < n; j += 32) q[j] = df{0.f, 0.f};
+        __syncwarp();
+        const df di = df_split(mar[i]);
+        const df *Pi = P + (long long)i * n;
+        const int klo = lo[i], khi = hi[i];
+        for (int k0 = klo; k0 <= khi; k0 += 32) {
+            const int kk = k0 + lane;
+            const df al = kk <= khi ? Pi[kk] : df{0.f, 0.f};
+            unsigned m = __ballot_sync(0xffffffffu, al.hi != 0.f);
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1;
+                const int k = k0 + b;
+                const df a = df_shfl(al, b);
+                const df rd = df_div(one, df_fma(di, py[k], eps13));
+                const df *Pk = P + (long long)k * n;
+                for (int j = lo[k] + lane; j <= hi[k]; j += 32) {
+                    const df rp = df_mul(a, Pk[j]);
+                    if (rp.hi != 0.f) q[j] = df_fma(rp, rd, q[j]);
+                }
+                __syncwarp();
+            }
+        }
+        df *Ai = A + (long long)i * n;
+        for (int j = lane; j < n; j += 32) Ai[j] = q[j];
+        __syncwarp();
+    }
+}
+
 // Hessenberg reduction of Q in place (HessenbergDecomposition::_compute,
 // HessenbergDecomposition.h:292-318): column i's reflector from the sequential
 // tail sum, then H A on the trailing rows and A H on all rows.  One CTA per
 // matrix; products that the reference forms per element (tau * ess_r, tau * t)
 // are formed once, with the same value.
-// FUSED (mixed form): fused multiply-adds in the two updates.
-template <bool FUSED>
 __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
-    __shared__ double v[256], ess[256], tess[256], red[32];
+    __shared__ double v[256], ess[256], tess[256];
     __shared__ double s_tau, s_beta, s_den;
     __shared__ int s_triv;
     const int ang = blockIdx.y;
@@ -311,17 +368,9 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
         const int rem = n - i - 1;
         for (int k = threadIdx.x; k < rem; k += blockDim.x) v[k] = A[(long long)(i + 1 + k) * n + i];
         __syncthreads();
-        double tail_mixed = 0;
-        if (FUSED) {  // the mixed form sums the tail as a tree (no 255-deep dependent chain)
-            double q = 0;
-            for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) q = __fma_rn(v[k], v[k], q);
-            tail_mixed = block_sum(q, red);
-        }
         if (threadIdx.x == 0) {  // makeHouseholder (Householder.h:65-90)
             double tail = 0;
-            if (FUSED) tail = tail_mixed;
-            else
-                for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, __dmul_rn(v[k], v[k]));
+            for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, __dmul_rn(v[k], v[k]));
             const double c0 = v[0];
             if (rem == 1 || tail == 0) {
                 s_triv = 1;
@@ -354,13 +403,6 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
                 continue;
             }
             double t = 0;
-            if (FUSED) {
-                for (int r = 1; r < rem; r++) t = __fma_rn(ess[r - 1], col[(long long)r * n], t);
-                t = __dadd_rn(t, col[0]);
-                col[0] = __fma_rn(-tau, t, col[0]);
-                for (int r = 1; r < rem; r++) col[(long long)r * n] = __fma_rn(-tess[r - 1], t, col[(long long)r * n]);
-                continue;
-            }
             for (int r = 1; r < rem; r++) t = __dadd_rn(t, __dmul_rn(ess[r - 1], col[(long long)r * n]));
             t = __dadd_rn(t, col[0]);
             col[0] = __dsub_rn(col[0], __dmul_rn(tau, t));
@@ -375,14 +417,6 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
                 continue;
             }
             double t = 0;
-            if (FUSED) {
-                for (int c = 1; c < rem; c++) t = __fma_rn(row[c], ess[c - 1], t);
-                t = __dadd_rn(t, row[0]);
-                const double tt = __dmul_rn(tau, t);
-                row[0] = __dsub_rn(row[0], tt);
-                for (int c = 1; c < rem; c++) row[c] = __fma_rn(-tt, ess[c - 1], row[c]);
-                continue;
-            }
             for (int c = 1; c < rem; c++) t = __dadd_rn(t, __dmul_rn(row[c], ess[c - 1]));
             t = __dadd_rn(t, row[0]);
             const double tt = __dmul_rn(tau, t);
@@ -477,10 +511,7 @@ __global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj
 // takes the same decisions from the same values; writes of single entries are
 // made by tid 0; the reflector updates spread their columns / rows over the
 // group, with a barrier between dependent phases.
-// FUSED (mixed form): the bulge-chasing updates use fused multiply-adds, as a
-// reference build with FP contraction does; f14 then follows that build's
-// rounding instead of the oracle's (it is range-checked, never compared).
-template <int NW, bool FUSED>
+template <int NW>
 __device__ void har_schur(double *__restrict__ A, const int n, double *__restrict__ rowsum, double *__restrict__ res,
                           const int tid) {
     const int lane = tid & 31;
@@ -663,13 +694,6 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                         const double te0 = __dmul_rn(tau, ess[0]), te1 = __dmul_rn(tau, ess[1]);  // per column alike
                         for (int cc = k + tid; cc <= iu; cc += GS) {  // left: rows k..k+2
                             const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
-                            if (FUSED) {
-                                const double t = __dadd_rn(__fma_rn(ess[1], a2, __dmul_rn(ess[0], a1)), a0);
-                                T_(k, cc) = __fma_rn(-tau, t, a0);
-                                T_(k + 1, cc) = __fma_rn(-te0, t, a1);
-                                T_(k + 2, cc) = __fma_rn(-te1, t, a2);
-                                continue;
-                            }
                             double t = plus_zero(__dmul_rn(ess[0], a1));
                             t = __dadd_rn(t, __dmul_rn(ess[1], a2));
                             t = __dadd_rn(t, a0);
@@ -681,13 +705,6 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                         const int rend = min(iu, k + 3);
                         for (int rr = il + tid; rr <= rend; rr += GS) {  // right: cols k..k+2
                             const double b0 = T_(rr, k), b1 = T_(rr, k + 1), b2 = T_(rr, k + 2);
-                            if (FUSED) {
-                                const double tt = __dmul_rn(tau, __dadd_rn(__fma_rn(b2, ess[1], __dmul_rn(b1, ess[0])), b0));
-                                T_(rr, k) = __dsub_rn(b0, tt);
-                                T_(rr, k + 1) = __fma_rn(-tt, ess[0], b1);
-                                T_(rr, k + 2) = __fma_rn(-tt, ess[1], b2);
-                                continue;
-                            }
                             double t = plus_zero(__dmul_rn(b1, ess[0]));
                             t = __dadd_rn(t, __dmul_rn(b2, ess[1]));
                             t = __dadd_rn(t, b0);
@@ -750,9 +767,8 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                     i += 2;
                 }
             }
-            // Q's eigenvalues are >= 0; a negative one is rounding.  The FP64 form
-            // keeps the reference's sqrt (NaN there); the mixed form reads it as 0.
-            if (im2 == 0) f = sqrt(FUSED ? fmax(re2, 0.0) : re2);
+            // the reference's sqrt (NaN for a rounding-negative eigenvalue)
+            if (im2 == 0) f = sqrt(re2);
         }
         res[13] = f;  // no convergence: 0, as the oracle
     }
@@ -767,9 +783,9 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
 // there, or eps times the matrix's norm: clusters of eigenvalues near 1e-18
 // (Q is close to singular) cannot reach the relative threshold within float's
 // exponent range, and without the normwise one ran to the iteration limit.
-// The choices between candidates compare the leading floats.  The Hessenberg matrix arrives in FP64 and is converted
-// in place on the integer pipe (a double and a pair are both 8 bytes; zeros are
-// zero bits in both).
+// The choices between candidates compare the leading floats.  The Hessenberg
+// matrix arrives in pairs from k_har_hess_df (a double and a pair are both 8
+// bytes, in the same place).
 // The vector is first scaled by a power of two that brings its largest entry
 // into [0.5, 1): exact, leaves ess and tau unchanged and beta scaled back, and
 // keeps the squares within float's exponent range (FP64's wider range needs no
@@ -814,11 +830,6 @@ __device__ void har_schur_df(df *__restrict__ A, const int n, float *__restrict_
         return;
     }
 #define T_(r, c) A[(long long)(r) * n + (c)]
-    for (int r = 0; r < n; r++)
-        for (int c = (r > 0 ? r - 1 : 0) + tid; c < n; c += GS) {
-            T_(r, c) = df_split(*(const double *)&T_(r, c));
-        }
-    QR_SYNC();
     for (int j = tid; j < n; j += GS) {
         float s = 0.f;
         for (int c = (j > 0 ? j - 1 : 0); c < n; c++) s = __fadd_rn(s, fabsf(T_(j, c).hi));
@@ -1072,12 +1083,131 @@ __device__ void har_schur_df(df *__restrict__ A, const int n, float *__restrict_
 #undef T_
 }
 
+// The mixed form's Hessenberg reduction: the reflectors and updates of
+// k_har_hess in pairs of floats (FP32 pipe) on Q from k_har_q_df, each
+// column's vector scaled by a power of two
+// before its squares are summed (exact; keeps them within float's exponent
+// range).  The matrix stays in pairs for har_schur_df.
+__device__ __forceinline__ float block_max_f(float v, float *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    float r = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.f;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_down_sync(0xffffffffu, r, o));
+    if (threadIdx.x == 0) sh[0] = r;
+    __syncthreads();
+    r = sh[0];
+    __syncthreads();
+    return r;
+}
+__device__ __forceinline__ df block_sum_df(df v, df *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = df_add(v, {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    df r = (threadIdx.x < nw) ? sh[threadIdx.x] : df{0.f, 0.f};
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) r = df_add(r, {__shfl_down_sync(0xffffffffu, r.hi, o), __shfl_down_sync(0xffffffffu, r.lo, o)});
+    if (threadIdx.x == 0) sh[0] = r;
+    __syncthreads();
+    r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_har_hess_df(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
+    __shared__ df v[256], ess[256], tess[256], red[32];
+    __shared__ float redf[32];
+    __shared__ df s_tau, s_beta, s_den;
+    __shared__ int s_triv;
+    const int ang = blockIdx.y;
+    const HarJob H = hj[blockIdx.x];
+    const int n = ((const int *)(wsb + H.lut_b))[256];
+    if (n < 3) return;
+    df *A = (df *)((double *)(wsb + H.q_b) + (long long)ang * 256 * 256);
+    const df zero = {0.f, 0.f};
+    for (int i = 0; i < n - 1; i++) {
+        const int rem = n - i - 1;
+        float m = 0.f;
+        for (int k = threadIdx.x; k < rem; k += blockDim.x) {
+            const df x = A[(long long)(i + 1 + k) * n + i];
+            v[k] = x;
+            m = fmaxf(m, fabsf(x.hi));
+        }
+        m = block_max_f(m, redf);
+        float down = 1.f, up = 1.f;
+        if (m != 0.f) hh_scale(m, down, up);
+        df q = zero;
+        for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) {
+            const df w = df_scale(v[k], down);
+            q = df_fma(w, w, q);
+        }
+        const df tail = block_sum_df(q, red);
+        if (threadIdx.x == 0) {  // makeHouseholder (Householder.h:65-90) on the scaled vector
+            const df c0 = df_scale(v[0], down);
+            if (rem == 1 || tail.hi == 0.f) {
+                s_triv = 1;
+                s_beta = v[0];
+            } else {
+                df bb = df_sqrt(df_fma(c0, c0, tail));
+                if (c0.hi >= 0.f) bb = df_neg(bb);
+                s_triv = 0;
+                s_beta = df_scale(bb, up);
+                s_den = df_sub(c0, bb);
+                s_tau = df_div(df_sub(bb, c0), bb);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) A[(long long)(i + 1) * n + i] = s_beta;
+        if (s_triv) {  // tau = 0: both updates are the identity
+            __syncthreads();
+            continue;
+        }
+        const df tau = s_tau, ntau = df_neg(tau);
+        for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) {
+            const df e = df_div(df_scale(v[k], down), s_den);
+            ess[k - 1] = e;
+            tess[k - 1] = df_neg(df_mul(tau, e));
+        }
+        __syncthreads();
+        // H A: rows i+1.., columns i+1.. (threads over columns)
+        for (int c = i + 1 + threadIdx.x; c < n; c += blockDim.x) {
+            df *col = A + (long long)(i + 1) * n + c;
+            df t = zero;
+            for (int r = 1; r < rem; r++) t = df_fma(ess[r - 1], col[(long long)r * n], t);
+            t = df_add(t, col[0]);
+            col[0] = df_fma(ntau, t, col[0]);
+            for (int r = 1; r < rem; r++) col[(long long)r * n] = df_fma(tess[r - 1], t, col[(long long)r * n]);
+        }
+        __syncthreads();
+        // A H: all rows, columns i+1.. (threads over rows)
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            df *row = A + (long long)r * n + i + 1;
+            df t = zero;
+            for (int c = 1; c < rem; c++) t = df_fma(row[c], ess[c - 1], t);
+            t = df_add(t, row[0]);
+            const df ntt = df_neg(df_mul(tau, t));
+            row[0] = df_add(row[0], ntt);
+            for (int c = 1; c < rem; c++) row[c] = df_fma(ntt, ess[c - 1], row[c]);
+        }
+        __syncthreads();
+    }
+    for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
+        const int r = (int)(q / n), c = (int)(q - (long long)r * n);
+        if (c < r - 1) A[q] = zero;
+    }
+}
+
 // Matrices with at least QR_BIG tones (the long chains) get 4 warps each, one
 // per SM sub-partition, which quarters the reflector updates on the critical
 // path, as long as there are no more of them than max_groups; the rest (and
 // all of them beyond that) run one per warp, 4 to a block.  perm lists the
 // matrices by descending Ng and nbig counts the large ones.
-template <bool FUSED>
+template <bool MIXED>
 __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb,
                                                 const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat,
                                                 int max_groups) {
@@ -1100,14 +1230,14 @@ __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, c
     const int n = ((const int *)(wsb + H.lut_b))[256];
     double *res = (double *)(wsb + H.res_b) + ang * 14;
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
-    if (FUSED) {
+    if (MIXED) {
         float *rs = (float *)rowsum[(int)blockIdx.x < nbig ? 0 : wq];
         if ((int)blockIdx.x < nbig) har_schur_df<4>((df *)A, n, rs, res, threadIdx.x);
         else har_schur_df<1>((df *)A, n, rs, res, threadIdx.x & 31);
         return;
     }
-    if ((int)blockIdx.x < nbig) har_schur<4, false>(A, n, rowsum[0], res, threadIdx.x);
-    else har_schur<1, false>(A, n, rowsum[wq], res, threadIdx.x & 31);
+    if ((int)blockIdx.x < nbig) har_schur<4>(A, n, rowsum[0], res, threadIdx.x);
+    else har_schur<1>(A, n, rowsum[wq], res, threadIdx.x & 31);
 }
 
 // mean and range over the angles, permuted into the output order
@@ -1152,13 +1282,19 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     {
     ProfScope p2(c, "Haralick: Q");
     WC_LAUNCH(c);
-    k_har_q<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
+    if (c.prec == WC_PREC_MIXED) {
+        k_har_p_df<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+        WC_LAUNCH(c);
+        k_har_q_df<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
+    } else {
+        k_har_q<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
+    }
     }
     {
     ProfScope p3(c, "Haralick: Hessenberg");
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED) k_har_hess<true><<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
-    else k_har_hess<false><<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    if (c.prec == WC_PREC_MIXED) k_har_hess_df<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    else k_har_hess<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
     }
     {
     ProfScope p4(c, "Haralick: real Schur (f14)");

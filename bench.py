@@ -124,31 +124,34 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def stage_work(name, B):
+def stage_work(name, B, precision="mixed"):
     """Algorithmic work per step of a stage on the long plan at 512^2, for the
-    roofline of the dominant stage: (kind, amount) with kind 'bytes' (HBM) or
-    'flops'."""
+    roofline of the dominant stage: (kind, amount) with kind 'bytes' (HBM),
+    'fp64' (FP64 flops) or 'flops'; None where no model applies."""
     px = IMG * IMG
     planes_c = 12  # group C runs on 12 planes per image
     table = {
         # read each plane once (8 B/px) for every pass the family needs
-        # FP64 operations of Q, the Hessenberg reduction and the real-Schur QR for
-        # f14, counted by an instrumented run of the oracle on this workload
-        # (about 1.3 G per 512^2 image: 10/3 Ng^3 + 9 per touched element per
-        # Francis step + 3 per nonzero Q term, summed over the 48 matrices)
-        "Haralick Textures": ("fp64", B * 1.3e9),
         "Tamura Textures": ("bytes", B * planes_c * px * 8 * 4),
         "Gabor Textures": ("bytes", B * px * 8 * 2),
-        # two FP64 products per Chebyshev transform (C, then C of F and of W), FP64 in both forms
+        # three 2-D Chebyshev transforms per image (of the image, of its Fourier
+        # and of its wavelet plane), each two 512^3 products; a multiply and an
+        # add per term (FP64 and unfused in both forms: the reference's rounding)
         "Chebyshev": ("fp64", B * 3 * 2 * 2 * IMG ** 3),
-        # Zernike moments: FP64 in both forms
-        "Zernike Coefficients": ("fp64", B * 8 * px * 460),
-        "Chebyshev-Fourier Coefficients": ("flops", B * 8 * int(0.785 * 300 * 300) * 529 * 4),
         "Comb Moments": ("bytes", B * planes_c * px * 8),
         "Radon Coefficients": ("bytes", B * planes_c * px * 8),
         "Fractal Features": ("bytes", B * planes_c * px * 8),
         "PixStats+Gini (sort)": ("bytes", B * planes_c * px * 8 * 16),
     }
+    if precision == "fp64":
+        # FP64 operations of Q, the Hessenberg reduction and the real-Schur QR for
+        # f14, counted by an instrumented run of the oracle on this workload
+        # (about 1.3 G per 512^2 image: 10/3 Ng^3 + 9 per touched element per
+        # Francis step + 3 per nonzero Q term, summed over the 48 matrices); the
+        # mixed form computes them in pairs of floats
+        table["Haralick Textures"] = ("fp64", B * 1.3e9)
+        # Zernike moments (the mixed form sums them in pairs of floats)
+        table["Zernike Coefficients"] = ("fp64", B * 8 * px * 460)
     return table.get(name)
 
 
@@ -343,20 +346,28 @@ def main():
     prof = eng.profile_report()
     timeline = eng.profile_timeline()
     eng.profile(False)
-    tot_prof = sum(ms for name, ms, _ in prof if not name.startswith("host")) or 1.0
-    # the dominant kernel chain is Haralick's f14 (Q, Hessenberg, real Schur): the
-    # largest share of serialised kernel time in the launch lists under profiles/;
-    # in this concurrent step every stage's wall time also holds waits for the others
-    prof_ms = {name: ms for name, ms, _ in prof}
-    dom = ("Haralick Textures", prof_ms.get("Haralick Textures", 0.0), 1)
+    # and one with the lanes serialised: every stage's own duration (what a
+    # launch list shows, caches warm), for the roofline of the dominant stage
+    eng.profile(True, serial=True)
+    step_dev()
+    stream.synchronize()
+    prof_alone = {name: ms for name, ms, _ in eng.profile_report()}
+    eng.profile(False)
+    # the dominant stage: the largest share of the serialised step (each stage
+    # timed alone, as in the ncu launch lists under profiles/); its roofline
+    # uses that duration
+    top = {n: ms for n, ms in prof_alone.items() if not n.startswith("host") and ":" not in n}
+    tot_prof = sum(top.values()) or 1.0
+    dname = max(top, key=top.get)
+    dom = (dname, top[dname], 1)
     peaks = {}
     pk_path = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
     hbm = peaks.get("hbm_gbs", 6800.0)
     tfl = peaks.get("bf16_tflops", 1900.0)
-    work = stage_work(dom[0], B)
-    roof = {"stage": dom[0], "stage_ms_per_step": dom[1], "stage_share": dom[1] / tot_prof,
+    work = stage_work(dom[0], B, args.precision)
+    roof = {"stage": dom[0], "stage_ms_alone_per_step": dom[1], "stage_share": dom[1] / tot_prof,
             "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
             "peak_source": "measured" if peaks else "fallback"}
     if work:
@@ -371,12 +382,13 @@ def main():
         else:
             roof.update({"bound": "tensor", "achieved": amt / sec / 1e12, "peak": tfl, "unit": "TFLOP/s"})
         roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["stage_choice"] = ("largest share of serialised kernel time (ncu launch list); stage time is its "
-                            "wall time inside the concurrent step")
+    roof["stage_choice"] = ("largest share of the step with the lanes serialised (engine profile, each stage "
+                            "timed alone with CUDA events on the engine's stream); achieved uses that time")
     # the whole step against its floor: the FP64 families' algorithmic work at the
     # measured FP64 peak plus one read of every plane per scan family at HBM speed
     p64 = roof["peak"] if roof.get("bound") == "fp64" else fp64_peak_tflops(dev)
-    fl = sum(stage_work(n, B)[1] for n in ("Haralick Textures", "Chebyshev", "Zernike Coefficients"))
+    fl = sum(w[1] for w in (stage_work(n, B, args.precision) for n in ("Haralick Textures", "Chebyshev",
+                                                                        "Zernike Coefficients")) if w)
     by = sum(stage_work(n, B)[1] for n in ("Tamura Textures", "Gabor Textures", "Comb Moments", "Radon Coefficients",
                                             "Fractal Features", "PixStats+Gini (sort)"))
     floor_ms = 1000.0 * (fl / (p64 * 1e12) + by / (hbm * 1e9))
@@ -399,7 +411,8 @@ def main():
             "roofline": roof, "step_roofline": step_roof,
             "forms": forms,
             "stages_ms": {n: round(ms, 3) for n, ms, _ in prof},
-            "timeline_ms": {n: [round(a, 1), round(b, 1)] for n, a, b in timeline}}
+            "timeline_ms": {n: [round(a, 1), round(b, 1)] for n, a, b in timeline},
+            "stages_alone_ms": {n: round(ms, 3) for n, ms in prof_alone.items()}}
     if rank == 0 and not args.no_cpu_baseline:
         nth = os.cpu_count() or 1
         ncpu = min(nth, B)

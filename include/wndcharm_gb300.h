@@ -105,7 +105,9 @@ long long wc_engine_launch_count(const wc_engine *engine);
  * "stage<TAB>milliseconds<TAB>calls<TAB>start<TAB>end" lines accumulated since
  * the last switch (start / end: the stage's earliest start and latest end in ms
  * after the batch's first stage; -1 for the host-side stages, "host: ...",
- * which are wall-clock milliseconds of the calling thread). */
+ * which are wall-clock milliseconds of the calling thread).  on = 2 also runs
+ * every lane on the engine's stream, one stage after another, so that each
+ * stage's time is its own (as in a serialised launch list, caches warm). */
 int wc_engine_profile(wc_engine *engine, int on);
 int wc_engine_profile_report(wc_engine *engine, char *buf, int buflen);
 

@@ -390,7 +390,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     Ctx lc[WC_LANES];
     for (int k = 0; k < WC_LANES; k++) {
         lc[k] = ctx;
-        lc[k].st = E->lanes[k];
+        lc[k].st = E->prof.serial ? ctx.st : E->lanes[k];
     }
     fr.lanes = lc;
     // Families that read only the root planes (Gabor, object and edge features in
@@ -606,6 +606,7 @@ long long wc_engine_launch_count(const wc_engine *E) { return E ? E->launches : 
 int wc_engine_profile(wc_engine *E, int on) {
     if (!E) return set_err(WC_ERR_ARG, "null engine");
     E->prof.on = on != 0;
+    E->prof.serial = on == 2;
     E->prof.order.clear();
     E->prof.ms.clear();
     E->prof.calls.clear();

@@ -217,7 +217,6 @@ __global__ void __launch_bounds__(512) k_gini(const Plane *__restrict__ planes, 
                        const unsigned long long *__restrict__ keys, const long long *__restrict__ key_off,
                        double *__restrict__ feat) {
     __shared__ double sh[32];
-    __shared__ long long shl[32];
     const FJob J = jobs[blockIdx.x];
     const Plane P = planes[J.plane];
     const long long n = (long long)P.w * P.h;
@@ -459,6 +458,25 @@ template <typename R> __device__ __forceinline__ R to_r(double x);
 template <> __device__ __forceinline__ float to_r<float>(double x) { return f32_of(x); }
 template <> __device__ __forceinline__ double to_r<double>(double x) { return x; }
 
+// One sub-pixel's bin and split in FP64, as the reference computes them (the
+// FP64 form's every sub-pixel, the FP32 form's near-boundary ones); a call, so
+// that the FP32 form's common path issues none of these FP64 instructions.
+template <typename R> struct RadonSplit {
+    int rl;
+    R pix, pl;
+};
+template <typename R>
+static __device__ __noinline__ RadonSplit<R> radon_exact(int kx, int ky, double cs, double sn, int rFirst, double pd) {
+    const double xT = (double)kx * 0.25, yT = (double)ky * 0.25;
+    const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
+    RadonSplit<R> r;
+    r.rl = (int)ri;
+    const double pdq = pd * 0.25;
+    r.pix = to_r<R>(pdq);
+    r.pl = (R)__dmul_rn(pdq, __dadd_rn(__dsub_rn(1.0, ri), (double)r.rl));
+    return r;
+}
+
 // x == 0.0 (either sign) from the bits, off the FP64 pipe
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
@@ -545,12 +563,10 @@ __global__ void __launch_bounds__(1024) k_radon(const double *__restrict__ arena
                 }
             }
             if (exact) {
-                const double xT = (double)kx * 0.25, yT = (double)ky * 0.25;
-                const double ri = __dadd_rn(__dsub_rn(__dmul_rn(xT, cs), (double)rFirst), __dmul_rn(yT, sn));
-                rl = (int)ri;
-                const double pdq = pd * 0.25;
-                pix = to_r<R>(pdq);
-                pl = (R)__dmul_rn(pdq, __dadd_rn(__dsub_rn(1.0, ri), (double)rl));
+                const RadonSplit<R> e = radon_exact<R>(kx, ky, cs, sn, rFirst, pd);
+                rl = e.rl;
+                pix = e.pix;
+                pl = e.pl;
             }
             if (rl != cur) {
                 if (cur >= 0) {

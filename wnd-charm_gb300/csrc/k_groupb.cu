@@ -182,6 +182,13 @@ __global__ void k_zern_finish(const FJob *__restrict__ jobs, const double *__res
 // of ZCHUNK_DF pixels per block; the block's sums are reduced in pairs within
 // each warp and in FP64 across the warps.
 #define ZCHUNK_DF 16384
+// the FP64 kernel's disc test, for the pixels near the rim or the centre (a
+// call, so that the common path issues none of its FP64 instructions)
+static __device__ __noinline__ bool zern_in_disc(long long xx, long long yy, double cx, double cy, double inv_rad) {
+    const double xe = __dsub_rn((double)(xx + 1), cx) * inv_rad, ye = __dsub_rn((double)(yy + 1), cy) * inv_rad;
+    const double r = sqrt(__dadd_rn(__dmul_rn(xe, xe), __dmul_rn(ye, ye)));
+    return !(r < DBL_EPSILON || r > 1.0);
+}
 template <int HALF>
 __global__ void __launch_bounds__(256) k_zern_cmom_df(const double *__restrict__ arena, const Plane *__restrict__ planes,
                                                       const FJob *__restrict__ jobs, const double *__restrict__ mom,
@@ -207,14 +214,8 @@ __global__ void __launch_bounds__(256) k_zern_cmom_df(const double *__restrict__
             const df x = df_mul(df_sub({(float)(xx + 1), 0.f}, cxd), ird);
             const df y = df_mul(df_sub({(float)(yy + 1), 0.f}, cyd), ird);
             const df r2 = df_add(df_mul(x, x), df_mul(y, y));
-            bool in;
-            if (fabsf(r2.hi - 1.f) < 1e-6f || r2.hi < 1e-20f) {
-                const double xe = __dsub_rn((double)(xx + 1), cx) * inv_rad, ye = __dsub_rn((double)(yy + 1), cy) * inv_rad;
-                const double r = sqrt(__dadd_rn(__dmul_rn(xe, xe), __dmul_rn(ye, ye)));
-                in = !(r < DBL_EPSILON || r > 1.0);
-            } else {
-                in = r2.hi < 1.f;
-            }
+            const bool in = (fabsf(r2.hi - 1.f) < 1e-6f || r2.hi < 1e-20f) ? zern_in_disc(xx, yy, cx, cy, inv_rad)
+                                                                            : r2.hi < 1.f;
             if (!in) continue;
             const df r = df_sqrt(r2);
             df q[JMAX + 1];

@@ -44,6 +44,13 @@ __global__ void __launch_bounds__(1024) k_tam_prefix(const double *__restrict__ 
     }
 }
 
+// v / cnt for the clipped windows (and the quotients that leave the normal
+// range): a call, so that the common path issues none of its FP64 instructions
+static __device__ __noinline__ double mean_slow(double v, long long cnt) {
+    if ((cnt & (cnt - 1)) == 0) return __dmul_rn(v, __longlong_as_double((long long)(1023 - (__ffsll(cnt) - 1)) << 52));
+    return v / (double)cnt;
+}
+
 // efficientLocalMean (tamura.cpp:106-139)
 __device__ __forceinline__ double local_mean(const double *__restrict__ S, int W, int H, long long x, long long y, long long k) {
     const long long k2 = k / 2;
@@ -67,9 +74,8 @@ __device__ __forceinline__ double local_mean(const double *__restrict__ S, int W
         const int E = (int)((b >> 52) & 0x7ff);
         if (E > e && E != 0x7ff) return __longlong_as_double(b - ((long long)e << 52));
         if ((b & 0x7fffffffffffffffLL) == 0) return v;
-        return __dmul_rn(v, __longlong_as_double((long long)(1023 - e) << 52));
     }
-    return v / (double)cnt;
+    return mean_slow(v, cnt);
 }
 
 // |a - b| as bits (a nonnegative double orders as its bit pattern)
@@ -79,6 +85,26 @@ __device__ __forceinline__ long long absdiff_bits(double a, double b) {
 // a finite double below 2^1022 in magnitude (2x is exact and finite)
 __device__ __forceinline__ bool tame(double v) {
     return ((__double_as_longlong(v) >> 52) & 0x7ff) < 0x7fd;
+}
+
+// the 3x3 correlations term by term (non-finite or huge neighbourhoods); a
+// call, so that the common path issues none of its FP64 instructions
+static __device__ __noinline__ double2 tam_dir_slow(const double *__restrict__ nrm, int x, int y, int W, int H) {
+    const double fH[3][3] = {{-1, 2, 1}, {-2, 0, 2}, {-1, -2, -1}};
+    const double fV[3][3] = {{1, 0, 0}, {0, 0, 0}, {-1, 0, 0}};
+    double dH = 0, dV = 0;
+    for (int a = -1; a <= 1; a++) {
+        const int xx = x + a;
+        if (xx < 0 || xx >= W) continue;
+        for (int b = -1; b <= 1; b++) {
+            const int yy = y + b;
+            if (yy < 0 || yy >= H) continue;
+            const double v = nrm[(long long)yy * W + xx];
+            dH = __dadd_rn(dH, __dmul_rn(fH[b + 1][a + 1], v));
+            dV = __dadd_rn(dV, __dmul_rn(fV[b + 1][a + 1], v));
+        }
+    }
+    return make_double2(dH, dV);
 }
 
 #define TAM_TILE 1024
@@ -130,7 +156,6 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
         // products are exact and x + 2v is one rounding, so the same sums take
         // fused multiply-adds over the nonzero taps, in the same order.
         const double fH[3][3] = {{-1, 2, 1}, {-2, 0, 2}, {-1, -2, -1}};
-        const double fV[3][3] = {{1, 0, 0}, {0, 0, 0}, {-1, 0, 0}};
         double nb[3][3];
         bool fast = true;
         for (int a = -1; a <= 1; a++)
@@ -148,17 +173,9 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
                     if (fH[b][a] != 0) dH = __fma_rn(fH[b][a], nb[b][a], dH);
             dV = __dsub_rn(nb[0][0], nb[2][0]);
         } else {
-            for (int a = -1; a <= 1; a++) {
-                const int xx = x + a;
-                if (xx < 0 || xx >= W) continue;
-                for (int b = -1; b <= 1; b++) {
-                    const int yy = y + b;
-                    if (yy < 0 || yy >= H) continue;
-                    const double v = nb[b + 1][a + 1];
-                    dH = __dadd_rn(dH, __dmul_rn(fH[b + 1][a + 1], v));
-                    dV = __dadd_rn(dV, __dmul_rn(fV[b + 1][a + 1], v));
-                }
-            }
+            const double2 d = tam_dir_slow(nrm, x, y, W, H);
+            dH = d.x;
+            dV = d.y;
         }
         // dH >= 1e-4 and the running min / max of phi (phi is +0 or positive, or
         // NaN, which fmin / fmax skip) as comparisons of bit patterns

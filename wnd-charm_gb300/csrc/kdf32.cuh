@@ -25,6 +25,12 @@ __device__ __forceinline__ df df_from_double(double x) {
     const float h = __double2float_rn(x);
     return {h, __double2float_rn(x - (double)h)};
 }
+// The rare cases of df_split / f32_of take conversions (FP64-pipe
+// instructions), in calls that are not inlined, so that the common path
+// carries none of them (a short inlined branch may be predicated and issued
+// on every pass).
+static __device__ __noinline__ df df_split_slow(double x) { return df_from_double(x); }
+static __device__ __noinline__ float f32_slow(double x) { return __double2float_rn(x); }
 // The same pair from the double's bits, off the FP64 pipe (conversions from
 // and to double issue there): hi = the mantissa rounded to 24 bits (nearest,
 // ties to even), lo = the 29-bit remainder (exact as an integer, rounded once
@@ -34,7 +40,7 @@ __device__ __forceinline__ df df_split(double x) {
     const long long b = __double_as_longlong(x);
     if ((b & 0x7fffffffffffffffLL) == 0) return {0.f, 0.f};
     const int ef = (int)((b >> 52) & 0x7ff) - 1023 + 127;
-    if (ef < 53 || ef > 254) return df_from_double(x);
+    if (ef < 53 || ef > 254) return df_split_slow(x);
     const unsigned low = (unsigned)(b & 0x1fffffffLL);
     const unsigned top = ((unsigned)ef << 23) | (unsigned)((b >> 29) & 0x7fffff);
     const bool up = low > 0x10000000u || (low == 0x10000000u && (top & 1u));
@@ -51,7 +57,7 @@ __device__ __forceinline__ float f32_of(double x) {
     const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
     if ((b & 0x7fffffffffffffffLL) == 0) return __uint_as_float(sign);
     const int ef = (int)((b >> 52) & 0x7ff) - 1023 + 127;
-    if (ef < 1 || ef > 254) return __double2float_rn(x);
+    if (ef < 1 || ef > 254) return f32_slow(x);
     const unsigned low = (unsigned)(b & 0x1fffffffLL);
     const unsigned top = ((unsigned)ef << 23) | (unsigned)((b >> 29) & 0x7fffff);
     const bool up = low > 0x10000000u || (low == 0x10000000u && (top & 1u));

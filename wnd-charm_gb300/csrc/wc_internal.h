@@ -54,6 +54,7 @@ struct TJob {
 // Optional per-stage timing with CUDA events on the engine's stream.
 struct Prof {
     bool on = false;
+    bool serial = false;  // every lane on the engine's stream: each stage timed alone
     struct Mark {
         std::string name;
         cudaEvent_t a, b;

@@ -275,8 +275,10 @@ class Engine(object):
     def launches(self):
         return lib().wc_engine_launch_count(self._h)
 
-    def profile(self, on=True):
-        check(lib().wc_engine_profile(self._h, 1 if on else 0))
+    def profile(self, on=True, serial=False):
+        """Per-stage timing on (serial: the lanes run one after another, so each
+        stage's time is its own rather than its share of a concurrent step)."""
+        check(lib().wc_engine_profile(self._h, (2 if serial else 1) if on else 0))
 
     def profile_report(self):
         buf = ctypes.create_string_buffer(1 << 16)

@@ -370,6 +370,13 @@ def main():
     roof = {"stage": dom[0], "stage_ms_alone_per_step": dom[1], "stage_share": dom[1] / tot_prof,
             "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
             "peak_source": "measured" if peaks else "fallback"}
+    # DRAM bytes per image of the stage's kernels from one ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum over the four k_cheb_gemm launches of a 16-image step,
+    # profiles/cheb_gemm_long_plan_512_batch16_full.md), scaled by the images of this step
+    traffic_per_image = {"Chebyshev": 287e6 / 16}
+    if dom[0] in traffic_per_image:
+        roof["traffic"] = traffic_per_image[dom[0]] * B
+        roof["traffic_unit"] = "bytes per step (ncu, batch 16, scaled by images)"
     if work:
         kind, amt = work
         sec = dom[1] / 1000.0

@@ -1084,25 +1084,10 @@ __device__ void har_schur_df(df *__restrict__ A, const int n, float *__restrict_
 }
 
 // The mixed form's Hessenberg reduction: the reflectors and updates of
-// k_har_hess in pairs of floats (FP32 pipe) on Q from k_har_q_df, each
-// column's vector scaled by a power of two
-// before its squares are summed (exact; keeps them within float's exponent
-// range).  The matrix stays in pairs for har_schur_df.
-__device__ __forceinline__ float block_max_f(float v, float *sh) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
-    __syncthreads();
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    float r = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.f;
-    if (wid == 0)
-        for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_down_sync(0xffffffffu, r, o));
-    if (threadIdx.x == 0) sh[0] = r;
-    __syncthreads();
-    r = sh[0];
-    __syncthreads();
-    return r;
-}
+// k_har_hess in pairs of floats (FP32 pipe) on Q from k_har_q_df; a column
+// whose largest entry is far from 1 is scaled by a power of two before its
+// squares are summed (exact; keeps them within float's exponent range).  The
+// matrix stays in pairs for har_schur_df.
 __device__ __forceinline__ df block_sum_df(df v, df *sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int o = 16; o > 0; o >>= 1) v = df_add(v, {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
@@ -1119,6 +1104,38 @@ __device__ __forceinline__ df block_sum_df(df v, df *sh) {
     return r;
 }
 
+// max of the floats m and sum of the pairs q over the block (fixed tree); m is
+// replaced by the block's max, the sum returned; valid in every thread
+__device__ __forceinline__ df block_max_sum(float &m, df q, float *shm, df *shq) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        q = df_add(q, {__shfl_down_sync(0xffffffffu, q.hi, o), __shfl_down_sync(0xffffffffu, q.lo, o)});
+    }
+    __syncthreads();
+    if (lane == 0) {
+        shm[wid] = m;
+        shq[wid] = q;
+    }
+    __syncthreads();
+    float rm = (threadIdx.x < nw) ? shm[threadIdx.x] : 0.f;
+    df rq = (threadIdx.x < nw) ? shq[threadIdx.x] : df{0.f, 0.f};
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) {
+            rm = fmaxf(rm, __shfl_down_sync(0xffffffffu, rm, o));
+            rq = df_add(rq, {__shfl_down_sync(0xffffffffu, rq.hi, o), __shfl_down_sync(0xffffffffu, rq.lo, o)});
+        }
+    if (threadIdx.x == 0) {
+        shm[0] = rm;
+        shq[0] = rq;
+    }
+    __syncthreads();
+    m = shm[0];
+    rq = shq[0];
+    __syncthreads();
+    return rq;
+}
+
 __global__ void __launch_bounds__(256) k_har_hess_df(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
     __shared__ df v[256], ess[256], tess[256], red[32];
     __shared__ float redf[32];
@@ -1132,21 +1149,31 @@ __global__ void __launch_bounds__(256) k_har_hess_df(const HarJob *__restrict__ 
     const df zero = {0.f, 0.f};
     for (int i = 0; i < n - 1; i++) {
         const int rem = n - i - 1;
+        // the largest entry and the unscaled tail sum in one reduction; the
+        // scaled sum is formed only when the largest entry leaves [2^-40, 2^40]
+        // (inside it the sum of squares and its low parts stay well within
+        // float's normal range, as accurate as the scaled sum)
         float m = 0.f;
+        df q = zero;
         for (int k = threadIdx.x; k < rem; k += blockDim.x) {
             const df x = A[(long long)(i + 1 + k) * n + i];
             v[k] = x;
             m = fmaxf(m, fabsf(x.hi));
+            if (k > 0) q = df_fma(x, x, q);
         }
-        m = block_max_f(m, redf);
+        df tail = block_max_sum(m, q, redf, red);
         float down = 1.f, up = 1.f;
         if (m != 0.f) hh_scale(m, down, up);
-        df q = zero;
-        for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) {
-            const df w = df_scale(v[k], down);
-            q = df_fma(w, w, q);
+        if (m != 0.f && (m < 0x1p-40f || m > 0x1p40f)) {
+            q = zero;
+            for (int k = 1 + threadIdx.x; k < rem; k += blockDim.x) {
+                const df w = df_scale(v[k], down);
+                q = df_fma(w, w, q);
+            }
+            tail = block_sum_df(q, red);
+        } else {
+            tail = df_scale(tail, __fmul_rn(down, down));
         }
-        const df tail = block_sum_df(q, red);
         if (threadIdx.x == 0) {  // makeHouseholder (Householder.h:65-90) on the scaled vector
             const df c0 = df_scale(v[0], down);
             if (rem == 1 || tail.hi == 0.f) {

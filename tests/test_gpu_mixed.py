@@ -57,6 +57,25 @@ def test_mixed_deterministic(eng, long_plan):
     np.testing.assert_array_equal(a, b)
 
 
+def test_serialised_profile_same_features(eng, long_plan):
+    """Engine.profile(serial=True) runs every lane on the engine's stream:
+    the same features, and a time for every stage."""
+    imgs = images(seed=47, sizes=[(96, 96), (64, 80)])
+    a = eng.extract(long_plan, imgs)
+    eng.profile(True, serial=True)
+    try:
+        b = eng.extract(long_plan, imgs)
+        rep = {name: ms for name, ms, _ in eng.profile_report()}
+    finally:
+        eng.profile(False)
+    np.testing.assert_array_equal(a, b)
+    for stage in ("Chebyshev", "Fourier", "Haralick Textures", "Haralick: real Schur (f14)", "Tamura Textures",
+                  "Zernike Coefficients", "PixStats+Gini (sort)"):
+        assert rep.get(stage, 0.0) > 0.0, stage
+    c = eng.extract(long_plan, imgs)  # and back to the lanes
+    np.testing.assert_array_equal(a, c)
+
+
 def test_512_workload_both_forms(long_plan):
     """Two 512 x 512 images of the benchmark workload through both forms, against
     the oracle (run on two host threads)."""

@@ -4,9 +4,9 @@
 // out(y, x) = out(H - y, (W - x) mod W), no scaling, no shift.
 //
 // 1-D transforms are Stockham mixed-radix DFTs in shared memory, several
-// lines per CTA; any length up to kMaxFFT (radices 8, 4, 2, then odd primes;
-// a prime factor p costs O(p) per output).  Twiddles exp(-2 pi i k / n) come
-// from an FP64 table computed on the host.
+// lines per CTA; any length up to kMaxFFT (radices 8, 4, 2 as butterflies,
+// then odd primes as direct DFTs, O(p) per output).  Twiddles
+// exp(-2 pi i k / n) come from an FP64 table computed on the host.
 #include <cmath>
 
 #include "kcommon.cuh"

@@ -3,7 +3,11 @@
 // tw[k] = exp(-2 pi i k / n)).  Shared by the Fourier transform node and the
 // Gabor FFT convolution; templated on the element type (FP64 form, and FP32
 // for the mixed form's Gabor filtering) and on the twiddles' type (FP64, or
-// the FP64 twiddles rounded to FP32 once, in shared memory).
+// the FP64 twiddles rounded to FP32 once, in shared memory).  Radices 2, 4
+// and 8 are butterflies (radix 8 as two radix-4 butterflies and the factors
+// 1, (1-i)/sqrt2, -i, -(1+i)/sqrt2); an odd prime is a direct DFT over the
+// twiddle table.  The operations and their order are the oracle's DFT's
+// (oracle/fft_cpu.h), so the FP64 Fourier planes agree with it bit for bit.
 #pragma once
 #include "kernels.h"
 
@@ -21,6 +25,40 @@ __device__ __forceinline__ cpx<R> cmul(cpx<R> a, cpx<R> b) {
 template <typename R>
 __device__ __forceinline__ cpx<R> cadd(cpx<R> a, cpx<R> b) {
     return {a.x + b.x, a.y + b.y};
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> csub(cpx<R> a, cpx<R> b) {
+    return {a.x - b.x, a.y - b.y};
+}
+// X0 = a0 + a2, X1 = a1 - i a3, X2 = a0 - a2, X3 = a1 + i a3 with a0 = v0 + v2,
+// a1 = v0 - v2, a2 = v1 + v3, a3 = v1 - v3 (W = -i)
+template <typename R>
+__device__ __forceinline__ void bfly4(cpx<R> v0, cpx<R> v1, cpx<R> v2, cpx<R> v3, cpx<R> *X) {
+    const cpx<R> a0 = cadd(v0, v2), a1 = csub(v0, v2), a2 = cadd(v1, v3), a3 = csub(v1, v3);
+    X[0] = cadd(a0, a2);
+    X[1] = {a1.x + a3.y, a1.y - a3.x};
+    X[2] = csub(a0, a2);
+    X[3] = {a1.x - a3.y, a1.y + a3.x};
+}
+// E = DFT4 of the even inputs, O = DFT4 of the odd ones; X_q = E_q + W8^q O_q,
+// X_{q+4} = E_q - W8^q O_q, W8 = (1 - i) / sqrt2
+template <typename R>
+__device__ __forceinline__ void bfly8(const cpx<R> *v, cpx<R> *X) {
+    const R c = (R)0.70710678118654752440;
+    cpx<R> E[4], O[4];
+    bfly4(v[0], v[2], v[4], v[6], E);
+    bfly4(v[1], v[3], v[5], v[7], O);
+    const cpx<R> t1 = {c * (O[1].x + O[1].y), c * (O[1].y - O[1].x)};
+    const cpx<R> t2 = {O[2].y, -O[2].x};
+    const cpx<R> t3 = {c * (O[3].y - O[3].x), -(c * (O[3].x + O[3].y))};
+    X[0] = cadd(E[0], O[0]);
+    X[4] = csub(E[0], O[0]);
+    X[1] = cadd(E[1], t1);
+    X[5] = csub(E[1], t1);
+    X[2] = cadd(E[2], t2);
+    X[6] = csub(E[2], t2);
+    X[3] = cadd(E[3], t3);
+    X[7] = csub(E[3], t3);
 }
 template <typename R, typename T>
 __device__ __forceinline__ cpx<R> twid(const cpx<T> *tw, long long i) {
@@ -53,10 +91,25 @@ static __device__ void stockham_stage(const cpx<R> *src, cpx<R> *dst, int lines,
                     v[r] = a;
                 }
             }
-            for (int q = 0; q < p; q++) {
-                C acc = v[0];
-                for (int r = 1; r < p; r++) acc = cadd(acc, cmul(v[r], twid<R, T>(tw, (long long)((r * q) % p) * twstep_q)));
-                d[obase + q * Ns] = acc;
+            if (p == 2) {
+                d[obase] = cadd(v[0], v[1]);
+                d[obase + Ns] = csub(v[0], v[1]);
+            } else if (p == 4) {
+                C X[4];
+                bfly4(v[0], v[1], v[2], v[3], X);
+#pragma unroll
+                for (int q = 0; q < 4; q++) d[obase + q * Ns] = X[q];
+            } else if (p == 8) {
+                C X[8];
+                bfly8(v, X);
+#pragma unroll
+                for (int q = 0; q < 8; q++) d[obase + q * Ns] = X[q];
+            } else {
+                for (int q = 0; q < p; q++) {
+                    C acc = v[0];
+                    for (int r = 1; r < p; r++) acc = cadd(acc, cmul(v[r], twid<R, T>(tw, (long long)((r * q) % p) * twstep_q)));
+                    d[obase + q * Ns] = acc;
+                }
             }
         } else {
             for (int q = 0; q < p; q++) {

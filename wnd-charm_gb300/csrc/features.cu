@@ -71,7 +71,10 @@ int features_check(cudaStream_t st, int *dev_err) {
         cudaMemcpyToSymbolAsync(g_dev_err, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
         cudaStreamSynchronize(st);
     }
-    *dev_err = v;
+    int vo = 0;
+    if (objects_err_take(st, &vo))
+        return set_err(WC_ERR_CUDA, "reading the device error word failed: %s", cudaGetErrorString(cudaGetLastError()));
+    *dev_err = v ? v : vo;
     return WC_OK;
 }
 
@@ -283,8 +286,7 @@ int features_prepare(FeatureSetup &fs) {
         long long maxpix = 0;
         for (int a : {A_OBJ, A_INVOBJ})
             for (auto &j : fj[a]) all.push_back(j);
-        size_t zero_begin = fs.ws_take(0), zero_bytes = 0;
-        (void)zero_bytes;
+        size_t zero_begin = fs.ws_take(0);
         // zeroed block first: area (u32), xm, ym (u64) per job, accumulators
         std::vector<size_t> zoff;
         for (auto &j : all) {

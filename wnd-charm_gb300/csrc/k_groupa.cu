@@ -22,7 +22,24 @@
 
 namespace wc {
 
-extern __device__ int g_dev_err;
+// The error word of this file's kernels (a device symbol is private to its
+// translation unit without relocatable device code, so it is not the one in
+// features.cu): the union-find loops set it when their iteration cap runs
+// out; objects_err_take reads and clears it for features_check.
+__device__ int g_dev_err_ob = 0;
+
+int objects_err_take(cudaStream_t st, int *v) {
+    *v = 0;
+    if (cudaMemcpyFromSymbolAsync(v, g_dev_err_ob, sizeof(int), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return -1;
+    if (*v) {
+        const int z = 0;
+        cudaMemcpyToSymbolAsync(g_dev_err_ob, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+        cudaStreamSynchronize(st);
+    }
+    return 0;
+}
 
 // ---------------------------------------------------------------- Edge features
 __global__ void k_ef_prewitt(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
@@ -150,7 +167,7 @@ __global__ void __launch_bounds__(1024) k_ob_otsu(const double *__restrict__ are
     __syncthreads();
     if (threadIdx.x == 0) {
         const double wh = (double)(unsigned)(P.w * P.h);
-        double om = hist[0] / wh, my = 0.0;
+        double om = hist[0] / wh;
         // myu[L-1] first (sequential, as the reference accumulates the arrays)
         double om_i = om, my_i = 0.0, myL = 0.0;
         for (int i = 1; i < 1024; i++) myL = myL + i * (hist[i] / wh);
@@ -167,7 +184,6 @@ __global__ void __launch_bounds__(1024) k_ob_otsu(const double *__restrict__ are
             if (s > max_sigma) { max_sigma = s; th = i; }
         }
         (void)om;
-        (void)my;
         thr[blockIdx.x] = (((double)th / (double)(1023)) * (S.mx - S.mn)) + S.mn;
     }
 }
@@ -178,7 +194,7 @@ __device__ __forceinline__ int uf_find(volatile int *L, int x, long long cap) {
         if (p == x) return x;
         x = p;
     }
-    atomicExch(&g_dev_err, 22);
+    atomicExch(&g_dev_err_ob, 22);
     return x;
 }
 
@@ -192,7 +208,7 @@ __device__ void uf_unite(int *L, int a, int b, long long cap) {
         if (old == a) return;
         a = old;
     }
-    atomicExch(&g_dev_err, 23);
+    atomicExch(&g_dev_err_ob, 23);
 }
 
 // stage 0: init labels; 1: unions with the 4 earlier 8-neighbours; 2: flatten

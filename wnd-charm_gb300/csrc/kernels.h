@@ -98,6 +98,8 @@ struct OBJob {
     int pad_;
     long long src_ws, lab_ws, area_ws, xm_ws, ym_ws, roots_ws, keys_ws, tmp_ws, dist_ws;  // doubles offsets
 };
+// reads and clears the object kernels' error word (0 = ok; else the code); -1 if the copy fails
+int objects_err_take(cudaStream_t st, int *v);
 void launch_objects(Ctx &c, const double *arena, const Plane *planes, const PlaneStats *stats, const FJob *jobs, int njobs,
                     long long maxpix, const OBJob *oj, double *ws, const Plane *inv_planes, PlaneStats *inv_stats,
                     double *thr, unsigned long long *acc, double *feat);

@@ -69,6 +69,25 @@ def test_transforms(oracle, name):
         np.testing.assert_allclose(got, exp, rtol=1e-11, atol=1e-9 * np.abs(exp).max())
 
 
+@pytest.mark.parametrize("h,w", [(64, 64), (48, 40), (37, 53), (60, 70), (30, 29)])
+def test_fourier_against_numpy(oracle, h, w):
+    """The oracle's DFT (radix-2/4/8 butterflies, odd primes direct; the GPU's
+    Fourier node reproduces it bit for bit): |DFT| equals numpy's |fft2| to
+    FP64 accuracy, for power-of-two, odd and prime sides."""
+    import ctypes
+    from conftest import D
+    rng = np.random.default_rng(h * 100 + w)
+    img = np.ascontiguousarray(rng.integers(0, 4096, size=(h, w)), dtype=np.float64)
+    out = np.zeros(4 * img.size + 4096)
+    ow, oh = ctypes.c_int(), ctypes.c_int()
+    assert oracle.wco_transform(b"Fourier", img.ctypes.data_as(D), w, h, out.ctypes.data_as(D),
+                                ctypes.byref(ow), ctypes.byref(oh)) == 0
+    got = out[: ow.value * oh.value].reshape(oh.value, ow.value)
+    exp = np.abs(np.fft.fft2(img))
+    assert got.shape == exp.shape
+    np.testing.assert_allclose(got, exp, rtol=1e-12, atol=1e-12 * exp.max())
+
+
 def test_wnd_classify_fixture(oracle):
     """test01-classify.pl: classify -l test-l.fit test-l.fit (3-decimal table)."""
     g = golden("reference_wnd.npz")

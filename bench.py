@@ -37,6 +37,10 @@ import numpy as np  # noqa: E402
 
 METRIC = "images/sec, 2919-feature set, 512^2 uint16: mixed vs FP64 GPU form at stated tol"
 IMG = 512
+WORKLOAD = "long plan (2919 features), %dx%d uint16 12-bit blob+grating, 4 classes, seed 1" % (IMG, IMG)
+# the config object both arms print (the arm-specific set-up goes in top-level keys)
+CONFIG = {"workload": WORKLOAD, "parallelism": "replicas",
+          "l2": "GPU arm: flushed (256 MB write) between timed steps; CPU arm: not applicable"}
 
 
 def clocks_sampler(stop, out):
@@ -99,9 +103,14 @@ def cpu_baseline(images, nthreads):
 def run_reference(args, rank, world):
     if rank != 0:
         return
+    if args.workload == "short":
+        return run_short(args, reference=True)
+    if args.workload == "wnd":
+        return run_wnd(args, reference=True)
     nthreads = os.cpu_count() or 1
-    # each timed step: one image per host thread, bounded so the run stays within minutes
-    per_step = max(1, min(nthreads, int(nthreads * 150.0 / (max(1, args.steps) * 14.0))))
+    # each timed step: one image per host thread on every host thread (the
+    # reference's own model: one single-threaded process per image per core)
+    per_step = nthreads
     warm = make_images(1, seed=99)
     for _ in range(args.warmup):
         cpu_baseline([w[:64, :64] for w in warm], 1)
@@ -115,24 +124,23 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": v, "unit": "images/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": "long plan (2919 features), %dx%d uint16 12-bit blob+grating, seed 1" % (IMG, IMG),
-                       "images_per_step": per_step},
-            "cpu_baseline": {"value": v, "unit": "images/s", "cores": min(nthreads, per_step), "kind": "port",
+            "impl": "reference", "config": dict(CONFIG), "images_per_step": per_step,
+            "cpu_baseline": {"value": v, "unit": "images/s", "cores": nthreads, "kind": "port",
                              "sample": "%d images of %dx%d per step, one per host thread" % (per_step, IMG, IMG)},
             "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def stage_work(name, B, precision="mixed"):
+def stage_work(name, B, precision="mixed", f14="exact"):
     """Algorithmic work per step of a stage on the long plan at 512^2, for the
     roofline of the dominant stage: (kind, amount) with kind 'bytes' (HBM),
     'fp64' (FP64 flops) or 'flops'; None where no model applies."""
     px = IMG * IMG
     planes_c = 12  # group C runs on 12 planes per image
     table = {
-        # read each plane once (8 B/px) for every pass the family needs
-        "Tamura Textures": ("bytes", B * planes_c * px * 8 * 4),
+        # FP64 instructions: the coarseness search's local means and the
+        # direction quotient and atan, about 45 FP64 operations per pixel
+        "Tamura Textures": ("fp64", B * planes_c * px * 45),
         "Gabor Textures": ("bytes", B * px * 8 * 2),
         # three 2-D Chebyshev transforms per image (of the image, of its Fourier
         # and of its wavelet plane), each two 512^3 products; a multiply and an
@@ -143,13 +151,14 @@ def stage_work(name, B, precision="mixed"):
         "Fractal Features": ("bytes", B * planes_c * px * 8),
         "PixStats+Gini (sort)": ("bytes", B * planes_c * px * 8 * 16),
     }
-    if precision == "fp64":
+    if precision == "fp64" or f14 == "exact":
         # FP64 operations of Q, the Hessenberg reduction and the real-Schur QR for
         # f14, counted by an instrumented run of the oracle on this workload
         # (about 1.3 G per 512^2 image: 10/3 Ng^3 + 9 per touched element per
         # Francis step + 3 per nonzero Q term, summed over the 48 matrices); the
-        # mixed form computes them in pairs of floats
+        # mixed form's pairs-of-floats chain computes them on the FP32 pipe
         table["Haralick Textures"] = ("fp64", B * 1.3e9)
+    if precision == "fp64":
         # Zernike moments (the mixed form sums them in pairs of floats)
         table["Zernike Coefficients"] = ("fp64", B * 8 * px * 460)
     return table.get(name)
@@ -228,6 +237,8 @@ def main():
     ap.add_argument("--batch", type=int, default=128,
                     help="images per step (128: a quarter of the 4 x 128-image workload)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--f14", default="exact", choices=["exact", "pairs"],
+                    help="mixed form's Haralick f14 chain: exact (FP64, bit-identical to the oracle) or pairs of floats")
     ap.add_argument("--per-image", type=int, default=8, help="images timed one per call in the FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP64 comparison forms")
@@ -256,6 +267,7 @@ def main():
     nf = plan.n_features
     stream = torch.cuda.Stream()
     eng = wndcharm.Engine(local, args.precision)
+    eng.set_option("f14_exact", 1 if args.f14 == "exact" else 0)
     eng.set_stream(stream.cuda_stream)
     imgs = make_images(B, seed=1 + rank)
     host = torch.from_numpy(np.stack(imgs).view(np.int16)).pin_memory()
@@ -366,17 +378,19 @@ def main():
         peaks = json.load(open(pk_path))
     hbm = peaks.get("hbm_gbs", 6800.0)
     tfl = peaks.get("bf16_tflops", 1900.0)
-    work = stage_work(dom[0], B, args.precision)
+    work = stage_work(dom[0], B, args.precision, args.f14)
     roof = {"stage": dom[0], "stage_ms_alone_per_step": dom[1], "stage_share": dom[1] / tot_prof,
             "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
             "peak_source": "measured" if peaks else "fallback"}
-    # DRAM bytes per image of the stage's kernels from one ncu capture (dram__bytes_read.sum +
-    # dram__bytes_write.sum over the four k_cheb_gemm launches of a 16-image step,
-    # profiles/cheb_gemm_long_plan_512_batch16_full.md), scaled by the images of this step
+    # DRAM bytes per image of the stage's kernels: a constant taken from one ncu
+    # capture (dram__bytes_read.sum + dram__bytes_write.sum over the four
+    # k_cheb_gemm launches of a 16-image step of this workload), scaled by the
+    # images of this step; not measured in this run
     traffic_per_image = {"Chebyshev": 287e6 / 16}
     if dom[0] in traffic_per_image:
         roof["traffic"] = traffic_per_image[dom[0]] * B
-        roof["traffic_unit"] = "bytes per step (ncu, batch 16, scaled by images)"
+        roof["traffic_source"] = ("constant: one ncu capture of k_cheb_gemm at batch 16 (287 MB DRAM read+write), "
+                                  "scaled by images; bytes per step")
     if work:
         kind, amt = work
         sec = dom[1] / 1000.0
@@ -394,7 +408,7 @@ def main():
     # the whole step against its floor: the FP64 families' algorithmic work at the
     # measured FP64 peak plus one read of every plane per scan family at HBM speed
     p64 = roof["peak"] if roof.get("bound") == "fp64" else fp64_peak_tflops(dev)
-    fl = sum(w[1] for w in (stage_work(n, B, args.precision) for n in ("Haralick Textures", "Chebyshev",
+    fl = sum(w[1] for w in (stage_work(n, B, args.precision, args.f14) for n in ("Haralick Textures", "Chebyshev",
                                                                         "Zernike Coefficients")) if w)
     by = sum(stage_work(n, B)[1] for n in ("Tamura Textures", "Gabor Textures", "Comb Moments", "Radon Coefficients",
                                             "Fractal Features", "PixStats+Gini (sort)"))
@@ -404,13 +418,14 @@ def main():
 
     value = world * B * args.steps / t_dev
     e2e = world * B * args.steps / t_e2e
-    line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+    line = {"metric": METRIC, "value": value, "unit": "images/s",
+            "mixed_vs_fp64_per_image": forms["mixed_vs_fp64_per_image"] if forms else None,
+            "mixed_vs_fp64_batched": forms["mixed_vs_fp64_batched"] if forms else None,
+            "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": "long plan (2919 features), %dx%d uint16 12-bit blob+grating, 4 classes, seed 1"
-                       % (IMG, IMG), "images_per_step": B, "precision_form": args.precision,
-                       "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas"},
+            "data": "synthetic", "config": dict(CONFIG), "images_per_step": B, "precision_form": args.precision,
+            "f14_chain": args.f14,
             "e2e": {"value": e2e, "unit": "images/s", "h2d_bytes_per_step": B * IMG * IMG * 2,
                     "d2h_bytes_per_step": B * nf * 8},
             "gpu_launches": int(launches),
@@ -437,14 +452,15 @@ def main():
                 r0, g0, w0 = errs.get(k, (0.0, 0.0, ""))
                 errs[k] = (max(r0, r), max(g0, g), w if g >= g0 else w0)
             cmp = compare_mixed if args.precision == "mixed" else compare
-            if cmp(mixed_rows[i], ref[i], names):
+            # f14: bit-identical to the oracle through the exact chain; range-checked
+            # for the pairs-of-floats chain (its agreement is reported below)
+            if cmp(mixed_rows[i], ref[i], names, f14="exact" if args.f14 == "exact" else "range"):
                 ok = False
-        # f14 (Haralick in-group 16, 17) is range-checked only; report how often it agrees anyway
-        from parity import F14, group_of, index_of
-        f14i = np.array([i for i, nm in enumerate(names) if group_of(nm).startswith("Haralick") and index_of(nm) in F14])
-        a14, b14 = mixed_rows[:ncpu][:, f14i], ref[:ncpu][:, f14i]
-        f14_agree = float(np.mean(np.abs(a14 - b14) <= 1e-6 * np.maximum(np.abs(b14), 1e-12)))
+        from parity import f14_columns, f14_errors
+        f14i = f14_columns(names)
+        f14_agree, f14_abs, f14_rel = f14_errors(mixed_rows[:ncpu][:, f14i], ref[:ncpu][:, f14i])
         line["error_vs_oracle"] = {"images": ncpu, "tolerances_met": ok, "f14_agree_1e-6": f14_agree,
+                                   "f14_max_abs": f14_abs, "f14_max_rel": f14_rel,
                                    "max_rel": {k: float("%.3g" % v[0]) for k, v in sorted(errs.items())},
                                    "max_rel_to_group_max": {k: float("%.3g" % v[1]) for k, v in sorted(errs.items())},
                                    "worst": {k: v[2] for k, v in sorted(errs.items()) if v[1] > 0}}

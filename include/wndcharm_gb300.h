@@ -34,6 +34,11 @@ extern "C" {
 #define WC_ERR_DEVICE (-5)      /* a kernel reported a bounded-wait timeout or an internal check */
 #define WC_ERR_IO (-6)          /* a file could not be read or is malformed */
 
+/* largest image accepted: sides up to WC_MAX_SIDE pixels and at most
+ * WC_MAX_PIXELS pixels; larger images give WC_ERR_ARG before any allocation */
+#define WC_MAX_SIDE 32768
+#define WC_MAX_PIXELS (1LL << 28)
+
 /* plan kinds: the reference's standard feature sets */
 #define WC_PLAN_SHORT 0 /* 1059 features, StdFeatureComputationPlans::getFeatureSet */
 #define WC_PLAN_LONG 1  /* 2919 features, StdFeatureComputationPlans::getFeatureSetLong */
@@ -50,7 +55,7 @@ extern "C" {
 
 /* arithmetic form of an engine */
 #define WC_PREC_FP64 0  /* plain FP64 form: every family in double precision */
-#define WC_PREC_MIXED 1 /* batched mixed-precision form (FP32 + tensor cores, FP64 where required) */
+#define WC_PREC_MIXED 1 /* batched mixed-precision form: FP32 and pairs of floats on the CUDA cores, FP64 where required */
 
 typedef struct wc_plan wc_plan;     /* a feature computation plan (groups, offsets, names) */
 typedef struct wc_engine wc_engine; /* one GPU: device, stream, device memory pools */
@@ -94,6 +99,21 @@ int wc_plan_group(const wc_plan *plan, int g, char *buf, int buflen, int *offset
 /* ---- engines ---- */
 int wc_engine_create(int device, int precision, wc_engine **out);
 void wc_engine_destroy(wc_engine *engine);
+/* Engine options (no reference counterpart; defaults reproduce the reference):
+ *   "f14_exact"        1 (default): the mixed form computes Haralick f14 (Q, the
+ *                      Hessenberg reduction, the real-Schur QR) through the FP64
+ *                      chain, bit-identical to the FP64 form and the oracle;
+ *                      0: in pairs of floats on the FP32 pipe (faster; f14 is
+ *                      then only as reproducible as a different build).
+ *   "qr_iter_per_tone" real-Schur iterations allowed per tone, 40 (Eigen 3.1.2's
+ *                      m_maxIterationsPerRow, RealSchur.h); a matrix that runs
+ *                      out gives f14 = 0, as the reference's unconverged solver.
+ *   "union_find_cap"   iterations allowed per union-find link in the object
+ *                      labelling; 0 (default): the plane's pixel count, a bound
+ *                      no correct run reaches.  A run that reaches the cap
+ *                      returns WC_ERR_DEVICE (the bounded-wait error path).
+ * Unknown names and out-of-range values give WC_ERR_ARG. */
+int wc_engine_set_option(wc_engine *engine, const char *name, long long value);
 /* CUDA stream the engine launches on (as a cudaStream_t cast to void*); 0 = legacy default */
 int wc_engine_set_stream(wc_engine *engine, void *stream);
 /* kernels launched by this engine since creation (counts every launch) */
@@ -141,6 +161,30 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
                     const double *weights, const double *mins, const double *maxs, const double *test, int T,
                     double *probs, int *pred);
 
+/* Device-pointer forms of wc_wnd_fit and wc_wnd_classify (same semantics):
+ * every array argument is a device pointer on the engine's GPU, so rows that
+ * are already in device memory (e.g. feature rows of wc_extract_batch with
+ * out_on_device) are classified without a host round trip.  The calls return
+ * when the results are written.  In the mixed form, wc_wnd_classify* computes
+ * the distances on the tensor cores (when at most 511 features have a
+ * non-zero weight): the weighted rows are cut into four 8-bit digits held
+ * exactly in bf16, digit pairs are multiplied by tcgen05.mma into FP32 sums
+ * that stay exact, and every test row whose error bound, nearest-row distance
+ * or top-two class margin is not certified is recomputed by the FP64 kernel
+ * (the reference's order), so classes equal the FP64 form's and
+ * probabilities stay within 1e-6 of them.  More weighted features: pairs of
+ * floats on the CUDA cores. */
+int wc_wnd_fit_device(wc_engine *engine, const double *train, int N, int F, const int *labels, int C, double frac,
+                      double *weights, double *mins, double *maxs);
+int wc_wnd_classify_device(wc_engine *engine, const double *train, int N, int F, const int *labels, int C,
+                           const double *weights, const double *mins, const double *maxs, const double *test, int T,
+                           double *probs, int *pred);
+/* What the calling thread's last wc_wnd_classify* call did (no reference
+ * counterpart): stats[0] 1 if the tensor-core path ran, stats[1] the test rows
+ * the FP64 kernel recomputed, stats[2] the features with a non-zero weight,
+ * stats[3] the tensor-core kernel's CTAs. */
+int wc_wnd_last_stats(long long *stats);
+
 /* wc_wnd_classify_images: TrainingSet::ClassifyImage with WND-5
  * (src/wndchrm_src/TrainingSet.cpp:1603-1800) for n_images images of `tiles`
  * samples each: test holds n_images * tiles rows, an image's tiles consecutive.
@@ -185,8 +229,9 @@ int wc_tiff_read(const char *path, void *pixels, long long capacity);
  * that does not fit the rotated image (the reference then keeps the previous
  * sample's pixels) is WC_ERR_ARG.  Arithmetic is FP64 in the reference's
  * order (crop, rotation, tiles and Downsample are bit-identical to it); the
- * mean / standard deviation that normalisation divides by are two-pass sums
- * (the reference: Welford updates), so normalised pixels agree to ~1e-15. */
+ * mean / standard deviation that normalisation divides by come from the
+ * reference's own Welford chain (Moments2, in raster order), so normalised
+ * pixels are bit-identical too. */
 typedef struct {
     int crop_x, crop_y, crop_w, crop_h; /* bounding rectangle; crop_x < 0: the whole image */
     double downsample_x, downsample_y;  /* Downsample ratios in (0, 1); >= 1: no downsampling */
@@ -225,8 +270,11 @@ int wc_extract_samples(wc_engine *engine, const wc_plan *plan, const wc_image_de
  * (8.25 MiB per GPU, held until the process exits), enough for inputs up to
  * 1024 x 1024; larger inputs are rejected with WC_ERR_ARG.  All calls share that
  * array: calls whose work overlaps on the GPU race, so order them (one stream).
- * The first call on a device looks up the array's device address; make it
- * before any stream capture.  It has no counterpart in the reference. */
+ * Every call looks up the array's address on the current device (so a
+ * cudaDeviceReset in between is harmless); the first call on a device loads
+ * the library's device code there, so make it before any stream capture.
+ * A CUDA error left pending by an earlier call gives WC_ERR_CUDA before any
+ * launch.  It has no counterpart in the reference. */
 int wc_wavelet_noalloc(const double *d_in, int width, int height, double *d_out, void *stream);
 
 #ifdef __cplusplus

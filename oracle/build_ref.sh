@@ -5,15 +5,23 @@
 # (oracle/ref_shim/include), the FFTW3 shim (oracle/ref_shim/fftw_shim.cpp) and
 # the C ABI used by the tests (oracle/ref_shim/ref_capi.cpp).
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# VARIANT=fma builds a second copy into oracle/_ref_fma/ with floating-point
+# contraction into fused multiply-adds (x86-64: -mfma; aarch64 contracts by
+# default): the reference as a contracting compiler builds it, used to measure
+# the reference's own build-to-build spread on rounding-sensitive features.
 set -euo pipefail
 REF="${1:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
-OUT="$HERE/_ref"
+VARIANT="${VARIANT:-}"
+OUT="$HERE/_ref${VARIANT:+_$VARIANT}"
 SRC="$REF/src"
 if [ ! -d "$SRC" ]; then echo "reference sources not found at $SRC" >&2; exit 2; fi
 mkdir -p "$OUT/obj"
 CXX="${CXX:-g++}"
 FLAGS="-O2 -fPIC -w -std=gnu++11 -I$HERE/ref_shim/include -I$SRC"
+if [ "$VARIANT" = "fma" ]; then
+  case "$(uname -m)" in x86_64) FLAGS="$FLAGS -mfma -ffp-contract=fast" ;; *) FLAGS="$FLAGS -ffp-contract=fast" ;; esac
+fi
 FILES="cmatrix.cpp FeatureAlgorithms.cpp FeatureNames.cpp ImageTransforms.cpp Tasks.cpp wndchrm_error.cpp
 transforms/ChebyshevFourier.cpp transforms/chebyshev.cpp transforms/radon.cpp
 transforms/wavelet/Common.cpp transforms/wavelet/DataGrid2D.cpp transforms/wavelet/DataGrid3D.cpp

@@ -1,16 +1,23 @@
 """Per-family parity rules shared by the oracle tests and the GPU tests.
 
-Feature families are identified by the group name of each feature.  Three
-kinds of comparison:
+Feature families are identified by the group name of each feature.  Kinds of
+comparison:
   * "float": |a-b| <= rtol*|b| + atol;
-  * "counts": histogram-like groups whose values come from binning a
-    floating-point quantity: they may differ by a few single-count moves
-    between neighbouring bins (each move changes two entries by 1); the
-    number of such moves per group is budgeted;
+  * "counts": histogram-like groups (values from binning a floating-point
+    quantity).  Where the binned quantity is computed in the oracle's order of
+    operations (every family of the FP64 form, and the mixed form's FP64
+    families) they must be equal; a form that bins an FP32 quantity (the mixed
+    form's Radon projections and Chebyshev-Fourier magnitudes) may show a few
+    single-count moves between neighbouring bins (each move changes two
+    entries by 1), budgeted per group;
   * "f14": Haralick maximal-correlation-coefficient entries (in-group
-    indices 16, 17): sqrt of eigenvalue #2 in Schur order, which depends on
-    the eigen-solver's rounding (two builds of the reference itself differ);
-    reported, never gated beyond "finite and in [0, 1.5]".
+    indices 16, 17): sqrt of eigenvalue #2 in real-Schur order.  Against the
+    oracle they must be bit-identical (f14="exact": the GPU's FP64 chain
+    performs the oracle's operations in its order).  Against the reference
+    build they are range-checked (f14="range"): which eigenvalue lands in slot
+    2 depends on rounding, and two builds of the unmodified reference (with
+    and without fused multiply-adds) already disagree on 34 of 384 entries of
+    the 512 x 512 workload (tests/golden/reference_build_spread.npz).
 """
 import numpy as np
 
@@ -27,9 +34,15 @@ def index_of(name):
     return int(name.rsplit("[", 1)[1].rstrip("]"))
 
 
-def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=2, skip=()):
+def _f14_equal(va, vb):
+    return (va == vb) | (np.isnan(va) & np.isnan(vb))
+
+
+def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=0, skip=(), f14="range"):
     """Compare feature rows a (candidate) and b (expected).  Returns a dict of
-    failures keyed by group name; empty when everything is within rules."""
+    failures keyed by group name; empty when everything is within rules.
+    count_moves: single-count moves allowed per count group (0: equal);
+    f14: "exact" (bit-identical, NaN equal to NaN) or "range" (finite, in [0, 1.5])."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     groups = {}
@@ -43,15 +56,20 @@ def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=2, skip=()):
         alg = g.split(" (")[0]
         va, vb = a[idx], b[idx]
         if alg == "Haralick Textures":
-            f14 = np.array([index_of(names[i]) in F14 for i in idx])
-            bad14 = ~np.isfinite(va[f14]) | (va[f14] < 0) | (va[f14] > 1.5)
+            f14m = np.array([index_of(names[i]) in F14 for i in idx])
+            if f14 == "exact":
+                bad14 = ~_f14_equal(va[f14m], vb[f14m])
+            else:
+                bad14 = ~np.isfinite(va[f14m]) | (va[f14m] < 0) | (va[f14m] > 1.5)
             if bad14.any():
-                fails[g] = ("f14 out of range", va[f14])
-            va, vb = va[~f14], vb[~f14]
+                fails[g + " f14"] = ("f14 " + f14, va[f14m], vb[f14m])
+            va, vb = va[~f14m], vb[~f14m]
         if alg in COUNT_GROUPS:
             d = np.abs(va - vb)
             if alg == "Multiscale Histograms":
-                ok = np.allclose(va, vb, rtol=rtol, atol=0.02)
+                # bin counts over the largest bin: equal when the counts are
+                ok = np.array_equal(va, vb) if count_moves == 0 else bool(np.all(d <= 2.0 * count_moves * np.min(
+                    vb[vb > 0], initial=1.0)))
             else:
                 ok = (np.abs(np.round(d) - d) < 1e-9).all() and d.sum() <= 2 * count_moves
             if not ok:
@@ -70,18 +88,21 @@ def compare(a, b, names, rtol=1e-6, atol=1e-9, count_moves=2, skip=()):
 #   ("float", rtol, gtol): |a-b| <= rtol*|b| + gtol*max|group|
 #   ("counts", moves):     at most `moves` single-count moves per group
 MIXED_RULES = {
-    "Chebyshev-Fourier Coefficients": ("counts", 3),
+    # 32-bin histogram of FP32-recurrence projection magnitudes
+    "Chebyshev-Fourier Coefficients": ("counts", 2),
+    # 3-bin histograms of FP32 projections (sub-pixel bins are the FP64 form's)
+    "Radon Coefficients": ("counts", 2),
     # ratios of threshold counts over FP32 filter energies: a few pixels of the
     # 512 x 512 maps may cross the threshold
     "Gabor Textures": ("float", 1e-4, 0.0),
 }
 
 
-def compare_mixed(a, b, names, rtol=1e-7, atol=1e-9, count_moves=2, skip=()):
+def compare_mixed(a, b, names, rtol=1e-7, atol=1e-9, count_moves=0, skip=(), f14="range"):
     """compare() with the mixed form's per-family tolerances."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    fails = compare(a, b, names, rtol, atol, count_moves, skip=tuple(skip) + tuple(MIXED_RULES))
+    fails = compare(a, b, names, rtol, atol, count_moves, skip=tuple(skip) + tuple(MIXED_RULES), f14=f14)
     groups = {}
     for i, n in enumerate(names):
         groups.setdefault(group_of(n), []).append(i)
@@ -102,6 +123,22 @@ def compare_mixed(a, b, names, rtol=1e-7, atol=1e-9, count_moves=2, skip=()):
                 j = np.nonzero(bad)[0]
                 fails[g] = ("float", j[:8].tolist(), va[j[:4]].tolist(), vb[j[:4]].tolist())
     return fails
+
+
+def f14_columns(names):
+    return np.array([i for i, nm in enumerate(names) if group_of(nm).startswith("Haralick") and index_of(nm) in F14])
+
+
+def f14_errors(a, b):
+    """f14 entries of rows a against b: (fraction within 1e-6 relative, max abs
+    difference, max relative difference), NaN pairs counted as equal."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    both_nan = np.isnan(a) & np.isnan(b)
+    d = np.where(both_nan, 0.0, np.abs(a - b))
+    rel = d / np.maximum(np.abs(b), 1e-300)
+    agree = both_nan | (d <= 1e-6 * np.maximum(np.abs(b), 1e-12))
+    return float(np.mean(agree)), float(np.nanmax(d)), float(np.nanmax(np.where(d == 0, 0.0, rel)))
 
 
 def family_errors(a, b, names):

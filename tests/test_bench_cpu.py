@@ -39,9 +39,10 @@ def test_stage_work_model():
     # the Chebyshev transforms: 3 per image, two 512^3 products each, a multiply and an add per term
     assert bench.stage_work("Chebyshev", B) == ("fp64", B * 3 * 2 * 2 * 512 ** 3)
     assert bench.stage_work("Chebyshev", B, "fp64") == bench.stage_work("Chebyshev", B, "mixed")
-    # f14 and the Zernike moments are FP64 work only in the FP64 form
-    assert bench.stage_work("Haralick Textures", B, "mixed") is None
+    # f14 is FP64 work unless the mixed form runs its pairs-of-floats chain; Zernike only in the FP64 form
+    assert bench.stage_work("Haralick Textures", B, "mixed", "pairs") is None
+    assert bench.stage_work("Haralick Textures", B, "mixed", "exact")[0] == "fp64"
     assert bench.stage_work("Haralick Textures", B, "fp64")[0] == "fp64"
     assert bench.stage_work("Zernike Coefficients", B, "mixed") is None
-    assert bench.stage_work("Tamura Textures", B)[0] == "bytes"
+    assert bench.stage_work("Tamura Textures", B)[0] == "fp64"
     assert bench.stage_work("no such stage", B) is None

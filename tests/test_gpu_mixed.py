@@ -32,7 +32,7 @@ def test_mixed_synthetic_vs_oracle(eng, long_plan):
     worst = {}
     for i, img in enumerate(imgs):
         exp = oracle_features(lib, img)
-        fails = compare_mixed(got[i], exp, names)
+        fails = compare_mixed(got[i], exp, names, f14="exact")
         assert not fails, (img.shape, list(fails.items())[:3])
         for k, v in family_errors(got[i], exp, names).items():
             w = worst.get(k, (0.0, 0.0, ""))
@@ -102,5 +102,5 @@ def test_512_workload_both_forms(long_plan):
                 if v[1] > 0:
                     print(prec, i, "%-32s rel %.3g group %.3g %s" % (k, v[0], v[1], v[2]))
         for i in range(2):
-            fails = cmp(got[i], exp[i], names)
+            fails = cmp(got[i], exp[i], names, f14="exact")
             assert not fails, (prec, i, list(fails.items())[:4])

@@ -34,7 +34,7 @@ def test_uneven_tiles_one_batch():
     lib = oracle_lib()
     for k in (0, 17, 42, len(tl) - 1):
         exp = oracle_features(lib, np.ascontiguousarray(tl[k]))
-        fails = compare(got[k], exp, names, rtol=1e-7, atol=1e-9, count_moves=2)
+        fails = compare(got[k], exp, names, rtol=1e-7, atol=1e-9, count_moves=0, f14="exact")
         assert not fails, (k, tl[k].shape, list(fails.items())[:3])
         np.testing.assert_array_equal(eng.extract(plan, [np.ascontiguousarray(tl[k])])[0], got[k])
 

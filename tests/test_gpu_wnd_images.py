@@ -23,9 +23,12 @@ def test_classify_images(prec, max_tile):
     op, opr, onf = oracle_wnd_images(oracle_lib(), xtr, ytr, xte, 6, 0.15, 4, max_tile)
     np.testing.assert_array_equal(pr, opr)
     np.testing.assert_array_equal(pr, g["pred_max_tile%d" % max_tile])
-    np.testing.assert_allclose(p, op, rtol=0, atol=1e-12)
-    np.testing.assert_allclose(p, g["probs_max_tile%d" % max_tile], rtol=0, atol=1e-12)
-    np.testing.assert_allclose(nf, onf, rtol=1e-9)
+    # FP64 form: the reference's arithmetic; mixed form (distances on the tensor
+    # cores): the stated WND tolerance, probabilities within 1e-6
+    atol, nrtol = (1e-12, 1e-9) if prec == "fp64" else (1e-6, 1e-6)
+    np.testing.assert_allclose(p, op, rtol=0, atol=atol)
+    np.testing.assert_allclose(p, g["probs_max_tile%d" % max_tile], rtol=0, atol=atol)
+    np.testing.assert_allclose(nf, onf, rtol=nrtol)
     if not max_tile:
         pt, prt = eng.wnd_classify(xtr, ytr, 6, w, mn, mx, xte)
         avg = np.zeros((12, 6))

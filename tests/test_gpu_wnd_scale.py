@@ -41,8 +41,9 @@ def test_wnd_full_scale():
 
 
 def test_wnd_full_scale_mixed_matches_fp64():
-    """The mixed form (FP32-pair distances) at full scale: predicted classes
-    identical to the FP64 form, marginal probabilities within 1e-6."""
+    """The mixed form (distances on the tensor cores, uncertified rows
+    recomputed in FP64) at full scale: predicted classes identical to the FP64
+    form, marginal probabilities within 1e-6."""
     import wndcharm
     from wndcharm import synth
     xtr, ytr, xte, yte = synth.feature_vectors(100000, 10000, 2919, 10, 4)
@@ -51,7 +52,10 @@ def test_wnd_full_scale_mixed_matches_fp64():
     p64, pr64 = e64.wnd_classify(xtr, ytr, 10, w, mn, mx, xte)
     t0 = time.perf_counter()
     pmx, prmx = emx.wnd_classify(xtr, ytr, 10, w, mn, mx, xte)
-    print("mixed classify %.2f s" % (time.perf_counter() - t0))
+    st = emx.wnd_last_stats()
+    print("mixed classify %.2f s (tensor cores: %d, rows re-checked in FP64: %d, K = %d)"
+          % (time.perf_counter() - t0, st[0], st[1], st[2]))
+    assert st[0] == 1
     np.testing.assert_array_equal(prmx, pr64)
     np.testing.assert_allclose(pmx, p64, rtol=0, atol=1e-6)
     print("max |p_mixed - p_fp64| = %.3g" % np.abs(pmx - p64).max())

@@ -1,0 +1,93 @@
+"""WND-5 distances on the tensor cores (the mixed form's wc_wnd_classify*):
+against the FP64 form (the reference's order, itself pinned to the oracle
+and the reference's fixtures), predicted classes identical and marginal
+probabilities within 1e-6, on the synthetic feature vectors of the WND
+workload (per-feature N(mu_cf, 1), class means N(0, 0.5)), with duplicated
+rows (distance 0: the reference skips them; the tensor-core pass must hand
+them to the FP64 re-check), with more weighted features than the digit
+sums allow (the pairs-of-floats path), and through the device-pointer entry
+point."""
+import numpy as np
+import pytest
+
+import synth_loader  # noqa: F401
+
+pytestmark = pytest.mark.gpu
+
+
+def _fit(e64, xtr, ytr, C, frac):
+    return e64.wnd_fit(xtr, ytr, C, frac)
+
+
+@pytest.mark.parametrize("n_train,n_test,F,C,seed", [(3000, 700, 2919, 10, 4), (1500, 300, 1059, 4, 7),
+                                                       (200, 129, 300, 3, 1)])
+def test_tensor_core_matches_fp64(n_train, n_test, F, C, seed):
+    import wndcharm
+    from wndcharm import synth
+    xtr, ytr, xte, _ = synth.feature_vectors(n_train, n_test, F, C, seed)
+    e64, emx = wndcharm.Engine(0, "fp64"), wndcharm.Engine(0, "mixed")
+    w, mn, mx = e64.wnd_fit(xtr, ytr, C, 0.15)
+    p64, pr64 = e64.wnd_classify(xtr, ytr, C, w, mn, mx, xte)
+    pmx, prmx = emx.wnd_classify(xtr, ytr, C, w, mn, mx, xte)
+    stats = emx.wnd_last_stats()
+    assert stats[0] == 1, stats  # the tensor-core path ran
+    np.testing.assert_array_equal(prmx, pr64)
+    np.testing.assert_allclose(pmx, p64, rtol=0, atol=1e-6)
+    print("K=%d: max |p_tc - p_fp64| = %.3g, %d of %d rows re-checked in FP64"
+          % (stats[2], np.abs(pmx - p64).max(), stats[1], n_test))
+    assert stats[1] <= n_test // 20  # the re-check is the exception
+
+
+def test_duplicates_and_near_duplicates_go_to_the_fp64_recheck():
+    import wndcharm
+    from wndcharm import synth
+    xtr, ytr, xte, _ = synth.feature_vectors(1000, 200, 500, 5, 11)
+    xte[:10] = xtr[:10]              # exact duplicates: distance 0 (skipped by the reference)
+    xte[10:20] = xtr[20:30] + 1e-9   # near-duplicates
+    e64, emx = wndcharm.Engine(0, "fp64"), wndcharm.Engine(0, "mixed")
+    w, mn, mx = e64.wnd_fit(xtr, ytr, 5, 0.15)
+    p64, pr64 = e64.wnd_classify(xtr, ytr, 5, w, mn, mx, xte)
+    pmx, prmx = emx.wnd_classify(xtr, ytr, 5, w, mn, mx, xte)
+    stats = emx.wnd_last_stats()
+    assert stats[0] == 1 and stats[1] >= 20, stats
+    np.testing.assert_array_equal(prmx, pr64)
+    np.testing.assert_allclose(pmx, p64, rtol=0, atol=1e-6)
+    # recomputed by the FP64 kernel itself (its chunks of training rows are
+    # split finer for a few rows: the sums differ from the full pass in the last bits)
+    np.testing.assert_allclose(pmx[:20], p64[:20], rtol=0, atol=1e-14)
+
+
+def test_many_weighted_features_use_pairs_of_floats():
+    import wndcharm
+    from wndcharm import synth
+    xtr, ytr, xte, _ = synth.feature_vectors(800, 100, 1200, 4, 3)
+    e64, emx = wndcharm.Engine(0, "fp64"), wndcharm.Engine(0, "mixed")
+    w, mn, mx = e64.wnd_fit(xtr, ytr, 4, 1.0)  # every feature weighted
+    p64, pr64 = e64.wnd_classify(xtr, ytr, 4, w, mn, mx, xte)
+    pmx, prmx = emx.wnd_classify(xtr, ytr, 4, w, mn, mx, xte)
+    assert emx.wnd_last_stats()[0] == 0
+    np.testing.assert_array_equal(prmx, pr64)
+    np.testing.assert_allclose(pmx, p64, rtol=0, atol=1e-6)
+
+
+def test_device_entry_points_match_host_ones():
+    import torch
+    import wndcharm
+    from wndcharm import synth
+    xtr, ytr, xte, _ = synth.feature_vectors(2000, 256, 700, 6, 5)
+    emx = wndcharm.Engine(0, "mixed")
+    w, mn, mx = emx.wnd_fit(xtr, ytr, 6, 0.15)
+    p, pr = emx.wnd_classify(xtr, ytr, 6, w, mn, mx, xte)
+    d = lambda a, dt=torch.float64: torch.from_numpy(np.ascontiguousarray(a)).to(dtype=dt, device="cuda")  # noqa
+    X, y, T = d(xtr), d(ytr, torch.int32), d(xte)
+    dw, dmn, dmx = (torch.empty(700, dtype=torch.float64, device="cuda") for _ in range(3))
+    emx.wnd_fit_device(X, y, 6, 0.15, dw, dmn, dmx)
+    np.testing.assert_array_equal(dw.cpu().numpy(), w)
+    np.testing.assert_array_equal(dmn.cpu().numpy(), mn)
+    np.testing.assert_array_equal(dmx.cpu().numpy(), mx)
+    dp = torch.empty((256, 6), dtype=torch.float64, device="cuda")
+    dpr = torch.empty(256, dtype=torch.int32, device="cuda")
+    emx.wnd_classify_device(X, y, 6, dw, dmn, dmx, T, dp, dpr)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dpr.cpu().numpy(), pr)
+    np.testing.assert_array_equal(dp.cpu().numpy(), p)

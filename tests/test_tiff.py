@@ -126,3 +126,19 @@ def test_tiff_errors(tmp_path):
     with pytest.raises(wndcharm.WndcharmError):
         wndcharm.read_tiff(str(tmp_path / "missing.tif"))
     assert wndcharm.ImageMatrix().OpenImage(str(tmp_path / "x.png")) == 0
+
+
+@pytest.mark.parametrize("compression", [1, 32773])
+def test_truncated_tiffs_are_io_errors(tmp_path, compression):
+    """A TIFF cut short anywhere (header, directory, strips) is WC_ERR_IO, never a crash."""
+    rng = np.random.default_rng(4)
+    a = rng.integers(0, 4096, size=(20, 17)).astype(np.uint16)
+    full = tmp_path / "full.tif"
+    _write_tiff(full, a, compression, 1, "<")
+    raw = full.read_bytes()
+    np.testing.assert_array_equal(wndcharm.read_tiff(str(full))[0], a)
+    for cut in sorted({4, 8, 12, len(raw) // 3, len(raw) // 2, len(raw) - 7, len(raw) - 1}):
+        p = tmp_path / ("cut%d.tif" % cut)
+        p.write_bytes(raw[:cut])
+        with pytest.raises(wndcharm.WndcharmError):
+            wndcharm.read_tiff(str(p))

@@ -138,7 +138,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
               std::vector<Plane> *planes_out) {
     const auto h0 = std::chrono::steady_clock::now();
     auto host_ms = [&h0]() { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count(); };
-    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof};
+    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof, &E->opts};
     // ---- nodes: every prefix of every group's transform chain
     std::vector<Node> nodes(1);
     nodes[0] = {-1, -1, 0, {}};
@@ -197,6 +197,10 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     for (int b = 0; b < n; b++) {
         if (imgs[b].width < 1 || imgs[b].height < 1 || !imgs[b].pixels)
             return set_err(WC_ERR_ARG, "image %d: bad size or null pixels", b);
+        if (imgs[b].width > WC_MAX_SIDE || imgs[b].height > WC_MAX_SIDE ||
+            (long long)imgs[b].width * imgs[b].height > WC_MAX_PIXELS)
+            return set_err(WC_ERR_ARG, "image %d: %d x %d is larger than this build accepts (sides <= %d, <= %lld pixels)",
+                           b, imgs[b].width, imgs[b].height, WC_MAX_SIDE, (long long)WC_MAX_PIXELS);
         if (imgs[b].dtype < WC_U8 || imgs[b].dtype > WC_RGB16)
             return set_err(WC_ERR_ARG, "image %d: unknown pixel type %d", b, imgs[b].dtype);
         for (int k = 0; k < NN; k++) {
@@ -462,6 +466,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
 
 namespace wc {
 int engine_precision(const wc_engine *E) { return E->prec; }
+int engine_sms(const wc_engine *E) { return E->sms; }
 int engine_device(wc_engine *E, cudaStream_t *st, long long **launches) {
     CK(cudaSetDevice(E->dev));
     *st = E->st;
@@ -593,6 +598,25 @@ void wc_engine_destroy(wc_engine *E) {
     if (E->fork_ev) cudaEventDestroy(E->fork_ev);
     if (E->early_ev) cudaEventDestroy(E->early_ev);
     delete E;
+}
+
+int wc_engine_set_option(wc_engine *E, const char *name, long long value) {
+    if (!E || !name) return set_err(WC_ERR_ARG, "wc_engine_set_option: null argument");
+    std::lock_guard<std::mutex> lk(E->mu);
+    const std::string k(name);
+    if (k == "f14_exact") {
+        if (value != 0 && value != 1) return set_err(WC_ERR_ARG, "f14_exact must be 0 or 1");
+        E->opts.f14_exact = (int)value;
+    } else if (k == "qr_iter_per_tone") {
+        if (value < 1 || value > 1000000) return set_err(WC_ERR_ARG, "qr_iter_per_tone must be in 1..1e6");
+        E->opts.qr_iter_per_tone = (int)value;
+    } else if (k == "union_find_cap") {
+        if (value < 0) return set_err(WC_ERR_ARG, "union_find_cap must be >= 0");
+        E->opts.union_find_cap = value;
+    } else {
+        return set_err(WC_ERR_ARG, "unknown engine option '%s'", name);
+    }
+    return WC_OK;
 }
 
 int wc_engine_set_stream(wc_engine *E, void *stream) {

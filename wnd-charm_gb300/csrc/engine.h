@@ -98,6 +98,7 @@ struct wc_engine {
     std::vector<char> hmeta, hpre;
     std::mutex mu;
     wc::Prof prof;
+    wc::Opts opts;
     cudaStream_t lanes[WC_LANES] = {};
     cudaEvent_t fork_ev = nullptr, early_ev = nullptr, join_ev[WC_LANES] = {};
 };

@@ -71,14 +71,12 @@ int features_check(cudaStream_t st, int *dev_err) {
         cudaMemcpyToSymbolAsync(g_dev_err, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
         cudaStreamSynchronize(st);
     }
-    // the object kernels' word (the stream is known good here; should reading
-    // it fail, the error is cleared and the word taken as 0 rather than the
-    // batch failed)
+    // the object kernels' word: a batch whose word cannot be read is failed,
+    // never reported as good (a union-find cap hit would otherwise be lost)
     int vo = 0;
-    if (objects_err_take(st, &vo)) {
-        cudaGetLastError();
-        vo = 0;
-    }
+    if (objects_err_take(st, &vo))
+        return set_err(WC_ERR_CUDA, "reading the object kernels' error word failed: %s",
+                       cudaGetErrorString(cudaGetLastError()));
     *dev_err = v ? v : vo;
     return WC_OK;
 }

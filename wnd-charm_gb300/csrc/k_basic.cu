@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "kcommon.cuh"
+#include "kwavelet.cuh"
 #include "kdf32.cuh"
 #include "kernels.h"
 
@@ -108,73 +109,35 @@ void launch_edge(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, i
 }
 
 // ---------------------------------------------------------------- Wavelet transform
-// One level of the zero-padded Symlet-5 decomposition
-// (Wavelet::transform2D, src/transforms/wavelet/Wavelet.cpp:136-434, with
-// downsampling_convolution MODE_ZEROPAD, convolution.cpp:86-325):
-// out[o] = sum_j f[j] * x[2o+1-j] over the taps inside the input, j ascending.
-__constant__ double c_sym_lo[10] = {0.027333068345077982, 0.029519490925774643, -0.039134249302383094,
-                                    0.1993975339773936, 0.72340769040242059, 0.63397896345821192,
-                                    0.016602105764522319, -0.17532808990845047, -0.021101834024758855,
-                                    0.019538882735286728};
-__constant__ double c_sym_hi[10] = {-0.019538882735286728, -0.021101834024758855, 0.17532808990845047,
-                                    0.016602105764522319, -0.63397896345821192, 0.72340769040242059,
-                                    -0.1993975339773936, -0.039134249302383094, -0.029519490925774643,
-                                    0.027333068345077982};
+// One level of the zero-padded Symlet-5 decomposition; the tap loops are in
+// kwavelet.cuh (shared with the allocation-free entry point and the adjoint).
 
 // pass 1: along y for each column x: tmp[(x*oy + o)*2 + {0: approx, 1: detail}]
 __global__ void k_wavelet_y(const double *__restrict__ arena, const Plane *__restrict__ planes,
                             const TJob *__restrict__ jobs, double *__restrict__ tmp, const long long *__restrict__ tmp_off) {
     const TJob J = jobs[blockIdx.z];
     const Plane S = planes[J.src];
-    const int X = S.w, Y = S.h, oy = (Y + 9) / 2;
+    const int X = S.w, Y = S.h, oy = sym5_out(Y);
     int x = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= X || o >= oy) return;
-    const double *in = arena + S.off;
-    const int i = 2 * o + 1;
-    double a = 0, d = 0;
-#pragma unroll
-    for (int j = 0; j < 10; j++) {
-        int k = i - j;
-        if (k >= 0 && k < Y) {
-            double v = in[(long long)k * X + x];
-            a = __dadd_rn(a, __dmul_rn(v, c_sym_lo[j]));
-            d = __dadd_rn(d, __dmul_rn(v, c_sym_hi[j]));
-        }
-    }
-    double *t = tmp + tmp_off[blockIdx.z];
-    t[((long long)x * oy + o) * 2 + 0] = a;
-    t[((long long)x * oy + o) * 2 + 1] = d;
+    double a, d;
+    sym5_col(arena + S.off, X, Y, x, o, a, d);
+    double *t = tmp + tmp_off[blockIdx.z] + sym5_tmp_index(x, oy, o);
+    t[0] = a;
+    t[1] = d;
 }
 
-// pass 2: along x for each row o of both pass-1 outputs, placed in quadrants:
-// (y<oy, x<ox) dd, (y>=oy, x<ox) da, (y<oy, x>=ox) ad, (y>=oy, x>=ox) aa.
+// pass 2: along x for each row o of both pass-1 outputs, placed in quadrants
 __global__ void k_wavelet_x(double *__restrict__ arena, const Plane *__restrict__ planes, const TJob *__restrict__ jobs,
                             const double *__restrict__ tmp, const long long *__restrict__ tmp_off) {
     const TJob J = jobs[blockIdx.z];
     const Plane S = planes[J.src], D = planes[J.dst];
-    const int X = S.w, Y = S.h, ox = (X + 9) / 2, oy = (Y + 9) / 2;
+    const int X = S.w, Y = S.h, ox = sym5_out(X), oy = sym5_out(Y);
     int u = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y * blockDim.y + threadIdx.y;
     if (u >= ox || o >= oy) return;
-    const double *t = tmp + tmp_off[blockIdx.z];
-    const int i = 2 * u + 1;
-    double a1 = 0, d1 = 0, a2 = 0, d2 = 0;
-#pragma unroll
-    for (int j = 0; j < 10; j++) {
-        int k = i - j;
-        if (k >= 0 && k < X) {
-            double va = t[((long long)k * oy + o) * 2 + 0], vd = t[((long long)k * oy + o) * 2 + 1];
-            a1 = __dadd_rn(a1, __dmul_rn(va, c_sym_lo[j]));
-            d1 = __dadd_rn(d1, __dmul_rn(va, c_sym_hi[j]));
-            a2 = __dadd_rn(a2, __dmul_rn(vd, c_sym_lo[j]));
-            d2 = __dadd_rn(d2, __dmul_rn(vd, c_sym_hi[j]));
-        }
-    }
-    double *out = arena + D.off;
-    const int W = D.w;
-    out[(long long)o * W + u] = d2;
-    out[(long long)(oy + o) * W + u] = a2;
-    out[(long long)o * W + ox + u] = d1;
-    out[(long long)(oy + o) * W + ox + u] = a1;
+    double a1, d1, a2, d2;
+    sym5_row(tmp + tmp_off[blockIdx.z], X, oy, u, o, a1, d1, a2, d2);
+    sym5_store(arena + D.off, ox, oy, u, o, a1, d1, a2, d2);
 }
 
 void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
@@ -331,8 +294,12 @@ void launch_fractal(Ctx &c, const double *arena, const Plane *planes, const FJob
 
 // ---------------------------------------------------------------- comb moments
 // CombFirst4Moments2D + matr4moments_to_hist + vd_Comb4Moments,
-// src/statistics/CombFirst4Moments.cpp:47-272.  One warp per comb line: two
-// passes (mean, then central sums) give Moments4's mean/std/skew/kurtosis.
+// src/statistics/CombFirst4Moments.cpp:47-272.  One thread per comb line runs
+// Moments4's Welford updates (src/statistics/Moments.h:60-107) over the line's
+// pixels in the reference's order, every operation rounded as the CPU rounds
+// it (no contraction), so the moments - and the 3-bin histograms of them,
+// whose bins mathematically tied lines (the mirrored halves of a Fourier
+// plane) decide by their last bits - are the reference's.
 __device__ __forceinline__ bool comb_pixel(int dir, long long j, long long ii, long long m, long long n, long long n2,
                                            long long m2, long long &y, long long &x) {
     if (dir == 0) { y = j; x = j + ii; return x >= 0 && x < n; }
@@ -341,25 +308,48 @@ __device__ __forceinline__ bool comb_pixel(int dir, long long j, long long ii, l
     y = m2 - 1 - ii; x = j; return y >= 0 && y < m;
 }
 
-__global__ void __launch_bounds__(512) k_comb(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
-                       double *__restrict__ feat) {
+struct CombMom4 {
+    double mean = 0, M2 = 0, M3 = 0, M4 = 0;
+    unsigned long long n = 0;
+    __device__ __forceinline__ void add(double x) {
+        if (isnan(x) || x > FLT_MAX || x < -FLT_MAX) return;
+        const unsigned long long n1 = n;
+        n = n + 1;
+        const double dn = (double)n;
+        const double delta = __dsub_rn(x, mean);
+        const double delta_n = __ddiv_rn(delta, dn);
+        const double delta_n2 = __dmul_rn(delta_n, delta_n);
+        const double term1 = __dmul_rn(__dmul_rn(delta, delta_n), (double)n1);
+        mean = __dadd_rn(mean, delta_n);
+        // size_t arithmetic of the reference: n*n - 3n + 3 and n - 2 (wraps at n = 1)
+        const double c4 = (double)(n * n - 3 * n + 3);
+        const double c3 = (double)(n - 2);
+        M4 = __dsub_rn(__dadd_rn(__dadd_rn(M4, __dmul_rn(__dmul_rn(term1, delta_n2), c4)),
+                                 __dmul_rn(__dmul_rn(6.0, delta_n2), M2)),
+                       __dmul_rn(__dmul_rn(4.0, delta_n), M3));
+        M3 = __dsub_rn(__dadd_rn(M3, __dmul_rn(__dmul_rn(term1, delta_n), c3)), __dmul_rn(__dmul_rn(3.0, delta_n), M2));
+        M2 = __dadd_rn(M2, term1);
+    }
+};
+
+__global__ void __launch_bounds__(128) k_comb(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                              const FJob *__restrict__ jobs, double *__restrict__ feat) {
     __shared__ double M[4][4][20];  // dir, moment, sample
     __shared__ int nsamp;
     const FJob J = jobs[blockIdx.x];
     const Plane P = planes[J.plane];
     const long long m = P.h, n = P.w, n2 = n / 2, m2 = m / 2;
     const double *p = arena + P.off;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (threadIdx.x == 0) {
         double step = (double)m / 10.0;
         if (step < 1.0) step = 1.0;
         int k = 0;
         for (double mp = 1.0 - m; mp <= m; mp += step) k++;
-        nsamp = k;
+        nsamp = k < 20 ? k : 20;
     }
     for (int i = threadIdx.x; i < 4 * 4 * 20; i += blockDim.x) (&M[0][0][0])[i] = 0.0;
     __syncthreads();
-    for (int line = wid; line < 4 * nsamp; line += nw) {
+    for (int line = threadIdx.x; line < 4 * nsamp; line += blockDim.x) {
         const int dir = line / nsamp, si = line % nsamp;
         double step = (double)m / 10.0;
         if (step < 1.0) step = 1.0;
@@ -367,43 +357,16 @@ __global__ void __launch_bounds__(512) k_comb(const double *__restrict__ arena, 
         for (int q = 0; q < si; q++) mp += step;  // same accumulation as the reference loop
         const long long ii = llround(mp);
         const long long len = (dir == 3) ? n : m;
-        double s = 0;
-        long long cnt = 0;
-        for (long long j = lane; j < len; j += 32) {
+        CombMom4 mm;
+        for (long long j = 0; j < len; j++) {
             long long y, x;
-            if (comb_pixel(dir, j, ii, m, n, n2, m2, y, x)) {
-                double v = p[y * n + x];
-                if (!(isnan(v) || v > FLT_MAX || v < -FLT_MAX)) { s += v; cnt++; }
-            }
+            if (comb_pixel(dir, j, ii, m, n, n2, m2, y, x)) mm.add(p[y * n + x]);
         }
-        s = warp_sum(s);
-        cnt = warp_sum_ll(cnt);
-        s = __shfl_sync(0xffffffffu, s, 0);
-        cnt = __shfl_sync(0xffffffffu, cnt, 0);
-        const double mean = cnt ? s / cnt : 0.0;
-        double a2 = 0, a3 = 0, a4 = 0;
-        for (long long j = lane; j < len; j += 32) {
-            long long y, x;
-            if (comb_pixel(dir, j, ii, m, n, n2, m2, y, x)) {
-                double v = p[y * n + x];
-                if (!(isnan(v) || v > FLT_MAX || v < -FLT_MAX)) {
-                    double d = v - mean, d2 = d * d;
-                    a2 += d2;
-                    a3 += d2 * d;
-                    a4 += d2 * d2;
-                }
-            }
-        }
-        a2 = warp_sum(a2);
-        a3 = warp_sum(a3);
-        a4 = warp_sum(a4);
-        if (lane == 0) {
-            const double nn = (double)cnt;
-            M[dir][0][si] = mean;
-            M[dir][1][si] = cnt > 2 ? sqrt(a2 / (nn - 1)) : 0.0;
-            M[dir][2][si] = cnt > 3 ? (sqrt(nn) * a3) / pow(a2, 1.5) : 0.0;
-            M[dir][3][si] = cnt > 4 ? (nn * a4) / (a2 * a2) : 0.0;
-        }
+        const double nn = (double)mm.n;
+        M[dir][0][si] = mm.mean;
+        M[dir][1][si] = mm.n > 2 ? sqrt(__ddiv_rn(mm.M2, (double)(mm.n - 1))) : 0.0;
+        M[dir][2][si] = mm.n > 3 ? __ddiv_rn(__dmul_rn(sqrt(nn), mm.M3), pow(mm.M2, 1.5)) : 0.0;
+        M[dir][3][si] = mm.n > 4 ? __ddiv_rn(__dmul_rn(nn, mm.M4), __dmul_rn(mm.M2, mm.M2)) : 0.0;
     }
     __syncthreads();
     if (threadIdx.x < 16) {
@@ -431,7 +394,7 @@ __global__ void __launch_bounds__(512) k_comb(const double *__restrict__ arena, 
 void launch_comb(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, double *feat) {
     if (njobs <= 0) return;
     WC_LAUNCH(c);
-    k_comb<<<njobs, 512, 0, c.st>>>(arena, planes, jobs, feat);
+    k_comb<<<njobs, 128, 0, c.st>>>(arena, planes, jobs, feat);
 }
 
 // ---------------------------------------------------------------- Radon

@@ -213,7 +213,8 @@ __device__ void uf_unite(int *L, int a, int b, long long cap) {
 
 // stage 0: init labels; 1: unions with the 4 earlier 8-neighbours; 2: flatten
 __global__ void k_ob_label(const double *__restrict__ arena, const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
-                           const OBJob *__restrict__ oj, const double *__restrict__ thr, double *__restrict__ ws, int stage) {
+                           const OBJob *__restrict__ oj, const double *__restrict__ thr, double *__restrict__ ws, int stage,
+                           long long uf_cap) {
     const FJob J = jobs[blockIdx.y];
     const OBJob O = oj[blockIdx.y];
     const Plane P = planes[J.plane];
@@ -222,20 +223,21 @@ __global__ void k_ob_label(const double *__restrict__ arena, const Plane *__rest
     int *L = (int *)(ws + O.lab_ws);
     const double *src = O.inverse ? ws + O.src_ws : arena + P.off;
     const double t = thr[blockIdx.y];
+    const long long cap = uf_cap > 0 ? uf_cap : n;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         if (stage == 0) {
             L[i] = (src[i] > t) ? (int)i : -1;
         } else if (stage == 1) {
             if (L[i] < 0) continue;
             const int y = (int)(i / W), x = (int)(i - (long long)y * W);
-            if (x > 0 && L[i - 1] >= 0) uf_unite(L, (int)i, (int)(i - 1), n);
+            if (x > 0 && L[i - 1] >= 0) uf_unite(L, (int)i, (int)(i - 1), cap);
             if (y > 0) {
-                if (x > 0 && L[i - W - 1] >= 0) uf_unite(L, (int)i, (int)(i - W - 1), n);
-                if (L[i - W] >= 0) uf_unite(L, (int)i, (int)(i - W), n);
-                if (x < W - 1 && L[i - W + 1] >= 0) uf_unite(L, (int)i, (int)(i - W + 1), n);
+                if (x > 0 && L[i - W - 1] >= 0) uf_unite(L, (int)i, (int)(i - W - 1), cap);
+                if (L[i - W] >= 0) uf_unite(L, (int)i, (int)(i - W), cap);
+                if (x < W - 1 && L[i - W + 1] >= 0) uf_unite(L, (int)i, (int)(i - W + 1), cap);
             }
         } else {
-            if (L[i] >= 0) L[i] = uf_find(L, (int)i, n);
+            if (L[i] >= 0) L[i] = uf_find(L, (int)i, cap);
         }
     }
 }
@@ -420,7 +422,8 @@ void launch_objects(Ctx &c, const double *arena, const Plane *planes, const Plan
     k_ob_otsu<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, inv_stats, jobs, oj, ws, thr);
     for (int stage = 0; stage < 3; stage++) {
         WC_LAUNCH(c);
-        k_ob_label<<<dim3(blocks, njobs), 256, 0, c.st>>>(arena, planes, jobs, oj, thr, ws, stage);
+        k_ob_label<<<dim3(blocks, njobs), 256, 0, c.st>>>(arena, planes, jobs, oj, thr, ws, stage,
+                                                          c.opt->union_find_cap);
     }
     WC_LAUNCH(c);
     k_ob_accum<<<dim3(blocks, njobs), 256, 0, c.st>>>(planes, jobs, oj, ws, acc);

@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj
 // group, with a barrier between dependent phases.
 template <int NW>
 __device__ void har_schur(double *__restrict__ A, const int n, double *__restrict__ rowsum, double *__restrict__ res,
-                          const int tid) {
+                          const int tid, const int iter_per_tone) {
     const int lane = tid & 31;
     constexpr int GS = 32 * NW;
     if (n < 3) {
@@ -532,7 +532,7 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
     double norm = 0;
     for (int j = 0; j < n; j++) norm = __dadd_rn(norm, rowsum[j]);
     const double eps = DBL_EPSILON;
-    const int maxIter = 40 * n;
+    const int maxIter = iter_per_tone * n;  // Eigen: m_maxIterationsPerRow (40) * n
     int iu = n - 1, iter = 0, totalIter = 0;
     double exshift = 0;
     bool failed = false;
@@ -822,7 +822,7 @@ __device__ __forceinline__ void hh_make3_df(const df v0, const df v1, const df v
 
 template <int NW>
 __device__ void har_schur_df(df *__restrict__ A, const int n, float *__restrict__ rowsum, double *__restrict__ res,
-                             const int tid) {
+                             const int tid, const int iter_per_tone) {
     const int lane = tid & 31;
     constexpr int GS = 32 * NW;
     if (n < 3) {
@@ -839,7 +839,7 @@ __device__ void har_schur_df(df *__restrict__ A, const int n, float *__restrict_
     float norm = 0.f;
     for (int j = 0; j < n; j++) norm = __fadd_rn(norm, rowsum[j]);
     const float eps = 0x1p-46f, nthr = __fmul_rn(eps, norm);
-    const int maxIter = 40 * n;
+    const int maxIter = iter_per_tone * n;  // Eigen: m_maxIterationsPerRow (40) * n
     int iu = n - 1, iter = 0, totalIter = 0;
     df exshift = {0.f, 0.f};
     bool failed = false;
@@ -1237,7 +1237,7 @@ __global__ void __launch_bounds__(256) k_har_hess_df(const HarJob *__restrict__ 
 template <bool MIXED>
 __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb,
                                                 const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat,
-                                                int max_groups) {
+                                                int max_groups, int iter_per_tone) {
     __shared__ double rowsum[4][256];
     // groups only while every large matrix can have an SM to itself; beyond that
     // the FP64 pipes are shared anyway and one warp per matrix issues fewer
@@ -1259,12 +1259,12 @@ __global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, c
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
     if (MIXED) {
         float *rs = (float *)rowsum[(int)blockIdx.x < nbig ? 0 : wq];
-        if ((int)blockIdx.x < nbig) har_schur_df<4>((df *)A, n, rs, res, threadIdx.x);
-        else har_schur_df<1>((df *)A, n, rs, res, threadIdx.x & 31);
+        if ((int)blockIdx.x < nbig) har_schur_df<4>((df *)A, n, rs, res, threadIdx.x, iter_per_tone);
+        else har_schur_df<1>((df *)A, n, rs, res, threadIdx.x & 31, iter_per_tone);
         return;
     }
-    if ((int)blockIdx.x < nbig) har_schur<4>(A, n, rowsum[0], res, threadIdx.x);
-    else har_schur<1>(A, n, rowsum[wq], res, threadIdx.x & 31);
+    if ((int)blockIdx.x < nbig) har_schur<4>(A, n, rowsum[0], res, threadIdx.x, iter_per_tone);
+    else har_schur<1>(A, n, rowsum[wq], res, threadIdx.x & 31, iter_per_tone);
 }
 
 // mean and range over the angles, permuted into the output order
@@ -1306,10 +1306,14 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     WC_LAUNCH(c);
     k_har_stats<<<dim3(njobs, 4), 256, 0, c.st>>>(jobs, hj, wsb);
     }
+    // the mixed form's f14 chain in pairs of floats, or (f14_exact) the FP64
+    // chain, whose f14 is bit-identical to the FP64 form's
+    const bool df14 = c.prec == WC_PREC_MIXED && !c.opt->f14_exact;
+    const int ipt = c.opt->qr_iter_per_tone;
     {
     ProfScope p2(c, "Haralick: Q");
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED) {
+    if (df14) {
         k_har_p_df<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
         WC_LAUNCH(c);
         k_har_q_df<<<dim3(njobs, 4, 4), 32 * Q_WARPS, 0, c.st>>>(hj, wsb);
@@ -1320,7 +1324,7 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     {
     ProfScope p3(c, "Haralick: Hessenberg");
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED) k_har_hess_df<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
+    if (df14) k_har_hess_df<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
     else k_har_hess<<<dim3(njobs, 4), 256, 0, c.st>>>(hj, wsb);
     }
     {
@@ -1328,10 +1332,12 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     WC_LAUNCH(c);
     k_har_order<<<1, 256, 0, c.st>>>(hj, wsb, 4 * njobs, perm);
     WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED) k_har_qr<true><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, c.sms);
-    // the FP64 form keeps the 4-warp groups at every batch size (measured faster there:
-    // its other families load the FP64 pipes more)
-    else k_har_qr<false><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, 1 << 30);
+    if (df14)
+        k_har_qr<true><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, c.sms, ipt);
+    // the FP64 chain keeps the 4-warp groups at every batch size (measured faster in
+    // the FP64 form: its other families load the FP64 pipes more)
+    else
+        k_har_qr<false><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, 1 << 30, ipt);
     }
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);

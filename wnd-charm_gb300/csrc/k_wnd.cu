@@ -111,6 +111,34 @@ __global__ void k_wnd_gather(const double *__restrict__ X, int rows, int F, cons
     Xc[(long long)k * rows + s] = v;
 }
 
+// rows of X (by index) gathered and normalised into the FP64 kernel's
+// column-major layout, Xc[k * n + i]
+__global__ void k_wnd_gather_rows(const double *__restrict__ X, const int *__restrict__ rowsel, int n, int F,
+                                  const int *__restrict__ keep, int K, const double *__restrict__ mins,
+                                  const double *__restrict__ maxs, double *__restrict__ Xc) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= (long long)n * K) return;
+    const int k = (int)(q / n), i = (int)(q - (long long)k * n);
+    const int f = keep[k];
+    const double mn = mins[f], mx = maxs[f];
+    double v = X[(long long)rowsel[i] * F + f];
+    if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) v = 0;
+    else if (v > mx) v = 100;
+    else v = 100 * ((v - mn) / (mx - mn));
+    Xc[(long long)k * n + i] = v;
+}
+
+__global__ void k_wnd_scatter_rows(const int *__restrict__ rowsel, int n, int C, const double *__restrict__ sp,
+                                   const int *__restrict__ spred, const double *__restrict__ snorm,
+                                   double *__restrict__ probs, int *__restrict__ pred, double *__restrict__ norm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int t = rowsel[i];
+    for (int c = 0; c < C; c++) probs[(long long)t * C + c] = sp[(long long)i * C + c];
+    pred[t] = spred[i];
+    norm[t] = snorm[i];
+}
+
 #define WT 64
 #define WK 16
 // distances for a 64-test x 64-train tile, then per-class sums of d^-5 in
@@ -380,33 +408,23 @@ using namespace wc;
         if (e_ != cudaSuccess) { rc = set_err(WC_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); goto done; } \
     } while (0)
 
-extern "C" int wc_wnd_fit(wc_engine *E, const double *train, int N, int F, const int *labels, int C, double frac,
-                          double *weights, double *mins, double *maxs) {
-    if (!E || !train || !labels || !weights || !mins || !maxs || N < 1 || F < 1 || C < 1 || C > 16)
-        return set_err(WC_ERR_ARG, "wc_wnd_fit: bad arguments (C must be 1..16)");
+// normalize + SetFisherScores over device rows: dmin/dmax (device) get the
+// per-feature range, weights (host) the thresholded Fisher scores
+static int wnd_fit_dev(wc_engine *E, const double *dX, int N, int F, const int *dy, int C, double frac, double *weights,
+                       double *dmin, double *dmax) {
     cudaStream_t st;
     long long *launches;
     int rc = engine_device(E, &st, &launches);
     if (rc) return rc;
-    double *dX = nullptr, *dXn = nullptr, *dmin = nullptr, *dmax = nullptr, *dw = nullptr;
-    int *dy = nullptr;
-    const size_t xb = (size_t)N * F * sizeof(double);
-    CKW(cudaMalloc(&dX, xb));
-    CKW(cudaMalloc(&dXn, xb));
-    CKW(cudaMalloc(&dmin, F * sizeof(double)));
-    CKW(cudaMalloc(&dmax, F * sizeof(double)));
+    double *dXn = nullptr, *dw = nullptr;
+    CKW(cudaMalloc(&dXn, (size_t)N * F * sizeof(double)));
     CKW(cudaMalloc(&dw, F * sizeof(double)));
-    CKW(cudaMalloc(&dy, N * sizeof(int)));
-    CKW(cudaMemcpyAsync(dX, train, xb, cudaMemcpyHostToDevice, st));
-    CKW(cudaMemcpyAsync(dy, labels, N * sizeof(int), cudaMemcpyHostToDevice, st));
     ++*launches;
     k_wnd_minmax<<<F, 256, 0, st>>>(dX, N, F, dmin, dmax, dXn);
     ++*launches;
     k_wnd_fisher<<<F, 256, 0, st>>>(dXn, dy, N, F, C, dw);
     CKW(cudaGetLastError());
     CKW(cudaMemcpyAsync(weights, dw, F * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CKW(cudaMemcpyAsync(mins, dmin, F * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CKW(cudaMemcpyAsync(maxs, dmax, F * sizeof(double), cudaMemcpyDeviceToHost, st));
     CKW(cudaStreamSynchronize(st));
     {
         // threshold at the weight of sorted (descending) rank floor(frac*F + 0.5)
@@ -420,17 +438,220 @@ extern "C" int wc_wnd_fit(wc_engine *E, const double *train, int N, int F, const
         }
     }
 done:
-    cudaFree(dX);
     cudaFree(dXn);
+    cudaFree(dw);
+    return rc;
+}
+
+extern "C" int wc_wnd_fit(wc_engine *E, const double *train, int N, int F, const int *labels, int C, double frac,
+                          double *weights, double *mins, double *maxs) {
+    if (!E || !train || !labels || !weights || !mins || !maxs || N < 1 || F < 1 || C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_fit: bad arguments (C must be 1..16)");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    double *dX = nullptr, *dmin = nullptr, *dmax = nullptr;
+    int *dy = nullptr;
+    const size_t xb = (size_t)N * F * sizeof(double);
+    CKW(cudaMalloc(&dX, xb));
+    CKW(cudaMalloc(&dmin, F * sizeof(double)));
+    CKW(cudaMalloc(&dmax, F * sizeof(double)));
+    CKW(cudaMalloc(&dy, N * sizeof(int)));
+    CKW(cudaMemcpyAsync(dX, train, xb, cudaMemcpyHostToDevice, st));
+    CKW(cudaMemcpyAsync(dy, labels, N * sizeof(int), cudaMemcpyHostToDevice, st));
+    if ((rc = wnd_fit_dev(E, dX, N, F, dy, C, frac, weights, dmin, dmax))) goto done;
+    CKW(cudaMemcpyAsync(mins, dmin, F * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKW(cudaMemcpyAsync(maxs, dmax, F * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKW(cudaStreamSynchronize(st));
+done:
+    cudaFree(dX);
     cudaFree(dmin);
     cudaFree(dmax);
-    cudaFree(dw);
     cudaFree(dy);
     return rc;
 }
 
-// classify2 for T test rows; with tiles > 0 the rows are n = T / tiles images'
-// tiles and ClassifyImage's per-image results are returned instead of the rows'.
+extern "C" int wc_wnd_fit_device(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                                 double frac, double *weights, double *mins, double *maxs) {
+    if (!E || !train || !labels || !weights || !mins || !maxs || N < 1 || F < 1 || C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_fit_device: bad arguments (C must be 1..16)");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    std::vector<double> w(F);
+    if ((rc = wnd_fit_dev(E, train, N, F, labels, C, frac, w.data(), mins, maxs))) return rc;
+    CKW(cudaMemcpyAsync(weights, w.data(), F * sizeof(double), cudaMemcpyHostToDevice, st));
+    CKW(cudaStreamSynchronize(st));
+done:
+    return rc;
+}
+
+namespace wc {
+int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double *dX, int N, int F, const int *labels,
+                    int C, const double *dT, int T, const std::vector<int> &keep, const std::vector<double> &w,
+                    const double *dmin, const double *dmax, double *dprob, int *dpred, double *dnorm,
+                    std::vector<int> &recheck, long long *tc_ctas);
+bool wnd_tc_supported(int K);
+int engine_sms(const wc_engine *E);
+}  // namespace wc
+
+namespace {
+
+// what the last classification did (wc_wnd_last_stats)
+thread_local long long g_last_stats[4] = {0, 0, 0, 0};
+
+// device buffers freed together
+struct WBufs {
+    std::vector<void *> ptrs;
+    template <typename T>
+    int get(T **p, size_t bytes) {
+        *p = nullptr;
+        void *q = nullptr;
+        if (cudaMalloc(&q, bytes ? bytes : 16) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(WC_ERR_NOMEM, "cudaMalloc of %zu bytes failed", bytes);
+        }
+        ptrs.push_back(q);
+        *p = (T *)q;
+        return WC_OK;
+    }
+    ~WBufs() {
+        for (void *q : ptrs) cudaFree(q);
+    }
+};
+
+#define CKR(x)                                                                                        \
+    do {                                                                                              \
+        cudaError_t e_ = (x);                                                                         \
+        if (e_ != cudaSuccess) return set_err(WC_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));     \
+    } while (0)
+
+// The FP64 kernel (the reference's order and skips) for the test rows `rows`
+// of dT; results scattered into dprob/dpred/dnorm.  chunks spread a few rows
+// over the whole GPU.
+int fp64_rows(cudaStream_t st, long long *launches, const double *dX, const double *dT, int N, int F, const int *dy,
+              int C, const std::vector<int> &keep_h, const int *dkeep, const double *dw2, const double *dmin,
+              const double *dmax, const std::vector<int> &rows, double *dprob, int *dpred, double *dnorm,
+              bool all_rows) {
+    const int K = (int)keep_h.size();
+    const int n = (int)rows.size();
+    if (!n) return WC_OK;
+    WBufs B;
+    double *dXc, *dTc, *dps, *sp, *sn;
+    long long *dpc;
+    int *drows, *spred;
+    const int nchunk = all_rows ? std::max(1, std::min(64, (N + 4095) / 4096)) : std::max(1, std::min(512, N / 256));
+    const int per = ((N + nchunk - 1) / nchunk + WT - 1) / WT * WT;
+    int rc;
+    if ((rc = B.get(&dXc, (size_t)N * std::max(K, 1) * 8)) || (rc = B.get(&dTc, (size_t)n * std::max(K, 1) * 8)) ||
+        (rc = B.get(&dps, (size_t)n * nchunk * C * 8)) || (rc = B.get(&dpc, (size_t)n * nchunk * C * 8)) ||
+        (rc = B.get(&sp, (size_t)n * C * 8)) || (rc = B.get(&sn, (size_t)n * 8)) || (rc = B.get(&drows, n * 4)) ||
+        (rc = B.get(&spred, n * 4)))
+        return rc;
+    CKR(cudaMemcpyAsync(drows, rows.data(), n * 4, cudaMemcpyHostToDevice, st));
+    if (K) {
+        ++*launches;
+        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, dXc);
+        ++*launches;
+        k_wnd_gather_rows<<<(int)(((long long)n * K + 255) / 256), 256, 0, st>>>(dT, drows, n, F, dkeep, K, dmin,
+                                                                                     dmax, dTc);
+    }
+    *launches += 3;
+    k_wnd_dist<<<dim3((n + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, n, dXc, N, dy, dw2, K, C, per, dps, dpc);
+    k_wnd_finish<<<(n + 127) / 128, 128, 0, st>>>(dps, dpc, n, nchunk, C, sp, spred, sn);
+    k_wnd_scatter_rows<<<(n + 127) / 128, 128, 0, st>>>(drows, n, C, sp, spred, sn, dprob, dpred, dnorm);
+    CKR(cudaGetLastError());
+    CKR(cudaStreamSynchronize(st));
+    return WC_OK;
+}
+
+}  // namespace
+
+// classify2 over device-resident rows: dX (N x F), dT (T x F), labels / weights
+// on the host, dmin / dmax on the device; probabilities, classes and
+// normalisation factors to dprob / dpred / dnorm (device).
+static int wnd_classify_dev(wc_engine *E, const double *dX, int N, int F, const int *labels, int C,
+                            const double *weights, const double *dmin, const double *dmax, const double *dT, int T,
+                            double *dprob, int *dpred, double *dnorm) {
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    std::vector<int> keep;
+    std::vector<double> w, w2;
+    for (int f = 0; f < F; f++)
+        if (!(weights[f] < DBL_EPSILON)) {
+            keep.push_back(f);
+            w.push_back(weights[f]);
+            w2.push_back(std::pow(weights[f], 2));
+        }
+    const int K = (int)keep.size();
+    const bool mixed = engine_precision(E) == WC_PREC_MIXED;
+    WBufs B;
+    int *dy, *dkeep;
+    double *dw2;
+    if ((rc = B.get(&dy, N * 4)) || (rc = B.get(&dkeep, std::max(K, 1) * 4)) || (rc = B.get(&dw2, std::max(K, 1) * 8)))
+        return rc;
+    CKR(cudaMemcpyAsync(dy, labels, N * 4, cudaMemcpyHostToDevice, st));
+    if (K) {
+        CKR(cudaMemcpyAsync(dkeep, keep.data(), K * 4, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync(dw2, w2.data(), K * 8, cudaMemcpyHostToDevice, st));
+    }
+    g_last_stats[0] = 0;
+    g_last_stats[1] = 0;
+    g_last_stats[2] = K;
+    g_last_stats[3] = 0;
+    if (mixed && wnd_tc_supported(K)) {
+        // tensor cores, then the FP64 kernel for the rows they cannot certify
+        std::vector<int> rows;
+        long long ctas = 0;
+        rc = wnd_tc_classify(st, launches, engine_sms(E), dX, N, F, labels, C, dT, T, keep, w, dmin, dmax, dprob, dpred,
+                             dnorm, rows, &ctas);
+        if (rc == WC_ERR_UNSUPPORTED) goto pairs;
+        if (rc) return rc;
+        g_last_stats[0] = 1;
+        g_last_stats[1] = (long long)rows.size();
+        g_last_stats[3] = ctas;
+        return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, rows, dprob, dpred, dnorm,
+                         false);
+    }
+pairs:
+    if (mixed && K) {
+        // pairs of floats on the CUDA cores (more features than the tensor-core digits allow)
+        const int nchunk = std::max(1, std::min(64, (N + 4095) / 4096));
+        const int per = ((N + nchunk - 1) / nchunk + WT - 1) / WT * WT;
+        double *dXc, *dTc, *dps;
+        long long *dpc;
+        float2 *fX, *fT, *fw;
+        if ((rc = B.get(&dXc, (size_t)N * K * 8)) || (rc = B.get(&dTc, (size_t)T * K * 8)) ||
+            (rc = B.get(&dps, (size_t)T * nchunk * C * 8)) || (rc = B.get(&dpc, (size_t)T * nchunk * C * 8)) ||
+            (rc = B.get(&fX, (size_t)N * K * 8)) || (rc = B.get(&fT, (size_t)T * K * 8)) || (rc = B.get(&fw, K * 8)))
+            return rc;
+        *launches += 7;
+        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, dXc);
+        k_wnd_gather<<<(int)(((long long)T * K + 255) / 256), 256, 0, st>>>(dT, T, F, dkeep, K, dmin, dmax, dTc);
+        k_wnd_split<<<1024, 256, 0, st>>>(dXc, (long long)N * K, fX);
+        k_wnd_split<<<1024, 256, 0, st>>>(dTc, (long long)T * K, fT);
+        k_wnd_split<<<1, 256, 0, st>>>(dw2, K, fw);
+        k_wnd_dist_df<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(fT, T, fX, N, dy, fw, K, C, per, dps, dpc);
+        k_wnd_finish<<<(T + 127) / 128, 128, 0, st>>>(dps, dpc, T, nchunk, C, dprob, dpred, dnorm);
+        CKR(cudaGetLastError());
+        CKR(cudaStreamSynchronize(st));
+        return WC_OK;
+    }
+    {
+        std::vector<int> all(T);
+        for (int t = 0; t < T; t++) all[t] = t;
+        return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, all, dprob, dpred, dnorm,
+                         true);
+    }
+}
+
+// classify2 for T test rows with host buffers; with tiles > 0 the rows are
+// n = T / tiles images' tiles and ClassifyImage's per-image results are
+// returned instead of the rows'.
 static int wnd_classify(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
                         const double *weights, const double *mins, const double *maxs, const double *test, int T,
                         double *probs, int *pred, int tiles, int max_tile, double *iprobs, int *ipred, double *inorm) {
@@ -438,109 +659,36 @@ static int wnd_classify(wc_engine *E, const double *train, int N, int F, const i
     long long *launches;
     int rc = engine_device(E, &st, &launches);
     if (rc) return rc;
-    std::vector<int> keep;
-    std::vector<double> w2;
-    for (int f = 0; f < F; f++)
-        if (!(weights[f] < DBL_EPSILON)) {
-            keep.push_back(f);
-            w2.push_back(std::pow(weights[f], 2));
-        }
-    const int K = (int)keep.size();
-    const int nchunk = std::max(1, std::min(64, (N + 4095) / 4096));
-    const int per = ((N + nchunk - 1) / nchunk + WT - 1) / WT * WT;
     const int n_img = tiles > 0 ? T / tiles : 0;
-    double *dX = nullptr, *dT = nullptr, *dXc = nullptr, *dTc = nullptr, *dmin = nullptr, *dmax = nullptr, *dw2 = nullptr,
-           *dps = nullptr, *dprob = nullptr, *dnorm = nullptr, *diprob = nullptr, *dinorm = nullptr;
-    int *dipred = nullptr;
-    long long *dpc = nullptr;
-    int *dkeep = nullptr, *dy = nullptr, *dpred = nullptr;
-    CKW(cudaMalloc(&dX, (size_t)N * F * 8));
-    CKW(cudaMalloc(&dT, (size_t)T * F * 8));
-    CKW(cudaMalloc(&dXc, (size_t)N * std::max(K, 1) * 8));
-    CKW(cudaMalloc(&dTc, (size_t)T * std::max(K, 1) * 8));
-    CKW(cudaMalloc(&dmin, F * 8));
-    CKW(cudaMalloc(&dmax, F * 8));
-    CKW(cudaMalloc(&dw2, std::max(K, 1) * 8));
-    CKW(cudaMalloc(&dkeep, std::max(K, 1) * 4));
-    CKW(cudaMalloc(&dy, N * 4));
-    CKW(cudaMalloc(&dps, (size_t)T * nchunk * C * 8));
-    CKW(cudaMalloc(&dpc, (size_t)T * nchunk * C * 8));
-    CKW(cudaMalloc(&dprob, (size_t)T * C * 8));
-    CKW(cudaMalloc(&dpred, (size_t)T * 4));
-    CKW(cudaMalloc(&dnorm, (size_t)T * 8));
-    if (n_img) {
-        CKW(cudaMalloc(&diprob, (size_t)n_img * C * 8));
-        CKW(cudaMalloc(&dipred, (size_t)n_img * 4));
-        CKW(cudaMalloc(&dinorm, (size_t)n_img * 8));
-    }
-    CKW(cudaMemcpyAsync(dX, train, (size_t)N * F * 8, cudaMemcpyHostToDevice, st));
-    CKW(cudaMemcpyAsync(dT, test, (size_t)T * F * 8, cudaMemcpyHostToDevice, st));
-    CKW(cudaMemcpyAsync(dmin, mins, F * 8, cudaMemcpyHostToDevice, st));
-    CKW(cudaMemcpyAsync(dmax, maxs, F * 8, cudaMemcpyHostToDevice, st));
-    CKW(cudaMemcpyAsync(dy, labels, N * 4, cudaMemcpyHostToDevice, st));
-    if (K) {
-        CKW(cudaMemcpyAsync(dw2, w2.data(), K * 8, cudaMemcpyHostToDevice, st));
-        CKW(cudaMemcpyAsync(dkeep, keep.data(), K * 4, cudaMemcpyHostToDevice, st));
-        ++*launches;
-        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, dXc);
-        ++*launches;
-        k_wnd_gather<<<(int)(((long long)T * K + 255) / 256), 256, 0, st>>>(dT, T, F, dkeep, K, dmin, dmax, dTc);
-    }
-    if (engine_precision(E) == WC_PREC_MIXED && K) {
-        float2 *fX = nullptr, *fT = nullptr, *fw = nullptr;
-        CKW(cudaMalloc(&fX, (size_t)N * K * 8));
-        CKW(cudaMalloc(&fT, (size_t)T * K * 8));
-        CKW(cudaMalloc(&fw, (size_t)K * 8));
-        *launches += 4;
-        k_wnd_split<<<1024, 256, 0, st>>>(dXc, (long long)N * K, fX);
-        k_wnd_split<<<1024, 256, 0, st>>>(dTc, (long long)T * K, fT);
-        k_wnd_split<<<1, 256, 0, st>>>(dw2, K, fw);
-        k_wnd_dist_df<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(fT, T, fX, N, dy, fw, K, C, per, dps, dpc);
-        const cudaError_t le = cudaGetLastError();
-        cudaStreamSynchronize(st);
-        cudaFree(fX);
-        cudaFree(fT);
-        cudaFree(fw);
-        CKW(le);
-    } else {
-        ++*launches;
-        k_wnd_dist<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, T, dXc, N, dy, dw2, K, C, per, dps, dpc);
-    }
-    ++*launches;
-    k_wnd_finish<<<(T + 127) / 128, 128, 0, st>>>(dps, dpc, T, nchunk, C, dprob, dpred, dnorm);
-    CKW(cudaGetLastError());
+    WBufs B;
+    double *dX, *dT, *dmin, *dmax, *dprob, *dnorm, *diprob = nullptr, *dinorm = nullptr;
+    int *dpred, *dipred = nullptr;
+    if ((rc = B.get(&dX, (size_t)N * F * 8)) || (rc = B.get(&dT, (size_t)T * F * 8)) || (rc = B.get(&dmin, F * 8)) ||
+        (rc = B.get(&dmax, F * 8)) || (rc = B.get(&dprob, (size_t)T * C * 8)) || (rc = B.get(&dpred, (size_t)T * 4)) ||
+        (rc = B.get(&dnorm, (size_t)T * 8)))
+        return rc;
+    if (n_img && ((rc = B.get(&diprob, (size_t)n_img * C * 8)) || (rc = B.get(&dipred, (size_t)n_img * 4)) ||
+                  (rc = B.get(&dinorm, (size_t)n_img * 8))))
+        return rc;
+    CKR(cudaMemcpyAsync(dX, train, (size_t)N * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dT, test, (size_t)T * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dmin, mins, F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dmax, maxs, F * 8, cudaMemcpyHostToDevice, st));
+    if ((rc = wnd_classify_dev(E, dX, N, F, labels, C, weights, dmin, dmax, dT, T, dprob, dpred, dnorm))) return rc;
     if (n_img) {
         ++*launches;
         k_wnd_tiles<<<(n_img + 127) / 128, 128, 0, st>>>(dprob, dpred, dnorm, n_img, tiles, C, max_tile, diprob, dipred,
                                                          dinorm);
-        CKW(cudaGetLastError());
-        CKW(cudaMemcpyAsync(iprobs, diprob, (size_t)n_img * C * 8, cudaMemcpyDeviceToHost, st));
-        CKW(cudaMemcpyAsync(ipred, dipred, (size_t)n_img * 4, cudaMemcpyDeviceToHost, st));
-        if (inorm) CKW(cudaMemcpyAsync(inorm, dinorm, (size_t)n_img * 8, cudaMemcpyDeviceToHost, st));
+        CKR(cudaGetLastError());
+        CKR(cudaMemcpyAsync(iprobs, diprob, (size_t)n_img * C * 8, cudaMemcpyDeviceToHost, st));
+        CKR(cudaMemcpyAsync(ipred, dipred, (size_t)n_img * 4, cudaMemcpyDeviceToHost, st));
+        if (inorm) CKR(cudaMemcpyAsync(inorm, dinorm, (size_t)n_img * 8, cudaMemcpyDeviceToHost, st));
     } else {
-        CKW(cudaMemcpyAsync(probs, dprob, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
-        CKW(cudaMemcpyAsync(pred, dpred, (size_t)T * 4, cudaMemcpyDeviceToHost, st));
+        CKR(cudaMemcpyAsync(probs, dprob, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
+        CKR(cudaMemcpyAsync(pred, dpred, (size_t)T * 4, cudaMemcpyDeviceToHost, st));
     }
-    CKW(cudaStreamSynchronize(st));
-done:
-    cudaFree(dX);
-    cudaFree(dT);
-    cudaFree(dXc);
-    cudaFree(dTc);
-    cudaFree(dmin);
-    cudaFree(dmax);
-    cudaFree(dw2);
-    cudaFree(dkeep);
-    cudaFree(dy);
-    cudaFree(dps);
-    cudaFree(dpc);
-    cudaFree(dprob);
-    cudaFree(dpred);
-    cudaFree(dnorm);
-    cudaFree(diprob);
-    cudaFree(dipred);
-    cudaFree(dinorm);
-    return rc;
+    CKR(cudaStreamSynchronize(st));
+    return WC_OK;
 }
 
 extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
@@ -562,4 +710,32 @@ extern "C" int wc_wnd_classify_images(wc_engine *E, const double *train, int N, 
         return set_err(WC_ERR_ARG, "wc_wnd_classify_images: bad arguments (C must be 1..16, tiles >= 1)");
     return wnd_classify(E, train, N, F, labels, C, weights, mins, maxs, test, n_images * tiles, nullptr, nullptr, tiles,
                         max_tile ? 1 : 0, probs, pred, norm_factors);
+}
+
+extern "C" int wc_wnd_classify_device(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                                      const double *weights, const double *mins, const double *maxs,
+                                      const double *test, int T, double *probs, int *pred) {
+    if (!E || !train || !labels || !weights || !mins || !maxs || !test || !probs || !pred || N < 1 || F < 1 || T < 1 ||
+        C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_classify_device: bad arguments (C must be 1..16)");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    // the labels and weights drive host-side choices (class order, kept features)
+    std::vector<int> y(N);
+    std::vector<double> w(F);
+    CKR(cudaMemcpyAsync(y.data(), labels, N * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(w.data(), weights, F * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    WBufs B;
+    double *dnorm;
+    if ((rc = B.get(&dnorm, (size_t)T * 8))) return rc;
+    return wnd_classify_dev(E, train, N, F, y.data(), C, w.data(), mins, maxs, test, T, probs, pred, dnorm);
+}
+
+extern "C" int wc_wnd_last_stats(long long *stats) {
+    if (!stats) return set_err(WC_ERR_ARG, "wc_wnd_last_stats: null stats");
+    for (int i = 0; i < 4; i++) stats[i] = g_last_stats[i];
+    return WC_OK;
 }

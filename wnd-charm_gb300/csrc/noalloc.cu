@@ -10,9 +10,11 @@
 // floor((height+9)/2) x 2 doubles) lives in a file-scope static device array of
 // fixed size instead of an allocation.
 //
-// The first call on each device looks up that array's device address (with
-// the device current) and keeps it; make that first call before any stream
-// capture begins.
+// The array's device address is looked up with the calling thread's current
+// device on every call (a cheap query once the library's device code is
+// loaded), so a cudaDeviceReset, which can move the array, never leaves a stale
+// address behind.  The first call on a device loads the library's device code
+// there; make that first call before any stream capture begins.
 //
 // The array is loaded with the library on every GPU that uses it and stays
 // allocated there until the process exits.  Every call shares it, so calls
@@ -25,10 +27,11 @@
 // of Wavelet::transform2D with zero padding, src/transforms/wavelet/Wavelet.cpp:136-434).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/wndcharm_gb300.h"
+#include "kwavelet.cuh"
 
 namespace wc {
 int set_err(int code, const char *fmt, ...);
@@ -41,100 +44,74 @@ namespace {
 constexpr long long kScratchDoubles = 1081344;
 static __device__ __align__(256) double g_wavelet_scratch[kScratchDoubles];
 
-__constant__ double c_lo[10] = {0.027333068345077982, 0.029519490925774643, -0.039134249302383094,
-                                0.1993975339773936,   0.72340769040242059,  0.63397896345821192,
-                                0.016602105764522319, -0.17532808990845047, -0.021101834024758855,
-                                0.019538882735286728};
-__constant__ double c_hi[10] = {-0.019538882735286728, -0.021101834024758855, 0.17532808990845047,
-                                0.016602105764522319,  -0.63397896345821192,  0.72340769040242059,
-                                -0.1993975339773936,   -0.039134249302383094, -0.029519490925774643,
-                                0.027333068345077982};
-
-// column pass: for every column x, approx/detail along y into the scratch
+// column pass: for every column x, approximation/detail along y into the
+// scratch; rows o advance by the grid's y extent, so any height fits the grid
 __global__ void k_wav_y(const double *__restrict__ in, int X, int Y, double *__restrict__ tmp) {
-    const int oy = (Y + 9) / 2;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= X || o >= oy) return;
-    const int i = 2 * o + 1;
-    double a = 0, d = 0;
-#pragma unroll
-    for (int j = 0; j < 10; j++) {
-        const int k = i - j;
-        if (k >= 0 && k < Y) {
-            const double v = in[(long long)k * X + x];
-            a = __dadd_rn(a, __dmul_rn(v, c_lo[j]));
-            d = __dadd_rn(d, __dmul_rn(v, c_hi[j]));
-        }
+    const int oy = sym5_out(Y);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= X) return;
+    for (int o = blockIdx.y * blockDim.y + threadIdx.y; o < oy; o += gridDim.y * blockDim.y) {
+        double a, d;
+        sym5_col(in, X, Y, x, o, a, d);
+        double *t = tmp + sym5_tmp_index(x, oy, o);
+        t[0] = a;
+        t[1] = d;
     }
-    tmp[((long long)x * oy + o) * 2 + 0] = a;
-    tmp[((long long)x * oy + o) * 2 + 1] = d;
 }
 
 // row pass of both column outputs, placed in the four quadrants
 __global__ void k_wav_x(const double *__restrict__ tmp, int X, int Y, double *__restrict__ out) {
-    const int ox = (X + 9) / 2, oy = (Y + 9) / 2, W = 2 * ox;
-    const int u = blockIdx.x * blockDim.x + threadIdx.x, o = blockIdx.y * blockDim.y + threadIdx.y;
-    if (u >= ox || o >= oy) return;
-    const int i = 2 * u + 1;
-    double a1 = 0, d1 = 0, a2 = 0, d2 = 0;
-#pragma unroll
-    for (int j = 0; j < 10; j++) {
-        const int k = i - j;
-        if (k >= 0 && k < X) {
-            const double va = tmp[((long long)k * oy + o) * 2 + 0], vd = tmp[((long long)k * oy + o) * 2 + 1];
-            a1 = __dadd_rn(a1, __dmul_rn(va, c_lo[j]));
-            d1 = __dadd_rn(d1, __dmul_rn(va, c_hi[j]));
-            a2 = __dadd_rn(a2, __dmul_rn(vd, c_lo[j]));
-            d2 = __dadd_rn(d2, __dmul_rn(vd, c_hi[j]));
-        }
+    const int ox = sym5_out(X), oy = sym5_out(Y);
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= ox) return;
+    for (int o = blockIdx.y * blockDim.y + threadIdx.y; o < oy; o += gridDim.y * blockDim.y) {
+        double a1, d1, a2, d2;
+        sym5_row(tmp, X, oy, u, o, a1, d1, a2, d2);
+        sym5_store(out, ox, oy, u, o, a1, d1, a2, d2);
     }
-    out[(long long)o * W + u] = d2;
-    out[(long long)(oy + o) * W + u] = a2;
-    out[(long long)o * W + ox + u] = d1;
-    out[(long long)(oy + o) * W + ox + u] = a1;
 }
 
-// Device address of the static array, looked up once per device with that
-// device current (in host code its name is only a host-side stand-in).
-std::mutex g_mu;
-double *g_ptr[64] = {nullptr};
-
+// Device address of the static array on the current device (in host code its
+// name is only a host-side stand-in, never a device address).
 int scratch_for_current_device(double **out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return wc::set_err(WC_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-    if (dev < 0 || dev >= 64) return wc::set_err(WC_ERR_UNSUPPORTED, "device %d out of range", dev);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_wavelet_scratch);
-        if (e != cudaSuccess || !p)
-            return wc::set_err(WC_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-        g_ptr[dev] = (double *)p;
-    }
-    *out = g_ptr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_wavelet_scratch);
+    if (e != cudaSuccess || !p)
+        return wc::set_err(WC_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    *out = (double *)p;
     return WC_OK;
 }
 
 }  // namespace
 
 extern "C" int wc_wavelet_noalloc(const double *d_in, int width, int height, double *d_out, void *stream) {
-    if (!d_in || !d_out || width < 1 || height < 1) return wc::set_err(WC_ERR_ARG, "wc_wavelet_noalloc: bad arguments");
+    if (!d_in || !d_out || width < 1 || height < 1 || width > (1 << 28) || height > (1 << 28))
+        return wc::set_err(WC_ERR_ARG, "wc_wavelet_noalloc: bad arguments");
     const long long need = (long long)width * ((height + 9) / 2) * 2;
     if (need > kScratchDoubles)
         return wc::set_err(WC_ERR_ARG,
                            "wc_wavelet_noalloc: %d x %d needs %lld scratch doubles, the static scratch holds %lld "
                            "(inputs up to 1024 x 1024 fit)",
                            width, height, need, kScratchDoubles);
+    // an error left pending by an earlier, unrelated call is reported, not
+    // taken (cleared) as this call's own
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return wc::set_err(WC_ERR_CUDA, "wc_wavelet_noalloc: a CUDA error from an earlier call is pending: %s",
+                           cudaGetErrorString(e));
     double *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    const int ox = (width + 9) / 2, oy = (height + 9) / 2;
+    const int ox = sym5_out(width), oy = sym5_out(height);
     const dim3 b(32, 8);
-    k_wav_y<<<dim3((width + 31) / 32, (oy + 7) / 8), b, 0, st>>>(d_in, width, height, scratch);
-    k_wav_x<<<dim3((ox + 31) / 32, (oy + 7) / 8), b, 0, st>>>(scratch, width, height, d_out);
-    cudaError_t e = cudaGetLastError();
+    const int gy = (int)std::min<long long>((oy + 7) / 8, 65535);
+    k_wav_y<<<dim3((width + 31) / 32, gy), b, 0, st>>>(d_in, width, height, scratch);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_wav_x<<<dim3((ox + 31) / 32, gy), b, 0, st>>>(scratch, width, height, d_out);
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return wc::set_err(WC_ERR_CUDA, "wc_wavelet_noalloc launch: %s", cudaGetErrorString(e));
     return WC_OK;
 }

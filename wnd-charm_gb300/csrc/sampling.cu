@@ -36,6 +36,8 @@ struct Opened {
 
 static int opened_geometry(const wc_sampling &s, int w, int h, Opened &o) {
     if (w < 1 || h < 1) return set_err(WC_ERR_ARG, "image of %d x %d pixels", w, h);
+    if (w > WC_MAX_SIDE || h > WC_MAX_SIDE || (long long)w * h > WC_MAX_PIXELS)
+        return set_err(WC_ERR_ARG, "image of %d x %d pixels is larger than this build accepts", w, h);
     o.cx = o.cy = 0;
     o.cw = w;
     o.ch = h;
@@ -248,7 +250,7 @@ static int prepare_samples(wc_engine *E, const wc_image_desc *imgs, int n, const
             CK(cudaMemcpyAsync(base + stage_off[b], imgs[b].pixels,
                                (size_t)imgs[b].width * imgs[b].height * elem_size(imgs[b].dtype),
                                cudaMemcpyHostToDevice, E->st));
-    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof};
+    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof, &E->opts};
     {
         ProfScope ps(ctx, "preprocess");
         const double *yh = E->tabs.d() + wf_tab;

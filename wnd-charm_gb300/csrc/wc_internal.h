@@ -121,6 +121,18 @@ struct Prof {
     }
 };
 
+// Engine options (wc_engine_set_option).
+struct Opts {
+    // mixed form: Haralick f14 (Q, Hessenberg reduction, real Schur) through the
+    // FP64 chain, bit-identical to the FP64 form, instead of pairs of floats
+    int f14_exact = 1;
+    // real-Schur iterations allowed per tone (Eigen's m_maxIterationsPerRow)
+    int qr_iter_per_tone = 40;
+    // union-find iterations allowed per pixel link in the object labelling;
+    // 0: the plane's pixel count (a bound no correct run reaches)
+    long long union_find_cap = 0;
+};
+
 // Launch context handed to every kernel launcher.
 struct Ctx {
     cudaStream_t st;
@@ -128,6 +140,7 @@ struct Ctx {
     int prec;             // WC_PREC_FP64 or WC_PREC_MIXED
     int sms;              // multiprocessors on the device
     Prof *prof;
+    const Opts *opt;      // the engine's options
 };
 struct ProfScope {  // may nest (e.g. a family's phases inside the family)
     Ctx &c;

@@ -303,6 +303,13 @@ class Engine(object):
     def set_stream(self, stream_ptr):
         check(lib().wc_engine_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
 
+    def set_option(self, name, value):
+        """Engine option (wc_engine_set_option): 'f14_exact' (mixed form: f14
+        through the FP64 chain, 1 by default), 'qr_iter_per_tone' (real-Schur
+        iterations allowed per tone, 40), 'union_find_cap' (labelling
+        iterations allowed per link, 0 = the pixel count)."""
+        check(lib().wc_engine_set_option(self._h, name.encode(), int(value)))
+
     def extract(self, plan, images, bits=16, out=None):
         """Features of a list of 2-D arrays (any sizes): (n, n_features) float64."""
         imgs = [_as_input(a) for a in images]
@@ -383,6 +390,33 @@ class Engine(object):
                                     T.ctypes.data_as(_lib.D), nt, probs.ctypes.data_as(_lib.D),
                                     pred.ctypes.data_as(_lib.I)))
         return probs, pred
+
+    def wnd_classify_device(self, train, labels, n_classes, weights, mins, maxs, test, probs, pred):
+        """wc_wnd_classify_device on device tensors (any objects with a
+        data_ptr(): float64 train (N, F), int32 labels, float64 weights / mins /
+        maxs (F,), float64 test (T, F); outputs float64 probs (T, C), int32 pred)."""
+        N, F = train.shape
+        T = test.shape[0]
+        vp = ctypes.c_void_p
+        check(lib().wc_wnd_classify_device(self._h, vp(train.data_ptr()), N, F, vp(labels.data_ptr()),
+                                           int(n_classes), vp(weights.data_ptr()), vp(mins.data_ptr()),
+                                           vp(maxs.data_ptr()), vp(test.data_ptr()), T, vp(probs.data_ptr()),
+                                           vp(pred.data_ptr())))
+
+    def wnd_fit_device(self, train, labels, n_classes, frac, weights, mins, maxs):
+        """wc_wnd_fit_device on device tensors (outputs float64 (F,) each)."""
+        N, F = train.shape
+        vp = ctypes.c_void_p
+        check(lib().wc_wnd_fit_device(self._h, vp(train.data_ptr()), N, F, vp(labels.data_ptr()), int(n_classes),
+                                      float(frac), vp(weights.data_ptr()), vp(mins.data_ptr()), vp(maxs.data_ptr())))
+
+    @staticmethod
+    def wnd_last_stats():
+        """What this thread's last WND-5 classification did: (tensor-core path
+        ran, test rows recomputed in FP64, weighted features, tensor-core CTAs)."""
+        st = (ctypes.c_longlong * 4)()
+        check(lib().wc_wnd_last_stats(st))
+        return tuple(int(v) for v in st)
 
     def wnd_classify_images(self, train, labels, n_classes, weights, mins, maxs, test, tiles, max_tile=False):
         """TrainingSet::ClassifyImage with WND-5 for images of `tiles`

@@ -59,6 +59,7 @@ def lib():
         L.wc_engine_destroy.argtypes = [vp]
         L.wc_engine_destroy.restype = None
         L.wc_engine_set_stream.argtypes = [vp, vp]
+        L.wc_engine_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong]
         L.wc_engine_launch_count.argtypes = [vp]
         L.wc_engine_launch_count.restype = ctypes.c_longlong
         L.wc_engine_profile.argtypes = [vp, ctypes.c_int]
@@ -80,6 +81,11 @@ def lib():
         L.wc_tiff_read.argtypes = [ctypes.c_char_p, vp, ctypes.c_longlong]
         L.wc_wnd_fit.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D, D, D]
         L.wc_wnd_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D, I]
+        L.wc_wnd_fit_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp, vp,
+                                         vp]
+        L.wc_wnd_classify_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp,
+                                             ctypes.c_int, vp, vp]
+        L.wc_wnd_last_stats.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
         L.wc_wnd_classify_images.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, D, I, D]
         _lib = L

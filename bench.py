@@ -228,6 +228,310 @@ def run_tiles(args):
                                  "io": "host images in, host rows out (inside the timed region)"}}))
 
 
+WND_METRIC = "test vectors/sec, WND-5 (normalize + Fisher top 15% + classify2), 1e5 train x 1e4 test x 2919 features"
+WND_CONFIG = {"workload": "WND-5 at scale: 100,000 train x 10,000 test fp64 vectors x 2919 features, 10 classes, "
+                          "N(mu_cf, 1) with mu_cf ~ N(0, 0.5), seed 4",
+              "parallelism": "replicas", "l2": "inputs (2.6 GB) larger than L2"}
+
+
+def wnd_cpu(xtr, ytr, xte, C, nthreads, rows):
+    """The oracle's WND-5 (the reference's arithmetic) on the host: one fit over
+    all training rows, then `rows` test rows split over nthreads threads.
+    Returns (fit s, classify s, probs, pred)."""
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+    ora = ctypes.CDLL(os.path.join(REPO, "oracle", "build", "libwc_oracle.so"))
+    N, F = xtr.shape
+    D, I = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    w, mn, mx = np.zeros(F), np.zeros(F), np.zeros(F)
+    p, pr, secs = np.zeros((rows, C)), np.zeros(rows, dtype=np.int32), np.zeros(2)
+    te = np.ascontiguousarray(xte[:rows])
+    ora.wco_wnd_mt(xtr.ctypes.data_as(D), N, F, ytr.ctypes.data_as(I), C, ctypes.c_double(0.15), te.ctypes.data_as(D),
+                   rows, w.ctypes.data_as(D), mn.ctypes.data_as(D), mx.ctypes.data_as(D), p.ctypes.data_as(D),
+                   pr.ctypes.data_as(I), nthreads, secs.ctypes.data_as(D))
+    return secs[0], secs[1], p, pr
+
+
+def run_wnd(args, reference=False):
+    """The WND-5 workload at scale: one step = normalize + Fisher scores on the
+    100,000 training vectors and classify2 of the 10,000 test vectors."""
+    from wndcharm import synth
+    C, T = 10, args.wnd_test
+    xtr, ytr, xte, yte = synth.feature_vectors(args.wnd_train, T, 2919, C, 4)
+    N, F = xtr.shape
+    nth = os.cpu_count() or 1
+    rows = nth * 16  # test rows of the CPU sample
+
+    def cpu_sample():
+        tf, tc, p, pr = wnd_cpu(xtr, ytr, xte, C, nth, rows)
+        # the full job at the sample's rates: one fit, T rows over nth threads
+        return T / (tf + tc * T / rows), tf, tc, p, pr
+
+    if (args.wnd_train, args.wnd_test) != (100000, 10000):
+        WND_CONFIG["workload"] += " (run at %d train x %d test)" % (args.wnd_train, args.wnd_test)
+
+    if reference:
+        vals, tot = [], 0.0
+        for _ in range(args.steps):
+            v, tf, tc, _, _ = cpu_sample()
+            vals.append(v)
+            tot += tf + tc * T / rows
+        v = statistics.median(vals)
+        print(json.dumps({"metric": WND_METRIC, "value": v, "unit": "test vectors/s", "n_gpus": 1, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "impl": "reference", "config": dict(WND_CONFIG),
+                          "cpu_baseline": {"value": v, "unit": "test vectors/s", "cores": nth, "kind": "port",
+                                           "sample": "one fit over the 100,000 training vectors plus %d test vectors "
+                                                     "on %d threads per step, scaled to the 10,000" % (rows, nth)},
+                          "e2e": {"value": v, "unit": "test vectors/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    import torch
+    import wndcharm
+    stream = torch.cuda.Stream()
+    engines = {k: wndcharm.Engine(0, k) for k in ("mixed", "fp64")}
+    for e in engines.values():
+        e.set_stream(stream.cuda_stream)
+    X = torch.from_numpy(xtr).cuda()
+    y = torch.from_numpy(ytr).cuda()
+    Tt = torch.from_numpy(xte).cuda()
+    dw, dmn, dmx = (torch.empty(F, dtype=torch.float64, device="cuda") for _ in range(3))
+    dp = torch.empty((T, C), dtype=torch.float64, device="cuda")
+    dpr = torch.empty(T, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def step(e):
+        e.wnd_fit_device(X, y, C, 0.15, dw, dmn, dmx)
+        e.wnd_classify_device(X, y, C, dw, dmn, dmx, Tt, dp, dpr)
+
+    def timed(fn, k):
+        tot, st = 0.0, []
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            tot += a.elapsed_time(b) / 1000.0
+            st.append(wndcharm.Engine.wnd_last_stats())
+        return tot, st
+
+    emx = engines["mixed"]
+    for _ in range(max(3, args.warmup)):
+        step(emx)
+    stop, samples = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    l0 = emx.launches
+    t_dev, stats = timed(lambda: step(emx), args.steps)
+    launches = emx.launches - l0
+    p_mx, pr_mx = dp.cpu().numpy().copy(), dpr.cpu().numpy().copy()
+    # end to end: pinned host arrays through the host-buffer entry points
+    hx, hy, ht = (torch.from_numpy(a).pin_memory() for a in (xtr, ytr, xte))
+    hxn, hyn, htn = hx.numpy(), hy.numpy(), ht.numpy()
+
+    def step_e2e():
+        w, mn, mx = emx.wnd_fit(hxn, hyn, C, 0.15)
+        emx.wnd_classify(hxn, hyn, C, w, mn, mx, htn)
+
+    step_e2e()
+    t_e2e, _ = timed(step_e2e, args.steps)
+    stop.set()
+    th.join(timeout=10)
+    clocks = summarize_clocks(samples)
+    # the FP64 form on the same step
+    t64, _ = timed(lambda: step(engines["fp64"]), max(1, min(args.steps, 2)))
+    k64 = max(1, min(args.steps, 2))
+    p64, pr64 = dp.cpu().numpy(), dpr.cpu().numpy()
+    st = stats[-1]
+    K = st[2]
+    kern_s = st[4] / 1e9 if st[4] else None
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("bf16_tflops", 1900.0)
+    alg = 2.0 * T * N * K  # one multiply-add per (test, training, feature) term
+    roof = {"kernel": "k_wnd_tc (tcgen05.mma, bf16 digits, FP32 accumulate)", "bound": "tensor",
+            "achieved": alg / kern_s / 1e12 if kern_s else None, "peak": peak, "unit": "TFLOP/s",
+            "frac": (alg / kern_s / 1e12) / peak if kern_s else None, "traffic": None,
+            "peak_source": "measured" if peaks else "fallback",
+            "algorithmic_flops_per_launch": alg, "kernel_ms": 1000 * kern_s if kern_s else None,
+            "issued_tflops": st[5] / kern_s / 1e12 if kern_s else None,
+            "issued_frac": st[5] / kern_s / 1e12 / peak if kern_s else None,
+            "issued_note": "13 digit-pair bf16 products per term over padded sizes (exact digit arithmetic)"}
+    v = T * args.steps / t_dev
+    h2d = 2 * N * F * 8 + T * F * 8 + 2 * N * 4 + 2 * F * 8
+    d2h = 3 * F * 8 + T * C * 8 + T * 4
+    line = {"metric": WND_METRIC, "value": v, "unit": "test vectors/s",
+            "mixed_vs_fp64": v / (T * k64 / t64), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 digits (exact) + f32 pairs + f64", "data": "synthetic",
+            "config": dict(WND_CONFIG), "precision_form": "mixed",
+            "e2e": {"value": T * args.steps / t_e2e, "unit": "test vectors/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": roof,
+            "fp64_form": {"value": T * k64 / t64, "ms_per_step": 1000 * t64 / k64},
+            "tensor_core": {"ran": bool(st[0]), "rows_rechecked_fp64": st[1], "weighted_features": K,
+                            "ctas": st[3]},
+            "vs_fp64_form": {"classes_identical": bool((pr_mx == pr64).all()),
+                             "max_abs_prob_diff": float(np.abs(p_mx - p64).max())},
+            "accuracy_vs_truth": float((pr_mx == yte).mean())}
+    if not args.no_cpu_baseline:
+        vc, tf, tc, pc, prc = cpu_sample()
+        line["cpu_baseline"] = {"value": vc, "unit": "test vectors/s", "cores": nth, "kind": "port",
+                                "sample": "one fit over the 100,000 training vectors (%.1f s) plus %d test vectors on "
+                                          "%d threads (%.1f s), scaled to the 10,000" % (tf, rows, nth, tc)}
+        line["vs_oracle"] = {"rows": rows, "classes_identical": bool((prc == pr_mx[:rows]).all()),
+                             "max_abs_prob_diff": float(np.abs(pc - p_mx[:rows]).max())}
+    print(json.dumps(line), flush=True)
+
+
+SHORT_METRIC = "images/sec, 1059-feature set + WND-5 (30 train / 10 test), 256^2 uint8, 2 classes"
+SHORT_CONFIG = {"workload": "short plan (1059 features), 2 classes x 20 uint8 256x256 blob+grating, seed 0; WND-5 "
+                            "Fisher top 15%, trained on 30, tested on 10",
+                "parallelism": "replicas", "l2": "GPU arm: inputs resident; CPU arm: not applicable"}
+
+
+def short_data():
+    from wndcharm import synth
+    imgs, labels = synth.image_set(2, 20, 256, 256, seed=0, bits=8)
+    tr = [i for i in range(40) if i % 20 < 15]
+    te = [i for i in range(40) if i % 20 >= 15]
+    order = tr + te  # training images first
+    return [imgs[i] for i in order], labels[order].astype(np.int32)
+
+
+def short_cpu(imgs, labels, nthreads):
+    """The oracle on the host: the short plan on the 40 images (one per thread),
+    then WND-5 fit on the first 30 rows and classify2 of the last 10."""
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+    ora = ctypes.CDLL(os.path.join(REPO, "oracle", "build", "libwc_oracle.so"))
+    n = len(imgs)
+    pix = np.concatenate([np.ascontiguousarray(a, dtype=np.float64).ravel() for a in imgs])
+    offs = np.cumsum([0] + [a.size for a in imgs[:-1]]).astype(np.int64)
+    ws = np.array([a.shape[1] for a in imgs], dtype=np.int32)
+    hs = np.array([a.shape[0] for a in imgs], dtype=np.int32)
+    nf = ora.wco_plan_n_features(0)
+    rows = np.zeros((n, nf))
+    D, I = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    t0 = time.perf_counter()
+    ora.wco_extract_std_batch(0, pix.ctypes.data_as(D), offs.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                              ws.ctypes.data_as(I), hs.ctypes.data_as(I), n, 8, rows.ctypes.data_as(D), nthreads)
+    w, mn, mx = np.zeros(nf), np.zeros(nf), np.zeros(nf)
+    p, pr = np.zeros((10, 2)), np.zeros(10, dtype=np.int32)
+    tr = np.ascontiguousarray(rows[:30])
+    te = np.ascontiguousarray(rows[30:])
+    ytr = np.ascontiguousarray(labels[:30])
+    ora.wco_wnd(tr.ctypes.data_as(D), 30, nf, ytr.ctypes.data_as(I), 2, ctypes.c_double(0.15), te.ctypes.data_as(D),
+                10, w.ctypes.data_as(D), mn.ctypes.data_as(D), mx.ctypes.data_as(D), p.ctypes.data_as(D),
+                pr.ctypes.data_as(I))
+    return time.perf_counter() - t0, rows, p, pr
+
+
+def run_short(args, reference=False):
+    """The short plan with WND-5: one step = features of the 40 images (FP64
+    form, as the plain reference method computes them), WND-5 fit on the 30
+    training rows and classify2 of the 10 test rows."""
+    imgs, labels = short_data()
+    nth = os.cpu_count() or 1
+    if reference:
+        tot = 0.0
+        for _ in range(args.steps):
+            dt, _, _, _ = short_cpu(imgs, labels, nth)
+            tot += dt
+        v = 40 * args.steps / tot
+        print(json.dumps({"metric": SHORT_METRIC, "value": v, "unit": "images/s", "n_gpus": 1, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "impl": "reference", "config": dict(SHORT_CONFIG),
+                          "cpu_baseline": {"value": v, "unit": "images/s", "cores": nth, "kind": "port",
+                                           "sample": "the whole step (40 images, one per thread; then WND-5)"},
+                          "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    import torch
+    import wndcharm
+    plan = wndcharm.StdFeatureComputationPlans.getFeatureSet()
+    nf = plan.n_features
+    eng = wndcharm.Engine(0, "fp64")
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    host = torch.from_numpy(np.stack(imgs)).pin_memory()
+    dev_imgs = host.cuda()
+    W = wndcharm._lib
+    L = wndcharm.lib()
+    descs_dev = (W.wc_image_desc * 40)()
+    descs_host = (W.wc_image_desc * 40)()
+    for i in range(40):
+        descs_dev[i] = W.wc_image_desc(dev_imgs[i].data_ptr(), W.WC_U8, 256, 256, 8, 1)
+        descs_host[i] = W.wc_image_desc(host[i].data_ptr(), W.WC_U8, 256, 256, 8, 0)
+    feat = torch.empty((40, nf), dtype=torch.float64, device="cuda")
+    y = torch.from_numpy(labels[:30]).cuda()
+    dw, dmn, dmx = (torch.empty(nf, dtype=torch.float64, device="cuda") for _ in range(3))
+    dp = torch.empty((10, 2), dtype=torch.float64, device="cuda")
+    dpr = torch.empty(10, dtype=torch.int32, device="cuda")
+    out_host = torch.empty((40, nf), dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+
+    def step_dev():
+        wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_dev, 40, ctypes.c_void_p(feat.data_ptr()), 1))
+        eng.wnd_fit_device(feat[:30], y, 2, 0.15, dw, dmn, dmx)
+        eng.wnd_classify_device(feat[:30], y, 2, dw, dmn, dmx, feat[30:], dp, dpr)
+
+    res = {}
+
+    def step_e2e():
+        wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_host, 40, ctypes.c_void_p(out_host.data_ptr()),
+                                          0))
+        rows = out_host.numpy()
+        w, mn, mx = eng.wnd_fit(rows[:30], labels[:30], 2, 0.15)
+        res["p"], res["pred"] = eng.wnd_classify(rows[:30], labels[:30], 2, w, mn, mx, rows[30:])
+
+    def timed(fn, k):
+        tot = 0.0
+        for _ in range(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            tot += a.elapsed_time(b) / 1000.0
+        return tot
+
+    for _ in range(max(3, args.warmup)):
+        step_dev()
+    stop, samples = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    l0 = eng.launches
+    t_dev = timed(step_dev, args.steps)
+    launches = eng.launches - l0
+    step_e2e()
+    t_e2e = timed(step_e2e, args.steps)
+    stop.set()
+    th.join(timeout=10)
+    line = {"metric": SHORT_METRIC, "value": 40 * args.steps / t_dev, "unit": "images/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(SHORT_CONFIG), "precision_form": "fp64",
+            "e2e": {"value": 40 * args.steps / t_e2e, "unit": "images/s", "h2d_bytes_per_step": 40 * 256 * 256 + 2 * 30 * nf * 8 + 10 * nf * 8,
+                    "d2h_bytes_per_step": 40 * nf * 8 + 3 * nf * 8 + 10 * 2 * 8 + 40},
+            "gpu_launches": int(launches), "clocks": summarize_clocks(samples),
+            "predicted": [int(v) for v in dpr.cpu().numpy()], "truth": [int(v) for v in labels[30:]]}
+    if not args.no_cpu_baseline:
+        dt, rows, p, pr = short_cpu(imgs, labels, nth)
+        line["cpu_baseline"] = {"value": 40 / dt, "unit": "images/s", "cores": nth, "kind": "port",
+                                "sample": "the whole step (40 images, one per host thread; then WND-5), %.1f s" % dt}
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        from parity import compare
+        names = open(os.path.join(REPO, "tests", "golden", "names_short.txt")).read().splitlines()
+        got = out_host.numpy()
+        line["vs_oracle"] = {"feature_rows_within_rules": all(not compare(got[i], rows[i], names, rtol=1e-7,
+                                                                          f14="exact") for i in range(40)),
+                             "classes_identical": bool((res["pred"] == pr).all()),
+                             "max_abs_prob_diff": float(np.abs(res["p"] - p).max())}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -241,10 +545,13 @@ def main():
                     help="mixed form's Haralick f14 chain: exact (FP64, bit-identical to the oracle) or pairs of floats")
     ap.add_argument("--per-image", type=int, default=8, help="images timed one per call in the FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--wnd-train", type=int, default=100000, help="--workload wnd: training vectors")
+    ap.add_argument("--wnd-test", type=int, default=10000, help="--workload wnd: test vectors")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP64 comparison forms")
-    ap.add_argument("--workload", default="512", choices=["512", "tiles"],
+    ap.add_argument("--workload", default="512", choices=["512", "tiles", "wnd", "short"],
                     help="512: the 512x512 images (the headline line); tiles: uneven images "
-                         "(sides 64..1024) cut into 4 x 4 tiles on the GPU, one line of its own")
+                         "(sides 64..1024) cut into 4 x 4 tiles on the GPU; wnd: WND-5 at 1e5 x 1e4 x 2919; "
+                         "short: the short plan with WND-5 on 40 256x256 uint8 images; one line each")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -252,6 +559,10 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "tiles":
         return run_tiles(args)
+    if args.workload == "wnd":
+        return run_wnd(args)
+    if args.workload == "short":
+        return run_short(args)
 
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -182,7 +182,9 @@ int wc_wnd_classify_device(wc_engine *engine, const double *train, int N, int F,
 /* What the calling thread's last wc_wnd_classify* call did (no reference
  * counterpart): stats[0] 1 if the tensor-core path ran, stats[1] the test rows
  * the FP64 kernel recomputed, stats[2] the features with a non-zero weight,
- * stats[3] the tensor-core kernel's CTAs. */
+ * stats[3] the tensor-core kernel's CTAs, stats[4] its time in nanoseconds
+ * (CUDA events on the engine's stream), stats[5] the tensor FLOPs it issued
+ * (13 digit-pair products over the padded sizes).  stats holds 6 values. */
 int wc_wnd_last_stats(long long *stats);
 
 /* wc_wnd_classify_images: TrainingSet::ClassifyImage with WND-5

@@ -15,6 +15,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <chrono>
 #include <thread>
 #include <vector>
 #include <atomic>
@@ -1857,11 +1858,11 @@ static bool parse_group(const std::string &s, Group &g) {
 }
 
 // ---------------------------------------------------------------- WND-5
-static void wnd_run(const double *train, int N, int F, const int *labels, int C, double frac,
-                    const double *test, int T, double *weights, double *mins, double *maxs,
-                    double *probs, int *pred, double *norms = nullptr) {
+// TrainingSet::normalize + SetFisherScores: X (N x F, a copy of the training
+// rows) normalised in place; weights thresholded at rank floor(frac*F + 0.5).
+static void wnd_fit_rows(std::vector<double> &X, int N, int F, const int *labels, int C, double frac,
+                         double *weights, double *mins, double *maxs) {
     // TrainingSet::normalize, src/wndchrm_src/TrainingSet.cpp:2090-2123
-    std::vector<double> X(train, train + (size_t)N * F);
     for (int f = 0; f < F; f++) {
         double mn = FLT_MAX, mx = -FLT_MAX;
         for (int s = 0; s < N; s++) {
@@ -1902,10 +1903,17 @@ static void wnd_run(const double *train, int N, int F, const int *labels, int C,
         double thr = sw[last];
         for (int f = 0; f < F; f++) if (weights[f] < thr) weights[f] = 0.0;
     }
+}
+
+// signatures::normalize + classify2 for test rows [q0, q1) against the
+// normalised training rows X.
+static void wnd_classify_rows(const std::vector<double> &X, int N, int F, const int *labels, int C,
+                              const double *weights, const double *mins, const double *maxs, const double *test,
+                              int q0, int q1, double *probs, int *pred, double *norms) {
     // signatures::normalize + TrainingSet::classify2, signatures.cpp:196-215,
     // TrainingSet.cpp:2429-2536
     std::vector<double> t(F), csim(C + 1), ncnt(C + 1);
-    for (int q = 0; q < T; q++) {
+    for (int q = q0; q < q1; q++) {
         for (int f = 0; f < F; f++) {
             double v = test[(size_t)q * F + f];
             if (std::isnan(v) || v < mins[f] || (maxs[f] - mins[f]) < DBL_EPSILON) v = 0;
@@ -1939,6 +1947,15 @@ static void wnd_run(const double *train, int N, int F, const int *labels, int C,
         pred[q] = (int)best;
         if (norms) norms[q] = tot;
     }
+}
+
+
+static void wnd_run(const double *train, int N, int F, const int *labels, int C, double frac,
+                    const double *test, int T, double *weights, double *mins, double *maxs,
+                    double *probs, int *pred, double *norms = nullptr) {
+    std::vector<double> X(train, train + (size_t)N * F);
+    wnd_fit_rows(X, N, F, labels, C, frac, weights, mins, maxs);
+    wnd_classify_rows(X, N, F, labels, C, weights, mins, maxs, test, 0, T, probs, pred, norms);
 }
 
 // TrainingSet::ClassifyImage, WND branch (src/wndchrm_src/TrainingSet.cpp:1603-1800),
@@ -2111,6 +2128,33 @@ int wco_haralick_tones(const double *pix, int w, int h) {
 int wco_wnd(const double *train, int N, int F, const int *labels, int C, double frac, const double *test,
             int T, double *weights, double *mins, double *maxs, double *probs, int *pred) {
     wnd_run(train, N, F, labels, C, frac, test, T, weights, mins, maxs, probs, pred);
+    return 0;
+}
+
+// WND-5 as wndchrm runs it over many test rows: one fit, then the test rows
+// split into nthreads contiguous ranges classified concurrently (the
+// reference's one process per test split, without repeating the fit).
+// Returns the fit's and the classification's wall seconds in secs[0..1].
+int wco_wnd_mt(const double *train, int N, int F, const int *labels, int C, double frac, const double *test, int T,
+               double *weights, double *mins, double *maxs, double *probs, int *pred, int nthreads, double *secs) {
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> X(train, train + (size_t)N * F);
+    wnd_fit_rows(X, N, F, labels, C, frac, weights, mins, maxs);
+    auto t1 = std::chrono::steady_clock::now();
+    if (nthreads < 1) nthreads = 1;
+    std::vector<std::thread> th;
+    for (int k = 0; k < nthreads; k++) {
+        const int q0 = (int)((long long)T * k / nthreads), q1 = (int)((long long)T * (k + 1) / nthreads);
+        th.emplace_back([&, q0, q1] {
+            wnd_classify_rows(X, N, F, labels, C, weights, mins, maxs, test, q0, q1, probs, pred, nullptr);
+        });
+    }
+    for (auto &t : th) t.join();
+    auto t2 = std::chrono::steady_clock::now();
+    if (secs) {
+        secs[0] = std::chrono::duration<double>(t1 - t0).count();
+        secs[1] = std::chrono::duration<double>(t2 - t1).count();
+    }
     return 0;
 }
 

@@ -62,6 +62,11 @@ int wco_wnd(const double *train, int N, int F, const int *labels, int C, double 
             const double *test, int T, double *weights, double *mins, double *maxs,
             double *probs, int *pred);
 
+// The same over many test rows: one fit, then nthreads contiguous test ranges
+// classified concurrently; secs[0] the fit's, secs[1] the classification's wall seconds.
+int wco_wnd_mt(const double *train, int N, int F, const int *labels, int C, double frac, const double *test, int T,
+               double *weights, double *mins, double *maxs, double *probs, int *pred, int nthreads, double *secs);
+
 #ifdef __cplusplus
 }
 #endif

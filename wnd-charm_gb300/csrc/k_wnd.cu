@@ -21,78 +21,167 @@ struct wc_engine;
 namespace wc {
 int engine_device(wc_engine *E, cudaStream_t *st, long long **launches);
 int engine_precision(const wc_engine *E);
+int engine_sms(const wc_engine *E);
 }
 
 namespace wc {
 
-// per feature: min/max over the rows (skipping NaN and |v| > FLT_MAX), then the
-// normalised column; X is N x F row-major, Xn written in the same layout.
-__global__ void k_wnd_minmax(const double *__restrict__ X, int N, int F, double *__restrict__ mins,
-                             double *__restrict__ maxs, double *__restrict__ Xn) {
-    __shared__ double sh[32];
-    const int f = blockIdx.x;
+// TrainingSet::normalize + SetFisherScores over X (N x F, row-major), read a
+// row at a time: a block takes 32 consecutive features (one per lane, so a
+// warp reads 256 contiguous bytes of a row) and one of R contiguous ranges of
+// rows (warp w of the block its rows w, w + 8, ...); per-range partial results
+// go to global memory and are combined in range order, so every result is
+// the same from run to run.
+
+#define FIT_U 8  // rows per warp and iteration
+
+// per-range min / max of each feature, skipping NaN and |v| > FLT_MAX
+__global__ void __launch_bounds__(256) k_wnd_fit_minmax(const double *__restrict__ X, int N, int F, int rows_per,
+                                                        double *__restrict__ pmin, double *__restrict__ pmax) {
+    __shared__ double smn[8][32], smx[8][32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int f = blockIdx.x * 32 + lane, r = blockIdx.y;
+    const int s0 = r * rows_per, s1 = min(N, s0 + rows_per);
     double mn = FLT_MAX, mx = -FLT_MAX;
-    for (int s = threadIdx.x; s < N; s += blockDim.x) {
-        double v = X[(long long)s * F + f];
-        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;
-        mn = fmin(mn, v);
-        mx = fmax(mx, v);
-    }
-    mn = block_min(mn, sh);
-    mx = block_max(mx, sh);
-    if (threadIdx.x == 0) {
-        mins[f] = mn;
-        maxs[f] = mx;
-    }
-    for (int s = threadIdx.x; s < N; s += blockDim.x) {
-        double v = X[(long long)s * F + f];
-        if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) v = 0;
-        else if (v > mx) v = 100;
-        else v = 100 * ((v - mn) / (mx - mn));
-        Xn[(long long)s * F + f] = v;
+    if (f < F)
+        for (int s = s0 + wp; s < s1; s += 8 * FIT_U) {
+            // FIT_U rows' loads in flight before any is used
+            double v[FIT_U];
+#pragma unroll
+            for (int u = 0; u < FIT_U; u++) v[u] = s + 8 * u < s1 ? X[(long long)(s + 8 * u) * F + f] : NAN;
+#pragma unroll
+            for (int u = 0; u < FIT_U; u++) {
+                if (isnan(v[u]) || v[u] > FLT_MAX || v[u] < -FLT_MAX) continue;
+                mn = fmin(mn, v[u]);
+                mx = fmax(mx, v[u]);
+            }
+        }
+    smn[wp][lane] = mn;
+    smx[wp][lane] = mx;
+    __syncthreads();
+    if (wp == 0 && f < F) {
+        for (int k = 1; k < 8; k++) {
+            mn = fmin(mn, smn[k][lane]);
+            mx = fmax(mx, smx[k][lane]);
+        }
+        pmin[(long long)r * F + f] = mn;
+        pmax[(long long)r * F + f] = mx;
     }
 }
 
-// Fisher score per feature: between-class variance of class means over the
-// mean within-class variance (Moments2 var, 0 for n <= 2), floor 1e-6.
-__global__ void k_wnd_fisher(const double *__restrict__ Xn, const int *__restrict__ y, int N, int F, int C,
-                             double *__restrict__ w) {
-    __shared__ double sh[32];
-    __shared__ long long shl[32];
-    const int f = blockIdx.x;
-    double s_all = 0;
-    long long n_all = 0;
-    for (int s = threadIdx.x; s < N; s += blockDim.x)
-        if (y[s]) { s_all += Xn[(long long)s * F + f]; n_all++; }
-    s_all = block_sum(s_all, sh);
-    n_all = block_sum_ll(n_all, shl);
-    const double mean_all = n_all ? s_all / n_all : 0.0;
+__global__ void k_wnd_fit_minmax_final(const double *__restrict__ pmin, const double *__restrict__ pmax, int R, int F,
+                                       double *__restrict__ mins, double *__restrict__ maxs) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    double mn = FLT_MAX, mx = -FLT_MAX;
+    for (int r = 0; r < R; r++) {
+        mn = fmin(mn, pmin[(long long)r * F + f]);
+        mx = fmax(mx, pmax[(long long)r * F + f]);
+    }
+    mins[f] = mn;
+    maxs[f] = mx;
+}
+
+// training rows per label: cnt[0] those with any label (y != 0), cnt[c] class c
+__global__ void k_wnd_fit_count(const int *__restrict__ y, int N, int C, long long *__restrict__ cnt) {
+    __shared__ unsigned int sc[17];
+    if (threadIdx.x <= 16) sc[threadIdx.x] = 0;
+    __syncthreads();
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
+        const int c = y[s];
+        if (c) atomicAdd(&sc[0], 1u);
+        if (c >= 1 && c <= C) atomicAdd(&sc[c], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x <= 16 && sc[threadIdx.x]) atomicAdd((unsigned long long *)&cnt[threadIdx.x], sc[threadIdx.x]);
+}
+
+__device__ __forceinline__ double fit_norm(double v, double mn, double mx) {
+    if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) return 0.0;
+    if (v > mx) return 100.0;
+    return 100 * ((v - mn) / (mx - mn));
+}
+
+// second = 0: per-range sums of the normalised values, slot 0 over every
+// labelled row, slot c over class c; second = 1: per-range sums of squared
+// deviations from the class means (mean[c * F + f])
+__global__ void __launch_bounds__(256) k_wnd_fit_moments(const double *__restrict__ X, const int *__restrict__ y, int N,
+                                                         int F, int C, int rows_per, const double *__restrict__ mins,
+                                                         const double *__restrict__ maxs,
+                                                         const double *__restrict__ mean, int second,
+                                                         double *__restrict__ part) {
+    __shared__ double acc[8][17][32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int f = blockIdx.x * 32 + lane, r = blockIdx.y;
+    const int s0 = r * rows_per, s1 = min(N, s0 + rows_per);
+    for (int c = 0; c <= C; c++) acc[wp][c][lane] = 0.0;
+    if (f < F) {
+        const double mn = mins[f], mx = maxs[f];
+        for (int s = s0 + wp; s < s1; s += 8 * FIT_U) {
+            // FIT_U rows' loads in flight, then added in row order
+            double xv[FIT_U];
+            int cv[FIT_U];
+#pragma unroll
+            for (int u = 0; u < FIT_U; u++) {
+                const bool in = s + 8 * u < s1;
+                xv[u] = in ? X[(long long)(s + 8 * u) * F + f] : 0.0;
+                cv[u] = in ? y[s + 8 * u] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < FIT_U; u++) {
+                const int c = cv[u];
+                const double v = fit_norm(xv[u], mn, mx);
+                if (!second) {
+                    if (c) acc[wp][0][lane] += v;
+                    if (c >= 1 && c <= C) acc[wp][c][lane] += v;
+                } else if (c >= 1 && c <= C) {
+                    const double d = v - mean[(long long)c * F + f];
+                    acc[wp][c][lane] += d * d;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (wp == 0 && f < F)
+        for (int c = 0; c <= C; c++) {
+            double t = acc[0][c][lane];
+            for (int k = 1; k < 8; k++) t += acc[k][c][lane];
+            part[((long long)r * (C + 1) + c) * F + f] = t;
+        }
+}
+
+// combine the ranges: class means (second = 0) into mean[c * F + f]; or
+// (second = 1) the Fisher score, between-class variance of the class means
+// over the mean within-class variance (0 for classes of <= 2 rows), floor 1e-6
+__global__ void k_wnd_fit_combine(const double *__restrict__ part, int R, int F, int C,
+                                  const long long *__restrict__ cnt, int second, double *__restrict__ mean,
+                                  double *__restrict__ w) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    if (!second) {
+        for (int c = 0; c <= C; c++) {
+            double t = 0;
+            for (int r = 0; r < R; r++) t += part[((long long)r * (C + 1) + c) * F + f];
+            mean[(long long)c * F + f] = cnt[c] ? t / cnt[c] : 0.0;
+        }
+        return;
+    }
+    const double mean_all = mean[f];
     double dev = 0, var = 0;
     for (int c = 1; c <= C; c++) {
-        double sc = 0;
-        long long nc = 0;
-        for (int s = threadIdx.x; s < N; s += blockDim.x)
-            if (y[s] == c) { sc += Xn[(long long)s * F + f]; nc++; }
-        sc = block_sum(sc, sh);
-        nc = block_sum_ll(nc, shl);
-        const double mc = nc ? sc / nc : 0.0;
         double m2 = 0;
-        for (int s = threadIdx.x; s < N; s += blockDim.x)
-            if (y[s] == c) { double d = Xn[(long long)s * F + f] - mc; m2 += d * d; }
-        m2 = block_sum(m2, sh);
-        dev += pow(mc - mean_all, 2);
-        var += nc > 2 ? m2 / (nc - 1) : 0.0;
+        for (int r = 0; r < R; r++) m2 += part[((long long)r * (C + 1) + c) * F + f];
+        dev += pow(mean[(long long)c * F + f] - mean_all, 2);
+        var += cnt[c] > 2 ? m2 / (cnt[c] - 1) : 0.0;
     }
-    if (threadIdx.x == 0) {
-        if (C > 1) {
-            dev /= (C - 1);
-            var /= C;
-        } else {
-            dev = 0;
-        }
-        if (var < 0.000001) var = 0.000001;
-        w[f] = dev / var;
+    if (C > 1) {
+        dev /= (C - 1);
+        var /= C;
+    } else {
+        dev = 0;
     }
+    if (var < 0.000001) var = 0.000001;
+    w[f] = dev / var;
 }
 
 // gather the kept features, normalised: Xc is K x rows (column-major per row
@@ -416,13 +505,26 @@ static int wnd_fit_dev(wc_engine *E, const double *dX, int N, int F, const int *
     long long *launches;
     int rc = engine_device(E, &st, &launches);
     if (rc) return rc;
-    double *dXn = nullptr, *dw = nullptr;
-    CKW(cudaMalloc(&dXn, (size_t)N * F * sizeof(double)));
+    const int fb = (F + 31) / 32;
+    const int R = std::max(1, std::min((N + 255) / 256, (8 * engine_sms(E) + fb - 1) / fb));
+    const int rows_per = (N + R - 1) / R;
+    double *dpmin = nullptr, *dpmax = nullptr, *dpart = nullptr, *dmean = nullptr, *dw = nullptr;
+    long long *dcnt = nullptr;
+    CKW(cudaMalloc(&dpmin, (size_t)R * F * sizeof(double)));
+    CKW(cudaMalloc(&dpmax, (size_t)R * F * sizeof(double)));
+    CKW(cudaMalloc(&dpart, (size_t)R * (C + 1) * F * sizeof(double)));
+    CKW(cudaMalloc(&dmean, (size_t)(C + 1) * F * sizeof(double)));
     CKW(cudaMalloc(&dw, F * sizeof(double)));
-    ++*launches;
-    k_wnd_minmax<<<F, 256, 0, st>>>(dX, N, F, dmin, dmax, dXn);
-    ++*launches;
-    k_wnd_fisher<<<F, 256, 0, st>>>(dXn, dy, N, F, C, dw);
+    CKW(cudaMalloc(&dcnt, 17 * sizeof(long long)));
+    CKW(cudaMemsetAsync(dcnt, 0, 17 * sizeof(long long), st));
+    *launches += 7;
+    k_wnd_fit_minmax<<<dim3(fb, R), 256, 0, st>>>(dX, N, F, rows_per, dpmin, dpmax);
+    k_wnd_fit_minmax_final<<<(F + 255) / 256, 256, 0, st>>>(dpmin, dpmax, R, F, dmin, dmax);
+    k_wnd_fit_count<<<std::min(1024, (N + 255) / 256), 256, 0, st>>>(dy, N, C, dcnt);
+    k_wnd_fit_moments<<<dim3(fb, R), 256, 0, st>>>(dX, dy, N, F, C, rows_per, dmin, dmax, nullptr, 0, dpart);
+    k_wnd_fit_combine<<<(F + 255) / 256, 256, 0, st>>>(dpart, R, F, C, dcnt, 0, dmean, nullptr);
+    k_wnd_fit_moments<<<dim3(fb, R), 256, 0, st>>>(dX, dy, N, F, C, rows_per, dmin, dmax, dmean, 1, dpart);
+    k_wnd_fit_combine<<<(F + 255) / 256, 256, 0, st>>>(dpart, R, F, C, dcnt, 1, dmean, dw);
     CKW(cudaGetLastError());
     CKW(cudaMemcpyAsync(weights, dw, F * sizeof(double), cudaMemcpyDeviceToHost, st));
     CKW(cudaStreamSynchronize(st));
@@ -438,8 +540,12 @@ static int wnd_fit_dev(wc_engine *E, const double *dX, int N, int F, const int *
         }
     }
 done:
-    cudaFree(dXn);
+    cudaFree(dpmin);
+    cudaFree(dpmax);
+    cudaFree(dpart);
+    cudaFree(dmean);
     cudaFree(dw);
+    cudaFree(dcnt);
     return rc;
 }
 
@@ -492,15 +598,14 @@ namespace wc {
 int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double *dX, int N, int F, const int *labels,
                     int C, const double *dT, int T, const std::vector<int> &keep, const std::vector<double> &w,
                     const double *dmin, const double *dmax, double *dprob, int *dpred, double *dnorm,
-                    std::vector<int> &recheck, long long *tc_ctas);
+                    std::vector<int> &recheck, long long *info);
 bool wnd_tc_supported(int K);
-int engine_sms(const wc_engine *E);
 }  // namespace wc
 
 namespace {
 
 // what the last classification did (wc_wnd_last_stats)
-thread_local long long g_last_stats[4] = {0, 0, 0, 0};
+thread_local long long g_last_stats[6] = {0, 0, 0, 0, 0, 0};
 
 // device buffers freed together
 struct WBufs {
@@ -599,21 +704,21 @@ static int wnd_classify_dev(wc_engine *E, const double *dX, int N, int F, const 
         CKR(cudaMemcpyAsync(dkeep, keep.data(), K * 4, cudaMemcpyHostToDevice, st));
         CKR(cudaMemcpyAsync(dw2, w2.data(), K * 8, cudaMemcpyHostToDevice, st));
     }
-    g_last_stats[0] = 0;
-    g_last_stats[1] = 0;
+    for (int i = 0; i < 6; i++) g_last_stats[i] = 0;
     g_last_stats[2] = K;
-    g_last_stats[3] = 0;
     if (mixed && wnd_tc_supported(K)) {
         // tensor cores, then the FP64 kernel for the rows they cannot certify
         std::vector<int> rows;
-        long long ctas = 0;
+        long long info[3] = {0, 0, 0};
         rc = wnd_tc_classify(st, launches, engine_sms(E), dX, N, F, labels, C, dT, T, keep, w, dmin, dmax, dprob, dpred,
-                             dnorm, rows, &ctas);
+                             dnorm, rows, info);
         if (rc == WC_ERR_UNSUPPORTED) goto pairs;
         if (rc) return rc;
         g_last_stats[0] = 1;
         g_last_stats[1] = (long long)rows.size();
-        g_last_stats[3] = ctas;
+        g_last_stats[3] = info[0];
+        g_last_stats[4] = info[1];
+        g_last_stats[5] = info[2];
         return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, rows, dprob, dpred, dnorm,
                          false);
     }
@@ -736,6 +841,6 @@ extern "C" int wc_wnd_classify_device(wc_engine *E, const double *train, int N, 
 
 extern "C" int wc_wnd_last_stats(long long *stats) {
     if (!stats) return set_err(WC_ERR_ARG, "wc_wnd_last_stats: null stats");
-    for (int i = 0; i < 4; i++) stats[i] = g_last_stats[i];
+    for (int i = 0; i < 6; i++) stats[i] = g_last_stats[i];
     return WC_OK;
 }

@@ -576,7 +576,7 @@ bool wnd_tc_supported(int K) { return K >= 1 && K <= tc::MAX_K; }
 int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double *dX, int N, int F,
                     const int *labels, int C, const double *dT, int T, const std::vector<int> &keep,
                     const std::vector<double> &w, const double *dmin, const double *dmax, double *dprob, int *dpred,
-                    double *dnorm, std::vector<int> &recheck, long long *tc_ctas) {
+                    double *dnorm, std::vector<int> &recheck, long long *info) {
     using namespace tc;
     const int K = (int)keep.size();
     if (!wnd_tc_supported(K)) return set_err(WC_ERR_UNSUPPORTED, "tensor-core WND: K = %d", K);
@@ -623,7 +623,11 @@ int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double 
         }
     }
     const int per_chunk = (ntiles + nch - 1) / nch;
-    if (tc_ctas) *tc_ctas = (long long)mblocks * nch;
+    // info: CTAs, the kernel's time (ns, CUDA events on the stream), issued
+    // tensor FLOPs (13 digit-pair products of T_pad x N_pad x Kp)
+    info[0] = (long long)mblocks * nch;
+    info[1] = 0;
+    info[2] = 13LL * 2 * T_pad * N_pad * Kp;
 
     TcBufs B;
     __nv_bfloat16 *digA, *digB;
@@ -691,8 +695,18 @@ int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double 
     const double eps_dd = DBL_EPSILON / std::ldexp(1.0, 2 * (E - 7) + g);
     P.dmin = (float)std::min<double>(std::max(1e-6, eps_dd), FLT_MAX);
     P.tol = 0x1p-26f;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    CKT(cudaEventCreate(&ev0));
+    CKT(cudaEventCreate(&ev1));
+    CKT(cudaEventRecord(ev0, st));
     k_wnd_tc<<<dim3(mblocks, nch), THREADS, SMEM_BYTES, st>>>(mA, mB, P);
-    CKT(cudaGetLastError());
+    const cudaError_t le = cudaGetLastError();
+    cudaEventRecord(ev1, st);
+    if (le != cudaSuccess) {
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        return set_err(WC_ERR_CUDA, "k_wnd_tc launch: %s", cudaGetErrorString(le));
+    }
     const double scale5 = std::ldexp(1.0, -5 * (2 * (E - 7) + g));
     k_wnd_tc_finish<<<(T + 127) / 128, 128, 0, st>>>(dpsim, dflag, T, nch, C, dncls, scale5, 20.0 * 0x1p-26, dprob,
                                                      dpred, dnorm, drc, dnrc);
@@ -700,6 +714,10 @@ int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double 
     int nr = 0;
     CKT(cudaMemcpyAsync(&nr, dnrc, sizeof(int), cudaMemcpyDeviceToHost, st));
     CKT(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) info[1] = (long long)(ms * 1e6);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
     int ev = 0;
     if (tc_err_take(st, &ev)) return set_err(WC_ERR_CUDA, "reading the tensor-core kernel's error word failed");
     if (ev) return set_err(WC_ERR_DEVICE, "tensor-core WND kernel: a bounded wait ran out (code %d)", ev);

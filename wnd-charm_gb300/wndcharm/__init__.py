@@ -413,8 +413,9 @@ class Engine(object):
     @staticmethod
     def wnd_last_stats():
         """What this thread's last WND-5 classification did: (tensor-core path
-        ran, test rows recomputed in FP64, weighted features, tensor-core CTAs)."""
-        st = (ctypes.c_longlong * 4)()
+        ran, test rows recomputed in FP64, weighted features, tensor-core CTAs,
+        tensor-core kernel time in ns, tensor FLOPs it issued)."""
+        st = (ctypes.c_longlong * 6)()
         check(lib().wc_wnd_last_stats(st))
         return tuple(int(v) for v in st)
 

@@ -107,6 +107,8 @@ def run_reference(args, rank, world):
         return run_short(args, reference=True)
     if args.workload == "wnd":
         return run_wnd(args, reference=True)
+    if args.workload == "grad":
+        return run_grad(args, reference=True)
     nthreads = os.cpu_count() or 1
     # each timed step: one image per host thread on every host thread (the
     # reference's own model: one single-threaded process per image per core)
@@ -532,6 +534,135 @@ def run_short(args, reference=False):
     print(json.dumps(line), flush=True)
 
 
+GRAD_METRIC = ("test images/sec, WND-5 class-evidence maps (d p_c / d pixel, every class) and d p / d Fisher "
+               "weights, 400 continuous features, 256^2 fp32")
+GRAD_CONFIG = {"workload": "differentiation: 256 fp32 256x256 blob+grating images in [0, 1], 4 classes, seed 3; "
+                           "WND-5 trained on 192, 400 Fisher-selected features of the continuous families "
+                           "(Zernike, pixel statistics, fractal, Gini on nonnegative planes); 64 test images",
+               "parallelism": "replicas", "l2": "host buffers through wc_wnd_grad (inputs staged each call)"}
+
+
+def run_grad(args, reference=False):
+    """One step = the class-evidence maps of the 64 test images: one forward
+    pass (features + classify2), then for each of the 4 classes a backward
+    pass to the pixels and the weights.  Beside it: central differences (h = 1e-3) on 64
+    random pixels of 8 test images through the GPU forward."""
+    from wndcharm import synth
+    imgs, labels = synth.config4(n=256, size=256, seed=3)
+    tr, te = list(range(192)), list(range(192, 256))
+    nth = os.cpu_count() or 1
+    if reference:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiation: its feature "
+                          "extraction and classify2 have no backward pass to time"}), flush=True)
+        return
+    import torch
+    import wndcharm
+    from wndcharm.grad import WNDModel, continuous_groups
+    plan = wndcharm.FeatureComputationPlan("continuous")
+    for g in continuous_groups():
+        plan.add(g)
+    eng = wndcharm.Engine(0, "fp64")
+    rows = eng.extract(plan, [imgs[i] for i in tr])
+    ytr = labels[tr]
+    w, mn, mx = eng.wnd_fit(rows, ytr, 4, 1.0)
+    thr = np.sort(w)[::-1][399]
+    w = np.where(w >= thr, w, 0.0)
+    model = WNDModel(eng, plan, rows, ytr, 4, mn, mx)
+    test = [imgs[i] for i in te]
+    n = len(test)
+
+    seeds = np.tile(np.eye(4)[None], (n, 1, 1))  # every class: the class-evidence maps
+
+    def step():
+        model.run(test, w, seed=seeds)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    stop, samples = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    l0 = eng.launches
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    launches = eng.launches - l0
+    stop.set()
+    th.join(timeout=10)
+    # central differences on a sample
+    probs, _, _ = model.run(test, w)
+    pred = probs.argmax(1)
+    rng = np.random.default_rng(7)
+    nimg, npix, h = 8, 64, 1e-3
+    seed = np.zeros((nimg, 4))
+    seed[np.arange(nimg), pred[:nimg]] = 1.0
+    _, gp, _ = model.run(test[:nimg], w, seed=seed)
+    fd, an = [], []
+    for i in range(nimg):
+        base = test[i].astype(np.float64)
+        batch, pix = [], []
+        for _ in range(npix):
+            yy, xx = int(rng.integers(256)), int(rng.integers(256))
+            pix.append((yy, xx))
+            for sg in (1, -1):
+                a = base.copy()
+                a[yy, xx] += sg * h
+                batch.append(a)
+        pb, _, _ = model.run(batch, w)
+        for k, (yy, xx) in enumerate(pix):
+            fd.append((pb[2 * k, pred[i]] - pb[2 * k + 1, pred[i]]) / (2 * h))
+            an.append(gp[i][yy, xx])
+    fd, an = np.array(fd), np.array(an)
+    # errors against the map's own scale (most pixels of a 256^2 map have a
+    # tiny derivative) and, for the pixels that matter (|derivative| above a
+    # hundredth of the map's largest), against their own value
+    big = np.abs(an) >= 1e-2 * np.abs(an).max()
+    q = np.quantile(np.abs(fd - an) / np.abs(an).max(), [0.5, 0.9, 0.95, 0.99])
+    qb = np.quantile(np.abs(fd - an)[big] / np.abs(an)[big], [0.5, 0.9, 0.95]) if big.any() else [np.nan] * 3
+    # the forward part alone on the host cores (the oracle: features of the
+    # continuous groups + classify2): the reference has no backward pass
+    cpu = None
+    if not args.no_cpu_baseline:
+        subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+        ora = ctypes.CDLL(os.path.join(REPO, "oracle", "build", "libwc_oracle.so"))
+        D = ctypes.POINTER(ctypes.c_double)
+        sample = test[:min(nth, n)]
+        out = np.zeros(256)
+
+        def one(a):
+            pix = np.ascontiguousarray(a, dtype=np.float64)
+            o = np.zeros(256)
+            for g in continuous_groups():
+                ora.wco_extract_group(g.encode(), pix.ctypes.data_as(D), 256, 256, 16, o.ctypes.data_as(D))
+
+        import concurrent.futures
+        t1 = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(nth) as ex:
+            list(ex.map(one, sample))
+        dt = time.perf_counter() - t1
+        cpu = {"value": len(sample) / dt, "unit": "test images/s (forward features only)", "cores": nth,
+               "kind": "port", "sample": "the 882 continuous features of %d test images, one per host thread; the "
+                                         "reference has no backward pass, so this times the forward alone" % len(sample)}
+    v = n * args.steps / t
+    line = {"metric": GRAD_METRIC, "value": v, "unit": "test images/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": dict(GRAD_CONFIG),
+            "e2e": {"value": v, "unit": "test images/s", "h2d_bytes_per_step": 4 * (n * 256 * 256 * 8 + rows.nbytes),
+                    "d2h_bytes_per_step": 4 * (n * 256 * 256 * 8 + n * 4 * 8 + w.nbytes)},
+            "gpu_launches": int(launches), "clocks": summarize_clocks(samples),
+            "features": {"plan": plan.n_features, "weighted": int((w > 0).sum())},
+            "finite_differences": {"h": h, "pixels": int(fd.size), "images": nimg,
+                                   "error_over_map_max_quantiles_50_90_95_99": [float("%.3g" % x) for x in q],
+                                   "pixels_above_1pct_of_max": int(big.sum()),
+                                   "their_relative_error_quantiles_50_90_95": [float("%.3g" % x) for x in qb]},
+            "accuracy_on_test": float((pred + 1 == labels[te]).mean())}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -548,7 +679,7 @@ def main():
     ap.add_argument("--wnd-train", type=int, default=100000, help="--workload wnd: training vectors")
     ap.add_argument("--wnd-test", type=int, default=10000, help="--workload wnd: test vectors")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP64 comparison forms")
-    ap.add_argument("--workload", default="512", choices=["512", "tiles", "wnd", "short"],
+    ap.add_argument("--workload", default="512", choices=["512", "tiles", "wnd", "short", "grad"],
                     help="512: the 512x512 images (the headline line); tiles: uneven images "
                          "(sides 64..1024) cut into 4 x 4 tiles on the GPU; wnd: WND-5 at 1e5 x 1e4 x 2919; "
                          "short: the short plan with WND-5 on 40 256x256 uint8 images; one line each")
@@ -563,6 +694,8 @@ def main():
         return run_wnd(args)
     if args.workload == "short":
         return run_short(args)
+    if args.workload == "grad":
+        return run_grad(args)
 
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -187,6 +187,28 @@ int wc_wnd_classify_device(wc_engine *engine, const double *train, int N, int F,
  * (13 digit-pair products over the padded sizes).  stats holds 6 values. */
 int wc_wnd_last_stats(long long *stats);
 
+/* ---- differentiation (no counterpart in the reference) ----
+ * wc_wnd_grad: the marginal probabilities that classify2 gives the n test
+ * images (their `plan` features computed by the engine, compared with the N
+ * training feature rows `train` (N x plan features, host) under `weights`,
+ * `mins`, `maxs` as wc_wnd_classify does), written to probs (n x C; may be
+ * NULL), and, when `seed` is given, one backward pass per seed after a
+ * single forward pass: seed holds n x n_seeds x C values of d loss / d
+ * probability (image-major); grad_pixels receives, for every image, its
+ * n_seeds maps of d loss / d pixel (width x height values each; images one
+ * after another; may be NULL) and grad_weights n_seeds x F values of d loss
+ * / d weight, each summed over the images (may be NULL).  n_seeds = C with
+ * one-hot seeds gives the per-class evidence maps d p_c / d pixel.  All in
+ * FP64, host buffers.  The backward runs through Zernike
+ * Coefficients, Pixel Intensity Statistics, Fractal Features and Gini
+ * Coefficient, on planes made by Fourier, Chebyshev, Wavelet and Edge chains;
+ * the binned families (histograms, counts, thresholds, Haralick) are
+ * piecewise-constant and contribute zero; a non-zero weight on a Tamura or
+ * Edge feature, or on a colour chain, gives WC_ERR_UNSUPPORTED. */
+int wc_wnd_grad(wc_engine *engine, const wc_plan *plan, const double *train, int N, const int *labels, int C,
+                const double *weights, const double *mins, const double *maxs, const wc_image_desc *images, int n,
+                const double *seed, int n_seeds, double *probs, double *grad_pixels, double *grad_weights);
+
 /* wc_wnd_classify_images: TrainingSet::ClassifyImage with WND-5
  * (src/wndchrm_src/TrainingSet.cpp:1603-1800) for n_images images of `tiles`
  * samples each: test holds n_images * tiles rows, an image's tiles consecutive.

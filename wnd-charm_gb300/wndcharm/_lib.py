@@ -86,6 +86,8 @@ def lib():
         L.wc_wnd_classify_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp,
                                              ctypes.c_int, vp, vp]
         L.wc_wnd_last_stats.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
+        L.wc_wnd_grad.argtypes = [vp, vp, D, ctypes.c_int, I, ctypes.c_int, D, D, D, ctypes.POINTER(wc_image_desc),
+                                  ctypes.c_int, D, ctypes.c_int, D, D, D]
         L.wc_wnd_classify_images.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, D, I, D]
         _lib = L

@@ -63,3 +63,33 @@ def feature_vectors(n_train, n_test, n_features, n_classes, seed):
     xtr = mu[ytr] + rng.normal(size=(n_train, n_features))
     xte = mu[yte] + rng.normal(size=(n_test, n_features))
     return xtr, (ytr + 1).astype(np.int32), xte, (yte + 1).astype(np.int32)
+
+
+def config4(n=256, size=256, n_classes=4, seed=3, dtype=np.float32):
+    """The differentiation workload: float32 images in [0, 1] from the same
+    blob + grating generator, not rounded (background N(0.08, 0.02), blob
+    amplitudes U[0.3, 0.8], grating amplitude 0.06; shifted up when below 0 and
+    scaled down when above 1), classes interleaved.
+    Returns (list of 2-D float32 arrays, labels 1..C)."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:size, 0:size].astype(np.float64)
+    imgs, labels = [], []
+    for i in range(n):
+        c = i % n_classes
+        img = rng.normal(0.08, 0.02, size=(size, size))
+        k = int(rng.integers(5 + 5 * c, 15 + 5 * c + 1))
+        for _ in range(k):
+            s = rng.uniform(3.0, 3.0 + 2.0 * c) * size / 256.0
+            a = rng.uniform(0.3, 0.8)
+            cx, cy = rng.uniform(0, size), rng.uniform(0, size)
+            img += a * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) / (2.0 * s * s))
+        period = (8.0 + 4.0 * c) * size / 256.0
+        th = rng.uniform(0, np.pi)
+        img += 0.06 * np.sin(2.0 * np.pi * (xx * np.cos(th) + yy * np.sin(th)) / period)
+        # into [0, 1] by a shift and a scale rather than clipping, so that no
+        # plateau of equal pixels (a kink of max / order statistics) appears
+        img = img - min(0.0, img.min())
+        img = img / max(1.0, img.max())
+        imgs.append(img.astype(dtype))
+        labels.append(c + 1)
+    return imgs, np.array(labels, dtype=np.int32)

@@ -108,12 +108,22 @@ void wc_engine_destroy(wc_engine *engine);
  *   "qr_iter_per_tone" real-Schur iterations allowed per tone, 40 (Eigen 3.1.2's
  *                      m_maxIterationsPerRow, RealSchur.h); a matrix that runs
  *                      out gives f14 = 0, as the reference's unconverged solver.
+ *   "autotune"         1 (default): launch shapes chosen by the tuner (below);
+ *                      0: each stage's first candidate.
  *   "union_find_cap"   iterations allowed per union-find link in the object
  *                      labelling; 0 (default): the plane's pixel count, a bound
  *                      no correct run reaches.  A run that reaches the cap
  *                      returns WC_ERR_DEVICE (the bounded-wait error path).
  * Unknown names and out-of-range values give WC_ERR_ARG. */
 int wc_engine_set_option(wc_engine *engine, const char *name, long long value);
+/* The engine's launch-shape tuner (no reference counterpart).  Stages with
+ * several candidate launch shapes (the real-Schur work queue's grouping and
+ * CTAs per SM, the Wavelet and Edge transforms' block shapes) try each once,
+ * per stage and size class, timing it with CUDA events, then keep the
+ * fastest ("autotune" option, on by default; 0 keeps the first candidate).
+ * The report has one line per key: "key<TAB>chosen<TAB>ms of candidate 0
+ * <TAB>..." (chosen -1 while still trying; -1 ms for an untried candidate). */
+int wc_engine_tuning_report(wc_engine *engine, char *buf, int buflen);
 /* CUDA stream the engine launches on (as a cudaStream_t cast to void*); 0 = legacy default */
 int wc_engine_set_stream(wc_engine *engine, void *stream);
 /* kernels launched by this engine since creation (counts every launch) */

@@ -138,7 +138,7 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
               std::vector<Plane> *planes_out) {
     const auto h0 = std::chrono::steady_clock::now();
     auto host_ms = [&h0]() { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count(); };
-    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof, &E->opts};
+    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof, &E->opts, &E->tune};
     // ---- nodes: every prefix of every group's transform chain
     std::vector<Node> nodes(1);
     nodes[0] = {-1, -1, 0, {}};
@@ -499,6 +499,7 @@ int extract_locked(wc_engine *E, const Plan &plan, const wc_image_desc *images, 
     }
     int dev_err = 0;
     if ((r = features_check(E->st, &dev_err))) return r;
+    E->tune.collect();  // the batch is complete: its tuning times are final
     if (dev_err) return set_err(WC_ERR_DEVICE, "a kernel reported error code %d", dev_err);
     return WC_OK;
 }
@@ -610,6 +611,10 @@ int wc_engine_set_option(wc_engine *E, const char *name, long long value) {
     } else if (k == "qr_iter_per_tone") {
         if (value < 1 || value > 1000000) return set_err(WC_ERR_ARG, "qr_iter_per_tone must be in 1..1e6");
         E->opts.qr_iter_per_tone = (int)value;
+    } else if (k == "autotune") {
+        if (value != 0 && value != 1) return set_err(WC_ERR_ARG, "autotune must be 0 or 1");
+        E->tune.on = value != 0;
+        if (!value) E->tune.st.clear();
     } else if (k == "union_find_cap") {
         if (value < 0) return set_err(WC_ERR_ARG, "union_find_cap must be >= 0");
         E->opts.union_find_cap = value;
@@ -617,6 +622,20 @@ int wc_engine_set_option(wc_engine *E, const char *name, long long value) {
         return set_err(WC_ERR_ARG, "unknown engine option '%s'", name);
     }
     return WC_OK;
+}
+
+int wc_engine_tuning_report(wc_engine *E, char *buf, int buflen) {
+    if (!E || !buf || buflen < 1) return set_err(WC_ERR_ARG, "bad arguments");
+    std::lock_guard<std::mutex> lk(E->mu);
+    std::string s;
+    for (auto &kv : E->tune.st) {
+        s += kv.first + "\t" + std::to_string(kv.second.chosen);
+        for (float v : kv.second.ms) s += "\t" + std::to_string(v);
+        s += "\n";
+    }
+    if ((int)s.size() >= buflen) return set_err(WC_ERR_ARG, "buffer too small (%d bytes needed)", (int)s.size() + 1);
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return (int)s.size();
 }
 
 int wc_engine_set_stream(wc_engine *E, void *stream) {

@@ -99,6 +99,7 @@ struct wc_engine {
     std::mutex mu;
     wc::Prof prof;
     wc::Opts opts;
+    wc::Tuner tune;
     cudaStream_t lanes[WC_LANES] = {};
     cudaEvent_t fork_ev = nullptr, early_ev = nullptr, join_ev[WC_LANES] = {};
 };

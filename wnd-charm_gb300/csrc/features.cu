@@ -240,7 +240,8 @@ int features_prepare(FeatureSetup &fs) {
             hj.push_back(h);
         }
         fs.off["har_jobs"] = fs.put_copy(hj.data(), hj.size() * sizeof(HarJob));
-        fs.off["har_perm"] = fs.ws_take((4 * hj.size() + 1) * sizeof(int));  // + the count of large matrices
+        // + the count of large matrices and the work queue's two tickets
+        fs.off["har_perm"] = fs.ws_take((4 * hj.size() + 3) * sizeof(int));
     }
     // Edge features: magnitude / direction planes in the workspace, sorted copies
     if (!fj[A_EDGEF].empty()) {

@@ -4,6 +4,7 @@
 // Gini, Radon, Chebyshev coefficients).  FP64 arithmetic throughout.
 #include <cfloat>
 #include <cmath>
+#include <string>
 
 #include "kcommon.cuh"
 #include "kwavelet.cuh"
@@ -103,9 +104,18 @@ __global__ void k_edge(double *__restrict__ arena, const Plane *__restrict__ pla
 
 void launch_edge(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh) {
     if (njobs <= 0) return;
-    dim3 b(32, 8), g((maxw + 31) / 32, (maxh + 7) / 8, njobs);
+    // block shape from the tuner (per size class): 32 x 8, 64 x 4 or 16 x 16
+    const std::string key = "edge/" + std::to_string(maxw / 64) + "x" + std::to_string(maxh / 64) + "/" +
+                            std::to_string(njobs / 16);
+    const int cand = c.tune ? c.tune->pick(key, 3) : 0;
+    const dim3 b = cand == 0 ? dim3(32, 8) : (cand == 1 ? dim3(64, 4) : dim3(16, 16));
+    const dim3 g((maxw + b.x - 1) / b.x, (maxh + b.y - 1) / b.y, njobs);
+    Tuner::Pending tp;
+    const bool timing = c.tune && c.tune->exploring(key);
+    if (timing) c.tune->begin(key, cand, c.st, tp);
     WC_LAUNCH(c);
     k_edge<<<g, b, 0, c.st>>>(arena, planes, jobs);
+    if (timing) c.tune->end(tp, c.st);
 }
 
 // ---------------------------------------------------------------- Wavelet transform
@@ -144,11 +154,21 @@ void launch_wavelet(Ctx &c, double *arena, const Plane *planes, const TJob *jobs
                     double *tmp, const long long *tmp_off) {
     if (njobs <= 0) return;
     int ox = (maxw + 9) / 2, oy = (maxh + 9) / 2;
-    dim3 b(32, 8);
+    // block shape of both passes from the tuner (per size class)
+    const std::string key = "wavelet/" + std::to_string(maxw / 64) + "x" + std::to_string(maxh / 64) + "/" +
+                            std::to_string(njobs / 16);
+    const int cand = c.tune ? c.tune->pick(key, 3) : 0;
+    const dim3 b = cand == 0 ? dim3(32, 8) : (cand == 1 ? dim3(64, 4) : dim3(16, 16));
+    Tuner::Pending tp;
+    const bool timing = c.tune && c.tune->exploring(key);
+    if (timing) c.tune->begin(key, cand, c.st, tp);
     WC_LAUNCH(c);
-    k_wavelet_y<<<dim3((maxw + 31) / 32, (oy + 7) / 8, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp, tmp_off);
+    k_wavelet_y<<<dim3((maxw + b.x - 1) / b.x, (oy + b.y - 1) / b.y, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp,
+                                                                                          tmp_off);
     WC_LAUNCH(c);
-    k_wavelet_x<<<dim3((ox + 31) / 32, (oy + 7) / 8, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp, tmp_off);
+    k_wavelet_x<<<dim3((ox + b.x - 1) / b.x, (oy + b.y - 1) / b.y, njobs), b, 0, c.st>>>(arena, planes, jobs, tmp,
+                                                                                         tmp_off);
+    if (timing) c.tune->end(tp, c.st);
 }
 
 // ---------------------------------------------------------------- pixel statistics + Gini

@@ -844,6 +844,7 @@ extern "C" int wc_wnd_grad(wc_engine *E, const wc_plan *plan, const double *trai
     {
         int dev_err = 0;
         if ((rc = features_check(st, &dev_err))) return rc;
+        E->tune.collect();
         if (dev_err) return set_err(WC_ERR_DEVICE, "a kernel reported error code %d", dev_err);
     }
     const double *arena = (const double *)E->arena.p;

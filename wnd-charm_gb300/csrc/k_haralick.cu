@@ -11,6 +11,7 @@
 // same gray image.  The eigen-solver is the same algorithm, loop orders and
 // rounding (no contraction) as the oracle's restatement of Eigen 3.1.2.
 #include <cfloat>
+#include <string>
 #include <cmath>
 
 #include "kcommon.cuh"
@@ -499,7 +500,11 @@ __global__ void __launch_bounds__(256) k_har_order(const HarJob *__restrict__ hj
         perm[atomicAdd(&cnt[256 - n], 1)] = m;
     }
     __syncthreads();
-    if (threadIdx.x == 0) perm[nmat] = cnt[256 - QR_BIG];  // after placement cnt[k] = end of key k: matrices with Ng >= QR_BIG
+    if (threadIdx.x == 0) {
+        perm[nmat] = cnt[256 - QR_BIG];  // after placement cnt[k] = end of key k: matrices with Ng >= QR_BIG
+        perm[nmat + 1] = 0;              // the work queue's tickets (k_har_qr_queue)
+        perm[nmat + 2] = 0;
+    }
 }
 
 #define QR_SYNC()                    \
@@ -1229,42 +1234,56 @@ __global__ void __launch_bounds__(256) k_har_hess_df(const HarJob *__restrict__ 
     }
 }
 
-// Matrices with at least QR_BIG tones (the long chains) get 4 warps each, one
-// per SM sub-partition, which quarters the reflector updates on the critical
-// path, as long as there are no more of them than max_groups; the rest (and
-// all of them beyond that) run one per warp, 4 to a block.  perm lists the
-// matrices by descending Ng and nbig counts the large ones.
+// The real-Schur QR of every matrix as a persistent work queue: a grid of a few CTAs
+// per SM, each of 4 warps.  While large matrices remain (those with at least
+// QR_BIG tones, first in the descending order, when `groups` is set) a CTA
+// takes the next one as a 4-warp group through ticket 0; then every warp
+// takes single matrices, largest first, through ticket 1, until the list is
+// exhausted.  A CTA that finishes a short matrix takes the next, so uneven
+// tone counts (uneven tiles, uneven planes) balance themselves; no thread
+// ever waits on another CTA.
 template <bool MIXED>
-__global__ void __launch_bounds__(128) k_har_qr(const HarJob *__restrict__ hj, char *__restrict__ wsb,
-                                                const int *__restrict__ perm, const int *__restrict__ nbig_p, int nmat,
-                                                int max_groups, int iter_per_tone) {
+__global__ void __launch_bounds__(128) k_har_qr_queue(const HarJob *__restrict__ hj, char *__restrict__ wsb,
+                                                      int *__restrict__ perm, int nmat, int groups,
+                                                      int iter_per_tone) {
     __shared__ double rowsum[4][256];
-    // groups only while every large matrix can have an SM to itself; beyond that
-    // the FP64 pipes are shared anyway and one warp per matrix issues fewer
-    // instructions (no reflector formed four times)
-    const int nbig = *nbig_p <= max_groups ? *nbig_p : 0;
-    int m, wq = 0;
-    if ((int)blockIdx.x < nbig) {
-        m = perm[blockIdx.x];
-    } else {
-        wq = threadIdx.x >> 5;
-        const int idx = nbig + ((int)blockIdx.x - nbig) * 4 + wq;
-        if (idx >= nmat) return;
-        m = perm[idx];
+    __shared__ int s_take;
+    int *tick = perm + nmat + 1;
+    const int nbig = groups ? perm[nmat] : 0;
+    const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // phase 1: 4-warp groups on the large matrices
+    for (;;) {
+        if (threadIdx.x == 0) s_take = atomicAdd(&tick[0], 1);
+        __syncthreads();
+        const int b = s_take;
+        __syncthreads();
+        if (b >= nbig) break;
+        const int m = perm[b];
+        const HarJob H = hj[m >> 2];
+        const int ang = m & 3;
+        const int n = ((const int *)(wsb + H.lut_b))[256];
+        double *res = (double *)(wsb + H.res_b) + ang * 14;
+        double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
+        if (MIXED) har_schur_df<4>((df *)A, n, (float *)rowsum[0], res, threadIdx.x, iter_per_tone);
+        else har_schur<4>(A, n, rowsum[0], res, threadIdx.x, iter_per_tone);
+        __syncthreads();
     }
-    const HarJob H = hj[m >> 2];
-    const int ang = m & 3;
-    const int n = ((const int *)(wsb + H.lut_b))[256];
-    double *res = (double *)(wsb + H.res_b) + ang * 14;
-    double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
-    if (MIXED) {
-        float *rs = (float *)rowsum[(int)blockIdx.x < nbig ? 0 : wq];
-        if ((int)blockIdx.x < nbig) har_schur_df<4>((df *)A, n, rs, res, threadIdx.x, iter_per_tone);
-        else har_schur_df<1>((df *)A, n, rs, res, threadIdx.x & 31, iter_per_tone);
-        return;
+    // phase 2: one warp per matrix
+    for (;;) {
+        int s = 0;
+        if (lane == 0) s = atomicAdd(&tick[1], 1);
+        s = __shfl_sync(0xffffffffu, s, 0);
+        const int idx = nbig + s;
+        if (idx >= nmat) break;
+        const int m = perm[idx];
+        const HarJob H = hj[m >> 2];
+        const int ang = m & 3;
+        const int n = ((const int *)(wsb + H.lut_b))[256];
+        double *res = (double *)(wsb + H.res_b) + ang * 14;
+        double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
+        if (MIXED) har_schur_df<1>((df *)A, n, (float *)rowsum[wq], res, lane, iter_per_tone);
+        else har_schur<1>(A, n, rowsum[wq], res, lane, iter_per_tone);
     }
-    if ((int)blockIdx.x < nbig) har_schur<4>(A, n, rowsum[0], res, threadIdx.x, iter_per_tone);
-    else har_schur<1>(A, n, rowsum[wq], res, threadIdx.x & 31, iter_per_tone);
 }
 
 // mean and range over the angles, permuted into the output order
@@ -1331,13 +1350,23 @@ void launch_haralick(Ctx &c, const double *arena, const Plane *planes, const Pla
     ProfScope p4(c, "Haralick: real Schur (f14)");
     WC_LAUNCH(c);
     k_har_order<<<1, 256, 0, c.st>>>(hj, wsb, 4 * njobs, perm);
+    // The work-queue kernel with the shape the tuner picks for this chain and
+    // batch size: 4-warp groups for the large matrices or not, 5 or 3 CTAs
+    // per SM (candidate 0: groups, 5 per SM, also used with tuning off).
+    const int nmat = 4 * njobs;
+    int lg = 0;
+    while ((1 << lg) < nmat) lg++;
+    const std::string key = std::string(df14 ? "har_qr/pairs/" : "har_qr/fp64/") + std::to_string(lg);
+    const int cand = c.tune ? c.tune->pick(key, 3) : 0;
+    const int groups = cand != 1, per_sm = cand == 2 ? 3 : 5;
+    const int grid = std::max(1, std::min(c.sms * per_sm, (nmat + 3) / 4));
+    Tuner::Pending tp;
+    const bool timing = c.tune && c.tune->exploring(key);
+    if (timing) c.tune->begin(key, cand, c.st, tp);
     WC_LAUNCH(c);
-    if (df14)
-        k_har_qr<true><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, c.sms, ipt);
-    // the FP64 chain keeps the 4-warp groups at every batch size (measured faster in
-    // the FP64 form: its other families load the FP64 pipes more)
-    else
-        k_har_qr<false><<<4 * njobs, 128, 0, c.st>>>(hj, wsb, perm, perm + 4 * njobs, 4 * njobs, 1 << 30, ipt);
+    if (df14) k_har_qr_queue<true><<<grid, 128, 0, c.st>>>(hj, wsb, perm, nmat, groups, ipt);
+    else k_har_qr_queue<false><<<grid, 128, 0, c.st>>>(hj, wsb, perm, nmat, groups, ipt);
+    if (timing) c.tune->end(tp, c.st);
     }
     WC_LAUNCH(c);
     k_har_final<<<njobs, 32, 0, c.st>>>(jobs, hj, wsb, feat);

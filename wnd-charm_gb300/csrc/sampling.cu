@@ -250,7 +250,7 @@ static int prepare_samples(wc_engine *E, const wc_image_desc *imgs, int n, const
             CK(cudaMemcpyAsync(base + stage_off[b], imgs[b].pixels,
                                (size_t)imgs[b].width * imgs[b].height * elem_size(imgs[b].dtype),
                                cudaMemcpyHostToDevice, E->st));
-    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof, &E->opts};
+    Ctx ctx{E->st, &E->launches, E->prec, E->sms, &E->prof, &E->opts, &E->tune};
     {
         ProfScope ps(ctx, "preprocess");
         const double *yh = E->tabs.d() + wf_tab;

@@ -1,5 +1,8 @@
 // Internal definitions shared by the host executor and the CUDA kernels.
 #pragma once
+#include <map>
+#include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <string>
@@ -133,6 +136,78 @@ struct Opts {
     long long union_find_cap = 0;
 };
 
+// Online autotuner of launch shapes (the engine's own): a stage with several
+// candidate shapes asks pick(key, n) per batch; each candidate is tried once
+// (explore: its launch bracketed by CUDA events on its stream), and once all
+// have a time the fastest is kept for that key (exploit).  Keys name the stage
+// and a size class, so a new batch size or image size is tuned again.
+struct Tuner {
+    bool on = true;
+    struct State {
+        std::vector<float> ms;  // per candidate: measured time (< 0: not yet)
+        int chosen = -1;
+    };
+    std::map<std::string, State> st;
+    struct Pending {
+        std::string key;
+        int cand;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pend;
+    // candidate for this batch (0 when tuning is off)
+    int pick(const std::string &key, int n) {
+        if (!on || n <= 1) return 0;
+        State &s = st[key];
+        if ((int)s.ms.size() != n) s.ms.assign(n, -1.f);
+        if (s.chosen >= 0) return s.chosen;
+        for (int c = 0; c < n; c++)
+            if (s.ms[c] < 0) return c;
+        return 0;
+    }
+    bool exploring(const std::string &key) const {
+        auto it = st.find(key);
+        return on && it != st.end() && it->second.chosen < 0;
+    }
+    void begin(const std::string &key, int cand, cudaStream_t s, Pending &p) {
+        p.key = key;
+        p.cand = cand;
+        p.a = p.b = nullptr;
+        if (cudaEventCreate(&p.a) != cudaSuccess || cudaEventCreate(&p.b) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        cudaEventRecord(p.a, s);
+    }
+    void end(Pending &p, cudaStream_t s) {
+        if (!p.a) return;
+        cudaEventRecord(p.b, s);
+        pend.push_back(p);
+    }
+    // after the batch has completed: record the times, choose where all are known
+    void collect() {
+        for (auto &p : pend) {
+            float ms = -1.f;
+            if (cudaEventElapsedTime(&ms, p.a, p.b) != cudaSuccess) {
+                cudaGetLastError();
+                ms = -1.f;
+            }
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+            State &s = st[p.key];
+            if (ms >= 0 && p.cand < (int)s.ms.size() && s.chosen < 0) s.ms[p.cand] = ms;
+            bool all = !s.ms.empty();
+            for (float v : s.ms) all &= v >= 0;
+            if (all && s.chosen < 0) {
+                int b = 0;
+                for (int c = 1; c < (int)s.ms.size(); c++)
+                    if (s.ms[c] < s.ms[b]) b = c;
+                s.chosen = b;
+            }
+        }
+        pend.clear();
+    }
+};
+
 // Launch context handed to every kernel launcher.
 struct Ctx {
     cudaStream_t st;
@@ -141,6 +216,7 @@ struct Ctx {
     int sms;              // multiprocessors on the device
     Prof *prof;
     const Opts *opt;      // the engine's options
+    Tuner *tune;          // the engine's launch-shape tuner
 };
 struct ProfScope {  // may nest (e.g. a family's phases inside the family)
     Ctx &c;

@@ -303,6 +303,16 @@ class Engine(object):
     def set_stream(self, stream_ptr):
         check(lib().wc_engine_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
 
+    def tuning(self):
+        """The launch-shape tuner's state: {key: (chosen candidate, [ms per candidate])}."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        check(lib().wc_engine_tuning_report(self._h, buf, 1 << 16))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            f = line.split("\t")
+            out[f[0]] = (int(f[1]), [float(x) for x in f[2:]])
+        return out
+
     def set_option(self, name, value):
         """Engine option (wc_engine_set_option): 'f14_exact' (mixed form: f14
         through the FP64 chain, 1 by default), 'qr_iter_per_tone' (real-Schur

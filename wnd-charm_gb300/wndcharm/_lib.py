@@ -60,6 +60,7 @@ def lib():
         L.wc_engine_destroy.restype = None
         L.wc_engine_set_stream.argtypes = [vp, vp]
         L.wc_engine_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong]
+        L.wc_engine_tuning_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
         L.wc_engine_launch_count.argtypes = [vp]
         L.wc_engine_launch_count.restype = ctypes.c_longlong
         L.wc_engine_profile.argtypes = [vp, ctypes.c_int]

@@ -349,8 +349,9 @@ def run_wnd(args, reference=False):
     hxn, hyn, htn = hx.numpy(), hy.numpy(), ht.numpy()
 
     def step_e2e():
-        w, mn, mx = emx.wnd_fit(hxn, hyn, C, 0.15)
-        emx.wnd_classify(hxn, hyn, C, w, mn, mx, htn)
+        # the reference's classification run: fit on the training rows, then
+        # classify the test rows, each host array copied to the GPU once
+        emx.wnd_fit_classify(hxn, hyn, C, htn, 0.15)
 
     step_e2e()
     t_e2e, _ = timed(step_e2e, args.steps)
@@ -377,7 +378,7 @@ def run_wnd(args, reference=False):
             "issued_frac": st[5] / kern_s / 1e12 / peak if kern_s else None,
             "issued_note": "13 digit-pair bf16 products per term over padded sizes (exact digit arithmetic)"}
     v = T * args.steps / t_dev
-    h2d = 2 * N * F * 8 + T * F * 8 + 2 * N * 4 + 2 * F * 8
+    h2d = N * F * 8 + T * F * 8 + N * 4
     d2h = 3 * F * 8 + T * C * 8 + T * 4
     line = {"metric": WND_METRIC, "value": v, "unit": "test vectors/s",
             "mixed_vs_fp64": v / (T * k64 / t64), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -501,8 +502,7 @@ def run_short(args, reference=False):
         wndcharm.check(L.wc_extract_batch(eng._h, plan.handle, descs_host, 40, ctypes.c_void_p(out_host.data_ptr()),
                                           0))
         rows = out_host.numpy()
-        w, mn, mx = eng.wnd_fit(rows[:30], labels[:30], 2, 0.15)
-        res["p"], res["pred"] = eng.wnd_classify(rows[:30], labels[:30], 2, w, mn, mx, rows[30:])
+        res["p"], res["pred"], _, _, _ = eng.wnd_fit_classify(rows[:30], labels[:30], 2, rows[30:], 0.15)
 
     def timed(fn, k):
         tot = 0.0
@@ -531,7 +531,7 @@ def run_short(args, reference=False):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_dev / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(SHORT_CONFIG), "precision_form": "fp64",
-            "e2e": {"value": 40 * args.steps / t_e2e, "unit": "images/s", "h2d_bytes_per_step": 40 * 256 * 256 + 2 * 30 * nf * 8 + 10 * nf * 8,
+            "e2e": {"value": 40 * args.steps / t_e2e, "unit": "images/s", "h2d_bytes_per_step": 40 * 256 * 256 + 30 * nf * 8 + 10 * nf * 8 + 30 * 4,
                     "d2h_bytes_per_step": 40 * nf * 8 + 3 * nf * 8 + 10 * 2 * 8 + 40},
             "gpu_launches": int(launches), "clocks": summarize_clocks(samples),
             "predicted": [int(v) for v in dpr.cpu().numpy()], "truth": [int(v) for v in labels[30:]]}

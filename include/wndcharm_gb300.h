@@ -171,6 +171,23 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
                     const double *weights, const double *mins, const double *maxs, const double *test, int T,
                     double *probs, int *pred);
 
+/* signatures::normalize (src/wndchrm_src/signatures.cpp:196-215) of n rows of F
+ * features against (mins, maxs): 0 for NaN, below the range or a range below
+ * DBL_EPSILON, 100 above it, else 100 * ((v - min) / (max - min)) with the
+ * correctly rounded quotient; the values every WND-5 call compares. */
+int wc_wnd_normalize(wc_engine *engine, const double *rows, int n, int F, const double *mins, const double *maxs,
+                     double *out);
+
+/* wc_wnd_fit followed by wc_wnd_classify of `test` against the same training
+ * rows, as the reference's classification run does them in one process
+ * (TrainingSet::normalize, SetFisherScores, then classify2 per test sample:
+ * src/wndchrm_src/wndchrm.cpp, TrainingSet.cpp:2090-2324, 2429-2586): each
+ * host array is copied to the GPU once.  Outputs: weights, mins, maxs (F), probs
+ * (T x C), pred (T). */
+int wc_wnd_fit_classify(wc_engine *engine, const double *train, int N, int F, const int *labels, int C, double frac,
+                        const double *test, int T, double *weights, double *mins, double *maxs, double *probs,
+                        int *pred);
+
 /* Device-pointer forms of wc_wnd_fit and wc_wnd_classify (same semantics):
  * every array argument is a device pointer on the engine's GPU, so rows that
  * are already in device memory (e.g. feature rows of wc_extract_batch with

@@ -91,3 +91,48 @@ def test_device_entry_points_match_host_ones():
     torch.cuda.synchronize()
     np.testing.assert_array_equal(dpr.cpu().numpy(), pr)
     np.testing.assert_array_equal(dp.cpu().numpy(), p)
+
+
+def test_normalisation_matches_the_division():
+    """signatures::normalize on the GPU (the values every WND-5 kernel
+    compares) takes the quotient by Markstein's method: equal bit for bit to
+    numpy's IEEE division on random rows and on the edges (the range's ends,
+    NaN, values outside it, a range below DBL_EPSILON, subnormal and huge
+    offsets, ranges near 2^900 and 2^-900)."""
+    import wndcharm
+    rng = np.random.default_rng(11)
+    F = 64
+    mn = rng.normal(size=F) * 10.0 ** rng.integers(-8, 9, size=F)
+    mx = mn + np.abs(rng.normal(size=F)) * 10.0 ** rng.integers(-12, 12, size=F)
+    mn[0], mx[0] = 0.0, 2.0 ** 950
+    mn[1], mx[1] = 1.0, 1.0 + 2.0 ** -40
+    mn[2], mx[2] = 5.0, 5.0 + 1e-17  # range below DBL_EPSILON
+    mn[3], mx[3] = -2.0 ** 901, 2.0 ** 901
+    mn[4], mx[4] = 0.0, 1e-300
+    X = mn + (mx - mn) * rng.uniform(-0.1, 1.1, size=(20000, F))
+    X[0] = mn
+    X[1] = mx
+    X[2] = np.nan
+    X[3] = np.nextafter(mn, np.inf)
+    X[4, 4] = 5e-324
+    X[5, 4] = 2.0 ** -1000
+    X[6, 0] = 2.0 ** -901
+    out = wndcharm.Engine(0, "fp64").wnd_normalize(X, mn, mx)
+    with np.errstate(all="ignore"):
+        ref = 100 * ((X - mn) / (mx - mn))
+    ref = np.where(X > mx, 100.0, ref)
+    ref = np.where(np.isnan(X) | (X < mn) | ((mx - mn) < np.finfo(np.float64).eps), 0.0, ref)
+    np.testing.assert_array_equal(out, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_fit_classify_matches_separate_calls(prec):
+    import wndcharm
+    from wndcharm import synth
+    xtr, ytr, xte, _ = synth.feature_vectors(2500, 300, 1059, 5, 9)
+    e = wndcharm.Engine(0, prec)
+    w, mn, mx = e.wnd_fit(xtr, ytr, 5, 0.15)
+    p, pr = e.wnd_classify(xtr, ytr, 5, w, mn, mx, xte)
+    p2, pr2, w2, mn2, mx2 = e.wnd_fit_classify(xtr, ytr, 5, xte, 0.15)
+    for a, b in ((w2, w), (mn2, mn), (mx2, mx), (pr2, pr), (p2, p)):
+        np.testing.assert_array_equal(a, b)

@@ -96,12 +96,6 @@ __global__ void k_wnd_fit_count(const int *__restrict__ y, int N, int C, long lo
     if (threadIdx.x <= 16 && sc[threadIdx.x]) atomicAdd((unsigned long long *)&cnt[threadIdx.x], sc[threadIdx.x]);
 }
 
-__device__ __forceinline__ double fit_norm(double v, double mn, double mx) {
-    if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) return 0.0;
-    if (v > mx) return 100.0;
-    return 100 * ((v - mn) / (mx - mn));
-}
-
 // second = 0: per-range sums of the normalised values, slot 0 over every
 // labelled row, slot c over class c; second = 1: per-range sums of squared
 // deviations from the class means (mean[c * F + f])
@@ -117,6 +111,7 @@ __global__ void __launch_bounds__(256) k_wnd_fit_moments(const double *__restric
     for (int c = 0; c <= C; c++) acc[wp][c][lane] = 0.0;
     if (f < F) {
         const double mn = mins[f], mx = maxs[f];
+        const double2 rc = wnd_recip(mn, mx);
         for (int s = s0 + wp; s < s1; s += 8 * FIT_U) {
             // FIT_U rows' loads in flight, then added in row order
             double xv[FIT_U];
@@ -130,7 +125,7 @@ __global__ void __launch_bounds__(256) k_wnd_fit_moments(const double *__restric
 #pragma unroll
             for (int u = 0; u < FIT_U; u++) {
                 const int c = cv[u];
-                const double v = fit_norm(xv[u], mn, mx);
+                const double v = wnd_norm(xv[u], mn, mx, rc);
                 if (!second) {
                     if (c) acc[wp][0][lane] += v;
                     if (c >= 1 && c <= C) acc[wp][c][lane] += v;
@@ -187,34 +182,46 @@ __global__ void k_wnd_fit_combine(const double *__restrict__ part, int R, int F,
 // gather the kept features, normalised: Xc is K x rows (column-major per row
 // set) so lanes reading consecutive rows coalesce.
 __global__ void k_wnd_gather(const double *__restrict__ X, int rows, int F, const int *__restrict__ keep, int K,
-                             const double *__restrict__ mins, const double *__restrict__ maxs, double *__restrict__ Xc) {
+                             const double *__restrict__ mins, const double *__restrict__ maxs,
+                             const double2 *__restrict__ rec, double *__restrict__ Xc) {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (q >= (long long)rows * K) return;
     const int k = (int)(q / rows), s = (int)(q - (long long)k * rows);
     const int f = keep[k];
     const double mn = mins[f], mx = maxs[f];
-    double v = X[(long long)s * F + f];
-    if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) v = 0;
-    else if (v > mx) v = 100;
-    else v = 100 * ((v - mn) / (mx - mn));
-    Xc[(long long)k * rows + s] = v;
+    Xc[(long long)k * rows + s] = wnd_norm(X[(long long)s * F + f], mn, mx, rec[f]);
 }
 
 // rows of X (by index) gathered and normalised into the FP64 kernel's
 // column-major layout, Xc[k * n + i]
 __global__ void k_wnd_gather_rows(const double *__restrict__ X, const int *__restrict__ rowsel, int n, int F,
                                   const int *__restrict__ keep, int K, const double *__restrict__ mins,
-                                  const double *__restrict__ maxs, double *__restrict__ Xc) {
+                                  const double *__restrict__ maxs, const double2 *__restrict__ rec,
+                                  double *__restrict__ Xc) {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (q >= (long long)n * K) return;
     const int k = (int)(q / n), i = (int)(q - (long long)k * n);
     const int f = keep[k];
     const double mn = mins[f], mx = maxs[f];
-    double v = X[(long long)rowsel[i] * F + f];
-    if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) v = 0;
-    else if (v > mx) v = 100;
-    else v = 100 * ((v - mn) / (mx - mn));
-    Xc[(long long)k * n + i] = v;
+    Xc[(long long)k * n + i] = wnd_norm(X[(long long)rowsel[i] * F + f], mn, mx, rec[f]);
+}
+
+// rows normalised against (mins, maxs), elementwise
+__global__ void k_wnd_normalize(const double *__restrict__ X, long long n, int F, const double *__restrict__ mins,
+                                const double *__restrict__ maxs, const double2 *__restrict__ rec,
+                                double *__restrict__ out) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n * F;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(q % F);
+        out[q] = wnd_norm(X[q], mins[f], maxs[f], rec[f]);
+    }
+}
+
+// the per-feature reciprocal pairs wnd_norm takes, from the range
+__global__ void k_wnd_recip(const double *__restrict__ mins, const double *__restrict__ maxs, int F,
+                            double2 *__restrict__ rec) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < F) rec[f] = wnd_recip(mins[f], maxs[f]);
 }
 
 __global__ void k_wnd_scatter_rows(const int *__restrict__ rowsel, int n, int C, const double *__restrict__ sp,
@@ -597,8 +604,8 @@ done:
 namespace wc {
 int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double *dX, int N, int F, const int *labels,
                     int C, const double *dT, int T, const std::vector<int> &keep, const std::vector<double> &w,
-                    const double *dmin, const double *dmax, double *dprob, int *dpred, double *dnorm,
-                    std::vector<int> &recheck, long long *info);
+                    const double *dmin, const double *dmax, const double2 *drec, double *dprob, int *dpred,
+                    double *dnorm, std::vector<int> &recheck, long long *info);
 bool wnd_tc_supported(int K);
 }  // namespace wc
 
@@ -638,7 +645,7 @@ struct WBufs {
 // over the whole GPU.
 int fp64_rows(cudaStream_t st, long long *launches, const double *dX, const double *dT, int N, int F, const int *dy,
               int C, const std::vector<int> &keep_h, const int *dkeep, const double *dw2, const double *dmin,
-              const double *dmax, const std::vector<int> &rows, double *dprob, int *dpred, double *dnorm,
+              const double *dmax, const double2 *drec, const std::vector<int> &rows, double *dprob, int *dpred, double *dnorm,
               bool all_rows) {
     const int K = (int)keep_h.size();
     const int n = (int)rows.size();
@@ -658,10 +665,11 @@ int fp64_rows(cudaStream_t st, long long *launches, const double *dX, const doub
     CKR(cudaMemcpyAsync(drows, rows.data(), n * 4, cudaMemcpyHostToDevice, st));
     if (K) {
         ++*launches;
-        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, dXc);
+        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, drec,
+                                                                            dXc);
         ++*launches;
         k_wnd_gather_rows<<<(int)(((long long)n * K + 255) / 256), 256, 0, st>>>(dT, drows, n, F, dkeep, K, dmin,
-                                                                                     dmax, dTc);
+                                                                                     dmax, drec, dTc);
     }
     *launches += 3;
     k_wnd_dist<<<dim3((n + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, n, dXc, N, dy, dw2, K, C, per, dps, dpc);
@@ -697,8 +705,12 @@ static int wnd_classify_dev(wc_engine *E, const double *dX, int N, int F, const 
     WBufs B;
     int *dy, *dkeep;
     double *dw2;
-    if ((rc = B.get(&dy, N * 4)) || (rc = B.get(&dkeep, std::max(K, 1) * 4)) || (rc = B.get(&dw2, std::max(K, 1) * 8)))
+    double2 *drec;
+    if ((rc = B.get(&dy, N * 4)) || (rc = B.get(&dkeep, std::max(K, 1) * 4)) || (rc = B.get(&dw2, std::max(K, 1) * 8)) ||
+        (rc = B.get(&drec, (size_t)F * 16)))
         return rc;
+    ++*launches;
+    k_wnd_recip<<<(F + 255) / 256, 256, 0, st>>>(dmin, dmax, F, drec);
     CKR(cudaMemcpyAsync(dy, labels, N * 4, cudaMemcpyHostToDevice, st));
     if (K) {
         CKR(cudaMemcpyAsync(dkeep, keep.data(), K * 4, cudaMemcpyHostToDevice, st));
@@ -710,7 +722,7 @@ static int wnd_classify_dev(wc_engine *E, const double *dX, int N, int F, const 
         // tensor cores, then the FP64 kernel for the rows they cannot certify
         std::vector<int> rows;
         long long info[3] = {0, 0, 0};
-        rc = wnd_tc_classify(st, launches, engine_sms(E), dX, N, F, labels, C, dT, T, keep, w, dmin, dmax, dprob, dpred,
+        rc = wnd_tc_classify(st, launches, engine_sms(E), dX, N, F, labels, C, dT, T, keep, w, dmin, dmax, drec, dprob, dpred,
                              dnorm, rows, info);
         if (rc == WC_ERR_UNSUPPORTED) goto pairs;
         if (rc) return rc;
@@ -719,7 +731,7 @@ static int wnd_classify_dev(wc_engine *E, const double *dX, int N, int F, const 
         g_last_stats[3] = info[0];
         g_last_stats[4] = info[1];
         g_last_stats[5] = info[2];
-        return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, rows, dprob, dpred, dnorm,
+        return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, drec, rows, dprob, dpred, dnorm,
                          false);
     }
 pairs:
@@ -735,8 +747,10 @@ pairs:
             (rc = B.get(&fX, (size_t)N * K * 8)) || (rc = B.get(&fT, (size_t)T * K * 8)) || (rc = B.get(&fw, K * 8)))
             return rc;
         *launches += 7;
-        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, dXc);
-        k_wnd_gather<<<(int)(((long long)T * K + 255) / 256), 256, 0, st>>>(dT, T, F, dkeep, K, dmin, dmax, dTc);
+        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, drec,
+                                                                            dXc);
+        k_wnd_gather<<<(int)(((long long)T * K + 255) / 256), 256, 0, st>>>(dT, T, F, dkeep, K, dmin, dmax, drec,
+                                                                            dTc);
         k_wnd_split<<<1024, 256, 0, st>>>(dXc, (long long)N * K, fX);
         k_wnd_split<<<1024, 256, 0, st>>>(dTc, (long long)T * K, fT);
         k_wnd_split<<<1, 256, 0, st>>>(dw2, K, fw);
@@ -749,7 +763,7 @@ pairs:
     {
         std::vector<int> all(T);
         for (int t = 0; t < T; t++) all[t] = t;
-        return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, all, dprob, dpred, dnorm,
+        return fp64_rows(st, launches, dX, dT, N, F, dy, C, keep, dkeep, dw2, dmin, dmax, drec, all, dprob, dpred, dnorm,
                          true);
     }
 }
@@ -804,6 +818,87 @@ extern "C" int wc_wnd_classify(wc_engine *E, const double *train, int N, int F, 
         return set_err(WC_ERR_ARG, "wc_wnd_classify: bad arguments (C must be 1..16)");
     return wnd_classify(E, train, N, F, labels, C, weights, mins, maxs, test, T, probs, pred, 0, 0, nullptr, nullptr,
                         nullptr);
+}
+
+// normalize + SetFisherScores on the training rows, then classify2 of the test
+// rows, with host buffers: each array crosses to the GPU once (the test rows'
+// copy overlaps the fit's kernels on a second stream)
+extern "C" int wc_wnd_fit_classify(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                                   double frac, const double *test, int T, double *weights, double *mins,
+                                   double *maxs, double *probs, int *pred) {
+    if (!E || !train || !labels || !test || !weights || !mins || !maxs || !probs || !pred || N < 1 || F < 1 ||
+        T < 1 || C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_fit_classify: bad arguments (C must be 1..16)");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    WBufs B;
+    double *dX, *dT, *dmin, *dmax, *dprob, *dnorm;
+    int *dy, *dpred;
+    if ((rc = B.get(&dX, (size_t)N * F * 8)) || (rc = B.get(&dT, (size_t)T * F * 8)) || (rc = B.get(&dmin, F * 8)) ||
+        (rc = B.get(&dmax, F * 8)) || (rc = B.get(&dprob, (size_t)T * C * 8)) || (rc = B.get(&dpred, (size_t)T * 4)) ||
+        (rc = B.get(&dnorm, (size_t)T * 8)) || (rc = B.get(&dy, (size_t)N * 4)))
+        return rc;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev = nullptr;
+    CKR(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaStreamDestroy(side);
+        return set_err(WC_ERR_CUDA, "cudaEventCreate failed");
+    }
+    struct Release {
+        cudaStream_t s;
+        cudaEvent_t e;
+        ~Release() {
+            cudaStreamSynchronize(s);
+            cudaEventDestroy(e);
+            cudaStreamDestroy(s);
+        }
+    } rel{side, ev};
+    CKR(cudaMemcpyAsync(dX, train, (size_t)N * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dy, labels, (size_t)N * 4, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dT, test, (size_t)T * F * 8, cudaMemcpyHostToDevice, side));
+    CKR(cudaEventRecord(ev, side));
+    if ((rc = wnd_fit_dev(E, dX, N, F, dy, C, frac, weights, dmin, dmax))) return rc;
+    CKR(cudaStreamWaitEvent(st, ev, 0));
+    if ((rc = wnd_classify_dev(E, dX, N, F, labels, C, weights, dmin, dmax, dT, T, dprob, dpred, dnorm))) return rc;
+    CKR(cudaMemcpyAsync(mins, dmin, F * 8, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(maxs, dmax, F * 8, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(probs, dprob, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(pred, dpred, (size_t)T * 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    return WC_OK;
+}
+
+// signatures::normalize of n rows (host buffers)
+extern "C" int wc_wnd_normalize(wc_engine *E, const double *rows, int n, int F, const double *mins,
+                                const double *maxs, double *out) {
+    if (!E || !rows || !mins || !maxs || !out || n < 1 || F < 1)
+        return set_err(WC_ERR_ARG, "wc_wnd_normalize: bad arguments");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    WBufs B;
+    double *dX, *dmin, *dmax, *dout;
+    double2 *drec;
+    const size_t nb = (size_t)n * F * 8;
+    if ((rc = B.get(&dX, nb)) || (rc = B.get(&dout, nb)) || (rc = B.get(&dmin, F * 8)) || (rc = B.get(&dmax, F * 8)) ||
+        (rc = B.get(&drec, (size_t)F * 16)))
+        return rc;
+    CKR(cudaMemcpyAsync(dX, rows, nb, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dmin, mins, F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dmax, maxs, F * 8, cudaMemcpyHostToDevice, st));
+    *launches += 2;
+    k_wnd_recip<<<(F + 255) / 256, 256, 0, st>>>(dmin, dmax, F, drec);
+    const long long tot = (long long)n * F;
+    k_wnd_normalize<<<(int)std::min<long long>((tot + 255) / 256, 8 * 1024), 256, 0, st>>>(dX, n, F, dmin, dmax, drec,
+                                                                                           dout);
+    CKR(cudaGetLastError());
+    CKR(cudaMemcpyAsync(out, dout, nb, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    return WC_OK;
 }
 
 extern "C" int wc_wnd_classify_images(wc_engine *E, const double *train, int N, int F, const int *labels, int C,

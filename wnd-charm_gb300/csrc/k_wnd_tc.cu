@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // dmax (as float bits: non-negative floats order as integers).
 __global__ void k_wnd_tc_digits(const double *__restrict__ X, int rows, int F, const int *__restrict__ keep, int K,
                                 int Kp, const double *__restrict__ mins, const double *__restrict__ maxs,
-                                const double *__restrict__ w, const int *__restrict__ pos, long long rows_pad,
+                                const double2 *__restrict__ rec, const double *__restrict__ w, const int *__restrict__ pos, long long rows_pad,
                                 double inv_u, double scale_g, double scale_g2, __nv_bfloat16 *__restrict__ dig,
                                 float4 *__restrict__ stat, float4 *__restrict__ dnorm, int *__restrict__ dmax) {
     const int lane = threadIdx.x & 31;
@@ -391,10 +391,7 @@ __global__ void k_wnd_tc_digits(const double *__restrict__ X, int rows, int F, c
         if (k < K) {
             const int fcol = keep[k];
             const double mn = mins[fcol], mx = maxs[fcol];
-            double v = X[rw * F + fcol];
-            if (isnan(v) || v < mn || (mx - mn) < DBL_EPSILON) v = 0;
-            else if (v > mx) v = 100;
-            else v = 100 * ((v - mn) / (mx - mn));
+            const double v = wnd_norm(X[rw * F + fcol], mn, mx, rec[fcol]);
             const double x = (w[k] * (v - 50.0)) * inv_u;  // |x| <= 128 by the choice of u
             double rem = x;
             double xt = 0.0;
@@ -575,8 +572,8 @@ bool wnd_tc_supported(int K) { return K >= 1 && K <= tc::MAX_K; }
 // kernel must recompute (their device results are then to be replaced).
 int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double *dX, int N, int F,
                     const int *labels, int C, const double *dT, int T, const std::vector<int> &keep,
-                    const std::vector<double> &w, const double *dmin, const double *dmax, double *dprob, int *dpred,
-                    double *dnorm, std::vector<int> &recheck, long long *info) {
+                    const std::vector<double> &w, const double *dmin, const double *dmax, const double2 *drec,
+                    double *dprob, int *dpred, double *dnorm, std::vector<int> &recheck, long long *info) {
     using namespace tc;
     const int K = (int)keep.size();
     if (!wnd_tc_supported(K)) return set_err(WC_ERR_UNSUPPORTED, "tensor-core WND: K = %d", K);
@@ -665,9 +662,9 @@ int wnd_tc_classify(cudaStream_t st, long long *launches, int sms, const double 
     CKT(cudaMemcpyAsync(dw, w.data(), K * sizeof(double), cudaMemcpyHostToDevice, st));
     CKT(cudaMemcpyAsync(dncls, ncls.data(), C * sizeof(long long), cudaMemcpyHostToDevice, st));
     *launches += 5;
-    k_wnd_tc_digits<<<(N + 7) / 8, 256, 0, st>>>(dX, N, F, dkeep, K, Kp, dmin, dmax, dw, dpos, N_pad, inv_u, scale_g,
+    k_wnd_tc_digits<<<(N + 7) / 8, 256, 0, st>>>(dX, N, F, dkeep, K, Kp, dmin, dmax, drec, dw, dpos, N_pad, inv_u, scale_g,
                                                   scale_g2, digB, bstat, dnB, dmaxd);
-    k_wnd_tc_digits<<<(T + 7) / 8, 256, 0, st>>>(dT, T, F, dkeep, K, Kp, dmin, dmax, dw, nullptr, T_pad, inv_u, scale_g,
+    k_wnd_tc_digits<<<(T + 7) / 8, 256, 0, st>>>(dT, T, F, dkeep, K, Kp, dmin, dmax, drec, dw, nullptr, T_pad, inv_u, scale_g,
                                                   scale_g2, digA, astat, dnA, nullptr);
     k_wnd_tc_rowbound<<<(T + 255) / 256, 256, 0, st>>>(dnA, dmaxd, T, 7.0 * Kp, scale_c, astat, dflag);
     CUtensorMap mA, mB;

@@ -11,6 +11,33 @@ namespace wc {
 
 #define WC_LAUNCH(ctx) (++*(ctx).launches)
 
+// signatures::normalize's value of one feature (src/wndchrm_src/signatures.cpp:196-215;
+// TrainingSet::normalize, src/wndchrm_src/TrainingSet.cpp:2090-2123): 0 for NaN,
+// below the range or a range below DBL_EPSILON, 100 above it, else
+// 100 * ((v - mn) / (mx - mn)).  The quotient is the correctly rounded one, by
+// Markstein's method (P. Markstein, IBM J. Res. Develop. 34(1), 1990): with
+// yh = RN(1/d) and yl ~ 1/d - yh (wnd_recip), q0 = RN(a yh + RN(a yl)) is within
+// one ulp of a/d, r = a - d q0 is exact, and RN(q0 + r yh) = RN(a/d); four FP64
+// operations where a division takes several more.  Far from the normal range
+// (a < 2^-900, d > 2^900) the division itself is used.
+__host__ __device__ __forceinline__ double2 wnd_recip(double mn, double mx) {
+    const double d = mx - mn;
+    const double yh = 1.0 / d;
+    return make_double2(yh, fma(-yh, d, 1.0) * yh);
+}
+static __device__ __noinline__ double wnd_div_far(double a, double d) { return a / d; }
+__device__ __forceinline__ double wnd_norm(double v, double mn, double mx, double2 r) {
+    const double d = mx - mn;
+    if (isnan(v) || v < mn || d < DBL_EPSILON) return 0.0;
+    if (v > mx) return 100.0;
+    const double a = v - mn;
+    if (a == 0.0) return 0.0;
+    if (a < 0x1p-900 || d > 0x1p+900) return 100 * wnd_div_far(a, d);
+    const double q0 = fma(a, r.x, a * r.y);
+    const double res = fma(-q0, d, a);
+    return 100 * fma(res, r.x, q0);
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;

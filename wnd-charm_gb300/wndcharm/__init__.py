@@ -401,6 +401,33 @@ class Engine(object):
                                     pred.ctypes.data_as(_lib.I)))
         return probs, pred
 
+    def wnd_normalize(self, rows, mins, maxs):
+        """signatures::normalize of each row against (mins, maxs): values in [0, 100]."""
+        X = np.ascontiguousarray(rows, dtype=np.float64)
+        n, F = X.shape
+        mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (mins, maxs))
+        out = np.zeros_like(X)
+        check(lib().wc_wnd_normalize(self._h, X.ctypes.data_as(_lib.D), n, F, mn.ctypes.data_as(_lib.D),
+                                     mx.ctypes.data_as(_lib.D), out.ctypes.data_as(_lib.D)))
+        return out
+
+    def wnd_fit_classify(self, train, labels, n_classes, test, frac=0.15):
+        """wnd_fit on the training rows, then wnd_classify of the test rows,
+        each array copied to the GPU once: (probs, pred, weights, mins, maxs)."""
+        X = np.ascontiguousarray(train, dtype=np.float64)
+        y = np.ascontiguousarray(labels, dtype=np.int32)
+        T = np.ascontiguousarray(test, dtype=np.float64)
+        N, F = X.shape
+        nt = T.shape[0]
+        w, mn, mx = np.zeros(F), np.zeros(F), np.zeros(F)
+        probs = np.zeros((nt, n_classes))
+        pred = np.zeros(nt, dtype=np.int32)
+        check(lib().wc_wnd_fit_classify(self._h, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I),
+                                        int(n_classes), float(frac), T.ctypes.data_as(_lib.D), nt,
+                                        w.ctypes.data_as(_lib.D), mn.ctypes.data_as(_lib.D), mx.ctypes.data_as(_lib.D),
+                                        probs.ctypes.data_as(_lib.D), pred.ctypes.data_as(_lib.I)))
+        return probs, pred, w, mn, mx
+
     def wnd_classify_device(self, train, labels, n_classes, weights, mins, maxs, test, probs, pred):
         """wc_wnd_classify_device on device tensors (any objects with a
         data_ptr(): float64 train (N, F), int32 labels, float64 weights / mins /

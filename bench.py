@@ -232,6 +232,19 @@ def run_tiles(args):
     b.record(stream)
     b.synchronize()
     t_loop = a.elapsed_time(b) / 1000.0
+    # the same loop with CUDA-graph replay (a tile shape is captured once the
+    # tuner has settled and replayed for the image's remaining tiles)
+    g_eng = wndcharm.Engine(0, args.precision)
+    g_eng.set_stream(stream.cuda_stream)
+    g_eng.set_option("graph", 1)
+    g_eng.extract(plan, [sample[0]])
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for tl in sample:
+        g_eng.extract(plan, [np.ascontiguousarray(tl)])
+    b.record(stream)
+    b.synchronize()
+    t_graph = a.elapsed_time(b) / 1000.0
     print(json.dumps({"metric": "tiles/sec, 2919-feature set, 4x4 ROI tiles of uneven 64..1024 px uint16 images",
                       "value": tiles / t, "unit": "tiles/s", "images_per_s": B * args.steps / t,
                       "megapixels_per_s": px / t / 1e6, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -239,6 +252,9 @@ def run_tiles(args):
                       "data": "synthetic", "gpu_launches": eng.launches - l0, "rows_per_step": int(rows.shape[0]),
                       "one_tile_per_call": {"value": len(sample) / t_loop, "unit": "tiles/s",
                                             "sample": "the 64 tiles of 4 images, one wc_extract_batch call each"},
+                      "one_tile_per_call_graph": {"value": len(sample) / t_graph, "unit": "tiles/s",
+                                                  "graphs": g_eng.graph_stats(),
+                                                  "sample": "the same 64 calls with the engine option graph = 1"},
                       "batched_vs_one_tile_per_call": (tiles / t) / (len(sample) / t_loop),
                       "autotuned": {k: v[0] for k, v in eng.tuning().items()},
                       "config": {"workload": "uneven sides {64..1024} (seed 2), blob+grating, 8 classes, 4x4 tiles "

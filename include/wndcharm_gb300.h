@@ -114,8 +114,21 @@ void wc_engine_destroy(wc_engine *engine);
  *                      labelling; 0 (default): the plane's pixel count, a bound
  *                      no correct run reaches.  A run that reaches the cap
  *                      returns WC_ERR_DEVICE (the bounded-wait error path).
- * Unknown names and out-of-range values give WC_ERR_ARG. */
+ *   "graph"            0 (default); 1: wc_extract / wc_extract_batch capture the
+ *                      launches of a batch shape (plan, image types and sizes,
+ *                      output) in a CUDA graph the second time the shape is seen,
+ *                      once the tuner has chosen every launch shape it is
+ *                      timing, and later calls of that shape upload their
+ *                      metadata and pixels and replay the graph (no host
+ *                      planning, one launch call).  Results are those of the
+ *                      ungraphed path bit for bit.  Up to 16 shapes are kept.
+ * Unknown names and out-of-range values give WC_ERR_ARG.  Setting any option
+ * drops the engine's graphs. */
 int wc_engine_set_option(wc_engine *engine, const char *name, long long value);
+/* Graph use since creation: stats[0] captures, stats[1] replays, stats[2]
+ * shapes that could not be captured (they run without a graph), stats[3]
+ * graphs kept.  stats holds 4 values. */
+int wc_engine_graph_stats(wc_engine *engine, long long *stats);
 /* The engine's launch-shape tuner (no reference counterpart).  Stages with
  * several candidate launch shapes (the real-Schur work queue's grouping and
  * CTAs per SM, the Wavelet and Edge transforms' block shapes) try each once,

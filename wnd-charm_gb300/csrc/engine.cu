@@ -359,16 +359,20 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
     char *dm = (char *)E->meta.p;
     char *dw = (char *)E->ws.p;
     E->prof.host("host: plan the batch", host_ms());
+    E->last_in_off = in_off;
+    E->last_meta_used = meta.used;
     CK(cudaMemcpyAsync(dm, E->hmeta.data(), meta.used, cudaMemcpyHostToDevice, E->st));
+    for (int b = 0; b < n; b++)
+        if (!imgs[b].on_device)
+            CK(cudaMemcpyAsync((char *)E->stage.p + in_off[b], imgs[b].pixels,
+                               (size_t)imgs[b].width * imgs[b].height * pixel_bytes(imgs[b].dtype),
+                               cudaMemcpyHostToDevice, E->st));
+    // a graph holds the launches from here on (the uploads stay outside: a
+    // replay repeats them from the new call's buffers)
+    if (E->capture) CK(cudaStreamBeginCapture(E->st, cudaStreamCaptureModeThreadLocal));
     for (int b = 0; b < n; b++) {
         const wc_image_desc &I = imgs[b];
-        size_t es = pixel_bytes(I.dtype);
-        const void *src = I.pixels;
-        if (!I.on_device) {
-            CK(cudaMemcpyAsync((char *)E->stage.p + in_off[b], I.pixels, (size_t)I.width * I.height * es,
-                               cudaMemcpyHostToDevice, E->st));
-            src = (char *)E->stage.p + in_off[b];
-        }
+        const void *src = I.on_device ? I.pixels : (const void *)((char *)E->stage.p + in_off[b]);
         ProfScope ps(ctx, "convert");
         if (I.dtype == WC_RGB8 || I.dtype == WC_RGB16)
             launch_rgb_ingest(ctx, src, I.dtype, (long long)I.width * I.height, arena + planes[(size_t)b * NN].off,
@@ -475,10 +479,163 @@ int engine_device(wc_engine *E, cudaStream_t *st, long long **launches) {
 }
 }  // namespace wc
 
+// ================================================================= CUDA graphs
+namespace wc {
+
+// What makes two batches replayable by one graph: the plan's groups, the
+// images' types, sizes and bit depths (and device addresses), the output.
+static std::string batch_key(const Plan &plan, const wc_image_desc *imgs, int n, const double *out,
+                             int out_on_device) {
+    std::string k;
+    auto add = [&](const void *p, size_t b) { k.append((const char *)p, b); };
+    add(&plan.n_features, sizeof plan.n_features);
+    for (const Group &g : plan.groups) {
+        add(&g.alg, sizeof g.alg);
+        add(&g.offset, sizeof g.offset);
+        for (int t : g.chain) add(&t, sizeof t);
+        k.push_back('|');
+    }
+    add(&n, sizeof n);
+    add(&out_on_device, sizeof out_on_device);
+    if (out_on_device) add(&out, sizeof out);
+    for (int b = 0; b < n; b++) {
+        const wc_image_desc &I = imgs[b];
+        const int v[5] = {I.dtype, I.width, I.height, I.bits, I.on_device};
+        add(v, sizeof v);
+        if (I.on_device) add(&I.pixels, sizeof I.pixels);
+    }
+    return k;
+}
+
+// the device buffers a batch's launches address
+static std::vector<void *> graph_bufs(wc_engine *E) {
+    return {E->arena.p, E->feat.p, E->ws.p, E->meta.p, E->stage.p, E->clr.p, E->tabs.dev.p};
+}
+
+static void graph_drop(wc_engine *E, const std::string &key) {
+    auto it = E->graphs.find(key);
+    if (it == E->graphs.end()) return;
+    if (it->second.exec) cudaGraphExecDestroy(it->second.exec);
+    E->graphs.erase(it);
+    for (size_t i = 0; i < E->graph_fifo.size(); i++)
+        if (E->graph_fifo[i] == key) {
+            E->graph_fifo.erase(E->graph_fifo.begin() + i);
+            break;
+        }
+}
+
+void graphs_clear(wc_engine *E) {
+    for (auto &kv : E->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    E->graphs.clear();
+    E->graph_fifo.clear();
+    E->graph_seen.clear();
+}
+
+// a replay: the metadata blob and the pixels uploaded as run_batch uploads
+// them, then the captured launches
+static int graph_replay(wc_engine *E, const GraphEntry &g, const wc_image_desc *imgs, int n) {
+    CK(cudaMemcpyAsync(E->meta.p, g.hmeta.data(), g.hmeta.size(), cudaMemcpyHostToDevice, E->st));
+    for (int b = 0; b < n; b++) {
+        if (imgs[b].on_device) continue;
+        if (!imgs[b].pixels) return set_err(WC_ERR_ARG, "image %d: null pixels", b);
+        CK(cudaMemcpyAsync((char *)E->stage.p + g.in_off[b], imgs[b].pixels,
+                           (size_t)imgs[b].width * imgs[b].height * pixel_bytes(imgs[b].dtype), cudaMemcpyHostToDevice,
+                           E->st));
+    }
+    CK(cudaGraphLaunch(g.exec, E->st));
+    E->launches += g.launches;
+    E->graph_replays++;
+    return WC_OK;
+}
+
+static const int kCaptureFailed = 1;  // not a status of the C ABI (those are <= 0)
+
+// after a run_batch that captured: end the capture; on success keep the graph
+// and launch it (the capture only recorded the launches)
+static int graph_finish(wc_engine *E, const std::string &key, int r, long long launches) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamIsCapturing(E->st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone &&
+        cudaStreamEndCapture(E->st, &g) != cudaSuccess)
+        g = nullptr;
+    cudaGetLastError();
+    if (r) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
+    cudaGraphExec_t ex = nullptr;
+    const bool ok = g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        E->graph_failures++;
+        return kCaptureFailed;  // the caller runs the batch without a graph
+    }
+    while (E->graph_fifo.size() >= 16) graph_drop(E, E->graph_fifo.front());
+    GraphEntry &ge = E->graphs[key];
+    ge.exec = ex;
+    ge.hmeta.assign(E->hmeta.begin(), E->hmeta.begin() + E->last_meta_used);
+    ge.in_off = E->last_in_off;
+    ge.bufs = graph_bufs(E);
+    ge.launches = launches;
+    E->graph_fifo.push_back(key);
+    E->graph_captures++;
+    CK(cudaGraphLaunch(ex, E->st));
+    return WC_OK;
+}
+
+// run_batch, or with the option "graph" a replay of the graph captured for a
+// batch of the same shape: a shape is captured the second time it is seen,
+// once the launch-shape tuner has chosen every shape it is timing (the
+// captured launches then stay those choices), and replays while the device
+// buffers it addresses are unchanged
+static int run_batch_graphed(wc_engine *E, const Plan &plan, const wc_image_desc *images, int n, double *dfeat,
+                             double *out, int out_on_device) {
+    if (!E->graph || E->prof.on) return run_batch(E, plan, images, n, dfeat);
+    const std::string key = batch_key(plan, images, n, out, out_on_device);
+    auto it = E->graphs.find(key);
+    if (it != E->graphs.end()) {
+        if (it->second.bufs == graph_bufs(E)) return graph_replay(E, it->second, images, n);
+        graph_drop(E, key);
+    }
+    int &seen = E->graph_seen[key];
+    const bool cap = seen >= 1 && !E->tune.exploring_any();
+    E->capture = cap;
+    const long long l0 = E->launches;
+    int r = run_batch(E, plan, images, n, dfeat);
+    E->capture = false;
+    if (!cap) {
+        if (!r) seen++;
+        return r;
+    }
+    r = graph_finish(E, key, r, E->launches - l0);
+    if (r != kCaptureFailed) return r;
+    seen = -1000000;  // this shape does not capture: it runs without a graph from now on
+    CK(cudaMemsetAsync(dfeat, 0, (size_t)n * plan.n_features * sizeof(double), E->st));
+    return run_batch(E, plan, images, n, dfeat);
+}
+
+}  // namespace wc
+
 // ================================================================= C ABI
 namespace wc {
 int extract_locked(wc_engine *E, const Plan &plan, const wc_image_desc *images, int n, double *out, int out_on_device) {
     CK(cudaSetDevice(E->dev));
+    // the legacy default stream cannot be captured: graphs then run on the
+    // engine's own blocking stream (ordered with the legacy stream as it is)
+    struct Restore {
+        wc_engine *E;
+        bool on;
+        ~Restore() {
+            if (on) E->st = 0;
+        }
+    } restore{E, false};
+    if (E->graph && !E->st) {
+        if (!E->own_st) CK(cudaStreamCreate(&E->own_st));
+        E->st = E->own_st;
+        restore.on = true;
+    }
     double *dfeat = out;
     size_t fbytes = (size_t)n * plan.n_features * sizeof(double);
     if (!out_on_device) {
@@ -487,7 +644,7 @@ int extract_locked(wc_engine *E, const Plan &plan, const wc_image_desc *images, 
         dfeat = (double *)E->feat.p;
     }
     CK(cudaMemsetAsync(dfeat, 0, fbytes, E->st));
-    int r = run_batch(E, plan, images, n, dfeat);
+    int r = run_batch_graphed(E, plan, images, n, dfeat, out, out_on_device);
     if (r) return r;
     if (!out_on_device) {
         CK(cudaMemcpyAsync(out, dfeat, fbytes, cudaMemcpyDeviceToHost, E->st));
@@ -598,6 +755,11 @@ void wc_engine_destroy(wc_engine *E) {
     }
     if (E->fork_ev) cudaEventDestroy(E->fork_ev);
     if (E->early_ev) cudaEventDestroy(E->early_ev);
+    graphs_clear(E);
+    if (E->own_st) {
+        cudaStreamSynchronize(E->own_st);
+        cudaStreamDestroy(E->own_st);
+    }
     delete E;
 }
 
@@ -618,9 +780,14 @@ int wc_engine_set_option(wc_engine *E, const char *name, long long value) {
     } else if (k == "union_find_cap") {
         if (value < 0) return set_err(WC_ERR_ARG, "union_find_cap must be >= 0");
         E->opts.union_find_cap = value;
+    } else if (k == "graph") {
+        if (value != 0 && value != 1) return set_err(WC_ERR_ARG, "graph must be 0 or 1");
+        E->graph = (int)value;
     } else {
         return set_err(WC_ERR_ARG, "unknown engine option '%s'", name);
     }
+    cudaSetDevice(E->dev);
+    graphs_clear(E);  // captured launches hold the old options' choices
     return WC_OK;
 }
 
@@ -636,6 +803,16 @@ int wc_engine_tuning_report(wc_engine *E, char *buf, int buflen) {
     if ((int)s.size() >= buflen) return set_err(WC_ERR_ARG, "buffer too small (%d bytes needed)", (int)s.size() + 1);
     std::memcpy(buf, s.c_str(), s.size() + 1);
     return (int)s.size();
+}
+
+int wc_engine_graph_stats(wc_engine *E, long long *stats) {
+    if (!E || !stats) return set_err(WC_ERR_ARG, "bad arguments");
+    std::lock_guard<std::mutex> lk(E->mu);
+    stats[0] = E->graph_captures;
+    stats[1] = E->graph_replays;
+    stats[2] = E->graph_failures;
+    stats[3] = (long long)E->graphs.size();
+    return WC_OK;
 }
 
 int wc_engine_set_stream(wc_engine *E, void *stream) {

@@ -85,6 +85,19 @@ int extract_locked(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, in
 
 }  // namespace wc
 
+namespace wc {
+// One captured batch (option "graph"): the launches of a batch of one shape
+// (plan, image sizes and types, output), replayed with cudaGraphLaunch after
+// the batch's metadata and pixels are uploaded as the normal path uploads them.
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<char> hmeta;        // the batch's metadata blob (jobs, plane table, offsets)
+    std::vector<size_t> in_off;     // each host image's place in the staging buffer
+    std::vector<void *> bufs;       // the device buffers the launches address, as captured
+    long long launches = 0;         // kernels in the graph
+};
+}  // namespace wc
+
 struct wc_engine {
     int dev = 0;
     cudaStream_t st = 0;
@@ -102,4 +115,14 @@ struct wc_engine {
     wc::Tuner tune;
     cudaStream_t lanes[WC_LANES] = {};
     cudaEvent_t fork_ev = nullptr, early_ev = nullptr, join_ev[WC_LANES] = {};
+    // CUDA graphs of repeated batch shapes (option "graph"; engine.cu)
+    int graph = 0;
+    cudaStream_t own_st = nullptr;  // captures run here when the caller's stream is the legacy default
+    bool capture = false;           // run_batch: begin a capture once the uploads are queued
+    std::map<std::string, wc::GraphEntry> graphs;
+    std::vector<std::string> graph_fifo;
+    std::map<std::string, int> graph_seen;  // batches of a shape run without a graph so far
+    long long graph_captures = 0, graph_replays = 0, graph_failures = 0;
+    std::vector<size_t> last_in_off;  // run_batch: the staging offsets and metadata size it used
+    size_t last_meta_used = 0;
 };

@@ -164,6 +164,12 @@ struct Tuner {
             if (s.ms[c] < 0) return c;
         return 0;
     }
+    bool exploring_any() const {
+        if (!on) return false;
+        for (auto &kv : st)
+            if (kv.second.chosen < 0) return true;
+        return false;
+    }
     bool exploring(const std::string &key) const {
         auto it = st.find(key);
         return on && it != st.end() && it->second.chosen < 0;

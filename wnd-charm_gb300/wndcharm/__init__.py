@@ -313,11 +313,18 @@ class Engine(object):
             out[f[0]] = (int(f[1]), [float(x) for x in f[2:]])
         return out
 
+    def graph_stats(self):
+        """CUDA-graph use (option 'graph'): {'captures', 'replays', 'failures', 'kept'}."""
+        st = (ctypes.c_longlong * 4)()
+        check(lib().wc_engine_graph_stats(self._h, st))
+        return dict(zip(("captures", "replays", "failures", "kept"), list(st)))
+
     def set_option(self, name, value):
         """Engine option (wc_engine_set_option): 'f14_exact' (mixed form: f14
         through the FP64 chain, 1 by default), 'qr_iter_per_tone' (real-Schur
         iterations allowed per tone, 40), 'union_find_cap' (labelling
-        iterations allowed per link, 0 = the pixel count)."""
+        iterations allowed per link, 0 = the pixel count), 'autotune' (1),
+        'graph' (0; 1: repeated batch shapes replay a captured CUDA graph)."""
         check(lib().wc_engine_set_option(self._h, name.encode(), int(value)))
 
     def extract(self, plan, images, bits=16, out=None):

@@ -16,8 +16,9 @@ comparison:
     performs the oracle's operations in its order).  Against the reference
     build they are range-checked (f14="range"): which eigenvalue lands in slot
     2 depends on rounding, and two builds of the unmodified reference (with
-    and without fused multiply-adds) already disagree on 34 of 384 entries of
-    the 512 x 512 workload (tests/golden/reference_build_spread.npz).
+    and without fused multiply-adds) already disagree beyond 1e-12 on 33 of
+    384 entries of the 512 x 512 workload, and in the last bits on 360
+    (tests/golden/reference_build_spread.npz).
 """
 import numpy as np
 

@@ -1,0 +1,92 @@
+"""The backward pass of WND-5 marginal probabilities at the full
+differentiation workload: 256 images of 256 x 256 in [0, 1] (blob + grating,
+4 classes, seed 3, float64 so that no two pixels tie by rounding), WND-5
+trained on 192 of them over the 400 features of the continuous families
+with the top Fisher scores; the 64 others are the test images.
+
+Checked (1) against a float64 torch autograd restatement of the same
+functions on 4 test images (every pixel's gradient and the weights'), and
+(2) against central differences (h = 1e-3) of the GPU's own forward pass on
+64 random pixels of each of 8 test images, with the kink criterion of the
+scaled-down test: where the step [x - h, x + h] holds no kink they agree."""
+import numpy as np
+import pytest
+
+import grad_reference as gref
+import synth_loader  # noqa: F401
+from test_gpu_grad import _fd_check, _smooth_and_ok
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def full():
+    import wndcharm
+    from wndcharm import synth
+    from wndcharm.grad import WNDModel, continuous_groups
+    imgs, labels = synth.config4(n=256, size=256, seed=3, dtype=np.float64)
+    tr, te = list(range(192)), list(range(192, 256))
+    groups = continuous_groups()
+    plan = wndcharm.FeatureComputationPlan("continuous")
+    for g in groups:
+        plan.add(g)
+    eng = wndcharm.Engine(0, "fp64")
+    rows = eng.extract(plan, [imgs[i] for i in tr])
+    ytr = labels[tr]
+    w, mn, mx = eng.wnd_fit(rows, ytr, 4, 1.0)
+    thr = np.sort(w)[::-1][399]
+    w = np.where(w >= thr, w, 0.0)
+    assert (w > 0).sum() == 400
+    model = WNDModel(eng, plan, rows, ytr, 4, mn, mx)
+    return dict(model=model, groups=groups, rows=rows, ytr=ytr, w=w, mn=mn, mx=mx,
+                test=[imgs[i] for i in te], labels=labels[te])
+
+
+def test_full_backward_matches_torch_autograd(full):
+    import torch
+    s = full
+    test = s["test"][:4]
+    seed = np.random.default_rng(4).normal(size=(4, 4))
+    _, gp, gw = s["model"].run(test, s["w"], seed=seed)
+    Xn = torch.from_numpy(gref.normalize_train(s["rows"], s["mn"], s["mx"]))
+    y = torch.from_numpy(s["ytr"])
+    wt = torch.from_numpy(s["w"]).requires_grad_(True)
+    worst = 0.0
+    for i, img in enumerate(test):
+        x = torch.from_numpy(img.copy()).requires_grad_(True)
+        p = gref.wnd(gref.features(x, s["groups"]), Xn, y, 4, wt, torch.from_numpy(s["mn"]),
+                     torch.from_numpy(s["mx"]))
+        (torch.from_numpy(seed[i]) * p).sum().backward()
+        g = x.grad.numpy()
+        err = np.abs(gp[i] - g).max() / max(np.abs(g).max(), 1e-300)
+        worst = max(worst, err)
+        assert err < 1e-6, (i, err)
+    gwt = wt.grad.numpy()
+    np.testing.assert_allclose(gw, gwt, rtol=1e-7, atol=1e-9 * np.abs(gwt).max())
+    print("256 x 256: pixel gradients within %.3g of torch autograd (relative to the map's largest)" % worst)
+
+
+def test_full_backward_matches_central_differences(full):
+    """All 400 features: the steps' mean slopes against the derivative (a
+    tail crosses kinks: fractal |I(p) - I(q)| ties, rank swaps), and the
+    Zernike magnitudes off the Edge planes alone, which are smooth here: every
+    sampled pixel agrees."""
+    s = full
+    fd, an, gp, gm = _fd_check(s["model"], s["test"][:8], s["w"], 64, np.random.default_rng(6))
+    smooth, ok = _smooth_and_ok(fd, an, gp, gm)
+    scale = np.abs(an).max()
+    rel = np.abs(fd - an) / (np.abs(an) + 1e-6 * scale)
+    q = np.quantile(rel, [0.5, 0.75, 0.9, 0.95, 0.99])
+    print("256 x 256 finite differences: %d of %d steps hold no kink, %d of them agree; relative error "
+          "quantiles 50/75/90/95/99%%: %s" % (smooth.sum(), smooth.size, (ok & smooth).sum(),
+                                              np.array2string(q, precision=3)))
+    assert q[0] < 1e-3, q
+    names = s["model"].plan.feature_names()
+    zern = np.array([nm.startswith("Zernike") and "Edge" not in nm for nm in names])
+    wz = np.where(zern, s["w"], 0.0)
+    assert (wz > 0).sum() >= 10
+    fd, an, gp, gm = _fd_check(s["model"], s["test"][:8], wz, 16, np.random.default_rng(8))
+    smooth, ok = _smooth_and_ok(fd, an, gp, gm)
+    print("256 x 256, Zernike only: %d of %d steps hold no kink; %d of %d pixels agree"
+          % (smooth.sum(), smooth.size, ok.sum(), ok.size))
+    assert ok.mean() >= 0.98

@@ -44,13 +44,25 @@ def full():
 
 def test_full_backward_matches_torch_autograd(full):
     import torch
+    from wndcharm.grad import class_evidence_maps
     s = full
-    test = s["test"][:4]
+    # an image classified with a probability within ~1e-15 of 1 has
+    # gradients below the forward pass's own rounding (every class's map is
+    # then a difference of nearly equal terms): the check takes the 4 test
+    # images the classifier is least sure of
+    probs, _, _ = s["model"].run(s["test"], s["w"])
+    pick = np.argsort(probs.max(1))[:4]
+    print("checked images' largest probabilities:", probs.max(1)[pick])
+    test = [s["test"][i] for i in pick]
     seed = np.random.default_rng(4).normal(size=(4, 4))
     _, gp, gw = s["model"].run(test, s["w"], seed=seed)
     Xn = torch.from_numpy(gref.normalize_train(s["rows"], s["mn"], s["mx"]))
     y = torch.from_numpy(s["ytr"])
     wt = torch.from_numpy(s["w"]).requires_grad_(True)
+    # the seeded sum mixes the classes' maps, which cancel where one class's
+    # probability is near 1 (the maps sum to zero): errors are measured
+    # against the largest contributing class map
+    maps = class_evidence_maps(s["model"], test, s["w"])
     worst = 0.0
     for i, img in enumerate(test):
         x = torch.from_numpy(img.copy()).requires_grad_(True)
@@ -58,12 +70,13 @@ def test_full_backward_matches_torch_autograd(full):
                      torch.from_numpy(s["mx"]))
         (torch.from_numpy(seed[i]) * p).sum().backward()
         g = x.grad.numpy()
-        err = np.abs(gp[i] - g).max() / max(np.abs(g).max(), 1e-300)
+        scale = max((np.abs(seed[i, c]) * np.abs(maps[i, c]).max() for c in range(4)))
+        err = np.abs(gp[i] - g).max() / max(scale, 1e-300)
         worst = max(worst, err)
-        assert err < 1e-6, (i, err)
+        assert err < 1e-7, (i, err, np.abs(g).max() / scale)
     gwt = wt.grad.numpy()
     np.testing.assert_allclose(gw, gwt, rtol=1e-7, atol=1e-9 * np.abs(gwt).max())
-    print("256 x 256: pixel gradients within %.3g of torch autograd (relative to the map's largest)" % worst)
+    print("256 x 256: pixel gradients within %.3g of torch autograd (relative to the largest class map)" % worst)
 
 
 def test_full_backward_matches_central_differences(full):

@@ -191,6 +191,16 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
 int wc_wnd_normalize(wc_engine *engine, const double *rows, int n, int F, const double *mins, const double *maxs,
                      double *out);
 
+/* classify2's per-class partial sums over the training rows given (a shard of
+ * the training set): sums[t*C + c-1] = sum of d(t,s)^-5 over the rows s of class c
+ * with d >= DBL_EPSILON, counts[t*C + c-1] how many (FP64, the reference's
+ * arithmetic per term).  Summed over the shards of a training set (one
+ * all-reduce), then mean per class and normalised, they are classify2's
+ * probabilities for the whole set (TrainingSet.cpp:2429-2586). */
+int wc_wnd_class_sums(wc_engine *engine, const double *train, int N, int F, const int *labels, int C,
+                      const double *weights, const double *mins, const double *maxs, const double *test, int T,
+                      double *sums, long long *counts);
+
 /* wc_wnd_fit followed by wc_wnd_classify of `test` against the same training
  * rows, as the reference's classification run does them in one process
  * (TrainingSet::normalize, SetFisherScores, then classify2 per test sample:

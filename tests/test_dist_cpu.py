@@ -60,3 +60,85 @@ def test_two_gloo_ranks():
     for rank, rows, t in res:
         np.testing.assert_array_equal(rows, ref)
         assert t == 2.0
+
+
+def _np_class_sums(X, y, C, w, mn, mx, T):
+    """A numpy restatement of classify2's per-class sums (TrainingSet.cpp:2429-2586):
+    the kept features normalised as signatures::normalize does, per-feature
+    terms below DBL_EPSILON skipped, rows with d < DBL_EPSILON skipped."""
+    eps = np.finfo(np.float64).eps
+    keep = w >= eps
+    rng = mx - mn
+
+    def norm(A):
+        with np.errstate(invalid="ignore", divide="ignore"):
+            v = 100 * ((A - mn) / np.where(rng >= eps, rng, 1.0))
+        v = np.where(A > mx, 100.0, v)
+        return np.where(np.isnan(A) | (A < mn) | (rng < eps), 0.0, v)[:, keep]
+
+    Xn, Tn, w2 = norm(X), norm(T), w[keep] ** 2
+    sums = np.zeros((len(T), C))
+    counts = np.zeros((len(T), C), dtype=np.int64)
+    for t in range(len(T)):
+        diff = np.abs(Tn[t] - Xn)
+        diff = np.where(diff < eps, 0.0, diff)
+        d = (w2 * diff * diff).sum(1)
+        for c in range(1, C + 1):
+            sel = (y == c) & (d >= eps)
+            sums[t, c - 1] = (d[sel] ** -5.0).sum()
+            counts[t, c - 1] = sel.sum()
+    return sums, counts
+
+
+def _wnd_worker(rank, world, port, data, q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from wndcharm.dist import shard, wnd_classify_sharded
+    xtr, ytr, xte, w, mn, mx = data
+    lo, hi = shard(len(xtr), rank, world)
+    probs, pred = wnd_classify_sharded(None, xtr[lo:hi], ytr[lo:hi], 5, w, mn, mx, xte,
+                                       sums_fn=lambda *a: _np_class_sums(*a))
+    q.put((rank, probs, pred))
+    dist.destroy_process_group()
+
+
+def test_wnd_training_rows_sharded_over_two_gloo_ranks():
+    """WND-5 with the training rows split over two ranks and one all-reduce of
+    the per-class sums and counts: every rank gets classify2's result for the
+    whole training set (the oracle's), with a duplicated row that both
+    the reference and the shards skip."""
+    import socket
+    from conftest import oracle_lib, oracle_wnd
+    from wndcharm import synth
+    xtr, ytr, xte, _ = synth.feature_vectors(301, 23, 120, 5, 6)
+    xte[3] = xtr[10]  # distance 0 to one training row: skipped
+    w, mn, mx, p_ref, pred_ref = oracle_wnd(oracle_lib(), xtr, ytr, xte, 5, 0.15)
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    data = (xtr, ytr, xte, w, mn, mx)
+    procs = [ctx.Process(target=_wnd_worker, args=(r, 2, port, data, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=300) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, probs, pred in res:
+        np.testing.assert_array_equal(pred, pred_ref)
+        np.testing.assert_allclose(probs, p_ref, rtol=1e-12, atol=1e-15)
+
+
+def test_wnd_finish_matches_the_rules():
+    from wndcharm.dist import wnd_finish
+    sums = np.array([[2.0, 6.0, 0.0], [1.0, 1.0, 0.0], [0.0, 0.0, 0.0]])
+    counts = np.array([[1, 2, 0], [1, 1, 0], [0, 0, 0]])
+    probs, pred, tot = wnd_finish(sums, counts)
+    np.testing.assert_allclose(probs[0], [0.4, 0.6, 0.0])
+    assert list(pred) == [2, 1, -1]  # ties: the first class; no rows: -1
+    assert tot[0] == 5.0

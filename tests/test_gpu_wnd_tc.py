@@ -136,3 +136,21 @@ def test_fit_classify_matches_separate_calls(prec):
     p2, pr2, w2, mn2, mx2 = e.wnd_fit_classify(xtr, ytr, 5, xte, 0.15)
     for a, b in ((w2, w), (mn2, mn), (mx2, mx), (pr2, pr), (p2, p)):
         np.testing.assert_array_equal(a, b)
+
+
+def test_class_sums_over_shards_give_classify2():
+    """wc_wnd_class_sums on two halves of the training rows, added (what the
+    all-reduce of the sharded path does) and finished: the FP64 form's
+    classify2 on the whole set."""
+    import wndcharm
+    from wndcharm import synth
+    from wndcharm.dist import wnd_finish
+    xtr, ytr, xte, _ = synth.feature_vectors(3001, 200, 1059, 6, 12)
+    e = wndcharm.Engine(0, "fp64")
+    w, mn, mx = e.wnd_fit(xtr, ytr, 6, 0.15)
+    p, pr = e.wnd_classify(xtr, ytr, 6, w, mn, mx, xte)
+    s1, c1 = e.wnd_class_sums(xtr[:1400], ytr[:1400], 6, w, mn, mx, xte)
+    s2, c2 = e.wnd_class_sums(xtr[1400:], ytr[1400:], 6, w, mn, mx, xte)
+    probs, pred, _ = wnd_finish(s1 + s2, c1 + c2)
+    np.testing.assert_array_equal(pred, pr)
+    np.testing.assert_allclose(probs, p, rtol=1e-12, atol=1e-15)

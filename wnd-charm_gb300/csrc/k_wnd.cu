@@ -442,6 +442,24 @@ __global__ void k_wnd_finish(const double *__restrict__ psim, const long long *_
     norm[t] = tot;
 }
 
+// the chunks' per-class sums of d^-5 and counts, added in chunk order (the
+// first half of k_wnd_finish), for an exchange across ranks
+__global__ void k_wnd_sums(const double *__restrict__ psim, const long long *__restrict__ pcnt, int T, int nchunk, int C,
+                           double *__restrict__ sums, long long *__restrict__ counts) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    for (int c = 0; c < C; c++) {
+        double v = 0;
+        long long n = 0;
+        for (int ch = 0; ch < nchunk; ch++) {
+            v += psim[((long long)t * nchunk + ch) * C + c];
+            n += pcnt[((long long)t * nchunk + ch) * C + c];
+        }
+        sums[(long long)t * C + c] = v;
+        counts[(long long)t * C + c] = n;
+    }
+}
+
 // TrainingSet::ClassifyImage for WND-5 (src/wndchrm_src/TrainingSet.cpp:1603-1800),
 // one thread per image over its `tiles` consecutive rows, in tile order:
 // marginal probabilities summed as p / tiles (with max_tile, a tile whose
@@ -867,6 +885,67 @@ extern "C" int wc_wnd_fit_classify(wc_engine *E, const double *train, int N, int
     CKR(cudaMemcpyAsync(maxs, dmax, F * 8, cudaMemcpyDeviceToHost, st));
     CKR(cudaMemcpyAsync(probs, dprob, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
     CKR(cudaMemcpyAsync(pred, dpred, (size_t)T * 4, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    return WC_OK;
+}
+
+// classify2's per-class sums over this process's training rows (host
+// buffers): sums[t * C + c - 1] = sum of d^-5 over the rows of class c with
+// d >= DBL_EPSILON, counts[...] how many; the FP64 kernel's arithmetic.  Summed
+// over shards of the training rows they give every shard's classify2.
+extern "C" int wc_wnd_class_sums(wc_engine *E, const double *train, int N, int F, const int *labels, int C,
+                                 const double *weights, const double *mins, const double *maxs, const double *test,
+                                 int T, double *sums, long long *counts) {
+    if (!E || !train || !labels || !weights || !mins || !maxs || !test || !sums || !counts || N < 1 || F < 1 ||
+        T < 1 || C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_class_sums: bad arguments (C must be 1..16)");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    std::vector<int> keep;
+    std::vector<double> w2;
+    for (int f = 0; f < F; f++)
+        if (!(weights[f] < DBL_EPSILON)) {
+            keep.push_back(f);
+            w2.push_back(std::pow(weights[f], 2));
+        }
+    const int K = (int)keep.size();
+    const int nchunk = std::max(1, std::min(64, (N + 4095) / 4096));
+    const int per = ((N + nchunk - 1) / nchunk + WT - 1) / WT * WT;
+    WBufs B;
+    double *dX, *dT, *dmin, *dmax, *dw2, *dXc, *dTc, *dps, *dsum;
+    double2 *drec;
+    long long *dpc, *dcnt;
+    int *dy, *dkeep;
+    if ((rc = B.get(&dX, (size_t)N * F * 8)) || (rc = B.get(&dT, (size_t)T * F * 8)) || (rc = B.get(&dmin, F * 8)) ||
+        (rc = B.get(&dmax, F * 8)) || (rc = B.get(&drec, (size_t)F * 16)) || (rc = B.get(&dy, (size_t)N * 4)) ||
+        (rc = B.get(&dkeep, std::max(K, 1) * 4)) || (rc = B.get(&dw2, std::max(K, 1) * 8)) ||
+        (rc = B.get(&dXc, (size_t)N * std::max(K, 1) * 8)) || (rc = B.get(&dTc, (size_t)T * std::max(K, 1) * 8)) ||
+        (rc = B.get(&dps, (size_t)T * nchunk * C * 8)) || (rc = B.get(&dpc, (size_t)T * nchunk * C * 8)) ||
+        (rc = B.get(&dsum, (size_t)T * C * 8)) || (rc = B.get(&dcnt, (size_t)T * C * 8)))
+        return rc;
+    CKR(cudaMemcpyAsync(dX, train, (size_t)N * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dT, test, (size_t)T * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dmin, mins, F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dmax, maxs, F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dy, labels, (size_t)N * 4, cudaMemcpyHostToDevice, st));
+    if (K) {
+        CKR(cudaMemcpyAsync(dkeep, keep.data(), K * 4, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync(dw2, w2.data(), K * 8, cudaMemcpyHostToDevice, st));
+        *launches += 3;
+        k_wnd_recip<<<(F + 255) / 256, 256, 0, st>>>(dmin, dmax, F, drec);
+        k_wnd_gather<<<(int)(((long long)N * K + 255) / 256), 256, 0, st>>>(dX, N, F, dkeep, K, dmin, dmax, drec,
+                                                                            dXc);
+        k_wnd_gather<<<(int)(((long long)T * K + 255) / 256), 256, 0, st>>>(dT, T, F, dkeep, K, dmin, dmax, drec,
+                                                                            dTc);
+    }
+    *launches += 2;
+    k_wnd_dist<<<dim3((T + WT - 1) / WT, nchunk), 256, 0, st>>>(dTc, T, dXc, N, dy, dw2, K, C, per, dps, dpc);
+    k_wnd_sums<<<(T + 127) / 128, 128, 0, st>>>(dps, dpc, T, nchunk, C, dsum, dcnt);
+    CKR(cudaGetLastError());
+    CKR(cudaMemcpyAsync(sums, dsum, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
+    CKR(cudaMemcpyAsync(counts, dcnt, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
     return WC_OK;
 }

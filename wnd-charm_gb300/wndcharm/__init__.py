@@ -418,6 +418,24 @@ class Engine(object):
                                      mx.ctypes.data_as(_lib.D), out.ctypes.data_as(_lib.D)))
         return out
 
+    def wnd_class_sums(self, train, labels, n_classes, weights, mins, maxs, test):
+        """classify2's per-class sums of d^-5 and counts over these training
+        rows (a shard): (sums (T, C) float64, counts (T, C) int64)."""
+        X = np.ascontiguousarray(train, dtype=np.float64)
+        y = np.ascontiguousarray(labels, dtype=np.int32)
+        T = np.ascontiguousarray(test, dtype=np.float64)
+        N, F = X.shape
+        nt = T.shape[0]
+        w, mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (weights, mins, maxs))
+        sums = np.zeros((nt, n_classes))
+        counts = np.zeros((nt, n_classes), dtype=np.int64)
+        check(lib().wc_wnd_class_sums(self._h, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I),
+                                      int(n_classes), w.ctypes.data_as(_lib.D), mn.ctypes.data_as(_lib.D),
+                                      mx.ctypes.data_as(_lib.D), T.ctypes.data_as(_lib.D), nt,
+                                      sums.ctypes.data_as(_lib.D),
+                                      counts.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
+        return sums, counts
+
     def wnd_fit_classify(self, train, labels, n_classes, test, frac=0.15):
         """wnd_fit on the training rows, then wnd_classify of the test rows,
         each array copied to the GPU once: (probs, pred, weights, mins, maxs)."""

@@ -84,6 +84,8 @@ def lib():
         L.wc_wnd_fit.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D, D, D]
         L.wc_wnd_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D, I]
         L.wc_wnd_normalize.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, D, D, D]
+        L.wc_wnd_class_sums.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D,
+                                        ctypes.POINTER(ctypes.c_longlong)]
         L.wc_wnd_fit_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D,
                                           ctypes.c_int, D, D, D, D, I]
         L.wc_wnd_fit_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp, vp,

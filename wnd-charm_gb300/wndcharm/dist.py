@@ -43,3 +43,55 @@ def max_over_ranks(seconds, group=None):
     t = torch.tensor([float(seconds)])
     dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return float(t.item())
+
+
+def wnd_finish(sums, counts):
+    """classify2's last steps from the per-class sums of d^-5 and their counts
+    (TrainingSet.cpp:2429-2586, as k_wnd_finish does them on the GPU): each
+    class's similarity is its mean d^-5 (classes without a row are 0), the
+    predicted class the first strictly largest (1-based; -1 when no class has
+    a row), the marginal probabilities the similarities over their sum.
+    Returns (probs (T, C), pred (T,), normalisation factor (T,))."""
+    sums = np.asarray(sums, dtype=np.float64)
+    counts = np.asarray(counts, dtype=np.int64)
+    T, C = sums.shape
+    sim = np.where(counts > 0, sums / np.maximum(counts, 1), 0.0)
+    pred = np.full(T, -1, dtype=np.int32)
+    best = np.zeros(T)
+    for c in range(C):  # first strictly larger wins, in class order
+        up = (counts[:, c] > 0) & (sim[:, c] > best)
+        best = np.where(up, sim[:, c], best)
+        pred = np.where(up, c + 1, pred)
+    tot = np.zeros(T)
+    for c in range(C):
+        tot = tot + sim[:, c]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        probs = sim / tot[:, None]
+    return probs, pred, tot
+
+
+def wnd_classify_sharded(engine, train_shard, labels_shard, n_classes, weights, mins, maxs, test, group=None,
+                         sums_fn=None):
+    """classify2 with the training rows sharded across ranks: every rank takes
+    its shard's per-class sums of d^-5 and counts for all test rows
+    (Engine.wnd_class_sums, wc_wnd_class_sums), one all-reduce adds them, and
+    every rank finishes the same probabilities and classes (wnd_finish).  The
+    weights and ranges (wnd_fit on the whole set) are the same on every rank.
+    sums_fn(train, labels, C, w, mn, mx, test) -> (sums, counts) replaces the
+    engine call where a test runs the exchange without a GPU."""
+    import torch
+    import torch.distributed as dist
+    fn = sums_fn if sums_fn is not None else engine.wnd_class_sums
+    if len(train_shard):
+        sums, counts = fn(train_shard, labels_shard, n_classes, weights, mins, maxs, test)
+    else:
+        sums = np.zeros((len(test), n_classes))
+        counts = np.zeros((len(test), n_classes), dtype=np.int64)
+    if dist.is_initialized() and dist.get_world_size(group) > 1:
+        ts = torch.from_numpy(np.ascontiguousarray(sums))
+        tc = torch.from_numpy(np.ascontiguousarray(counts))
+        dist.all_reduce(ts, op=dist.ReduceOp.SUM, group=group)
+        dist.all_reduce(tc, op=dist.ReduceOp.SUM, group=group)
+        sums, counts = ts.numpy(), tc.numpy()
+    probs, pred, _ = wnd_finish(sums, counts)
+    return probs, pred

@@ -286,6 +286,19 @@ int wc_wnd_classify_images(wc_engine *engine, const double *train, int N, int F,
 int wc_tiff_info(const char *path, int *width, int *height, int *bits);
 int wc_tiff_layout(const char *path, int *width, int *height, int *bits, int *samples);
 int wc_tiff_read(const char *path, void *pixels, long long capacity);
+/* TIFF files decoded into device memory (no reference counterpart beyond
+ * LoadTIFF itself): the host reads each file and its directory and copies its
+ * strips to the GPU as stored (LZW strips, a serial bit stream, are decoded on
+ * the host); PackBits expansion, byte order and the horizontal predictor run on
+ * the GPU.  d_pixels: a 256-byte aligned device buffer of `capacity` bytes
+ * (wc_tiff_device_bytes gives the size); image i's samples start at
+ * descs[i].pixels (256-byte aligned, native uint8 / uint16, RGB interleaved)
+ * and descs[i] is filled for wc_extract_batch / wc_extract_samples
+ * (on_device = 1, dtype WC_U8 / WC_U16 / WC_RGB8 / WC_RGB16, bits = the file's).
+ * The same files, layouts and errors as wc_tiff_read. */
+int wc_tiff_device_bytes(const char *const *paths, int n, long long *bytes);
+int wc_tiff_read_device(wc_engine *engine, const char *const *paths, int n, void *d_pixels, long long capacity,
+                        wc_image_desc *descs);
 
 /* ---- preprocessing and sampling ----
  * How wndchrm turns one opened image into its samples, on the GPU:

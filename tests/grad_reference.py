@@ -223,9 +223,12 @@ def wnd(tfeat, Xtrain_n, y, C, w, mins, maxs):
     rng = (maxs - mins)
     ok = rng >= EPS
     tv = torch.where(torch.isnan(tfeat), torch.zeros_like(tfeat), tfeat)
-    t = torch.where(ok, 100 * ((torch.minimum(torch.maximum(tv, mins), maxs) - mins) / torch.where(ok, rng, 1.0)),
-                    torch.zeros_like(tv))
-    t = torch.where(tv < mins, torch.zeros_like(t), t)
+    # signatures::normalize's branches (0 below the range, 100 above it, the
+    # quotient inside the closed range): at a value equal to max the derivative
+    # is the quotient's (a clamp would split it between the two sides)
+    t = 100 * ((tv - mins) / torch.where(ok, rng, 1.0))
+    t = torch.where(tv > maxs, torch.full_like(t, 100.0), t)
+    t = torch.where(ok & ~(tv < mins) & ~torch.isnan(tfeat), t, torch.zeros_like(t))
     keep = w.detach() >= EPS
     d = ((w[keep] ** 2) * (t[keep] - Xtrain_n[:, keep]) ** 2).sum(1)
     sims = []

@@ -80,26 +80,38 @@ def test_full_backward_matches_torch_autograd(full):
 
 
 def test_full_backward_matches_central_differences(full):
-    """All 400 features: the steps' mean slopes against the derivative (a
-    tail crosses kinks: fractal |I(p) - I(q)| ties, rank swaps), and the
-    Zernike magnitudes off the Edge planes alone, which are smooth here: every
-    sampled pixel agrees."""
+    """Central differences of the GPU's forward pass on 64 random pixels of
+    each of 8 test images, all 400 features.  At this size the pixels' values
+    lie ~1e-5 apart, so a step of h = 1e-3 crosses kinks (order statistics
+    change rank, fractal |I(p) - I(q)| change sign) on most pixels; those
+    statistics are reported.  With h = 1e-6 few steps cross one, and the
+    quotients agree with the derivative up to the forward pass's rounding.  The Zernike magnitudes off the
+    Edge planes are smooth at any h: every sampled pixel agrees at h = 1e-3."""
     s = full
-    fd, an, gp, gm = _fd_check(s["model"], s["test"][:8], s["w"], 64, np.random.default_rng(6))
+    rng_pix = np.random.default_rng(6)
+    fd, an, gp, gm = _fd_check(s["model"], s["test"][:8], s["w"], 64, rng_pix)
     smooth, ok = _smooth_and_ok(fd, an, gp, gm)
     scale = np.abs(an).max()
     rel = np.abs(fd - an) / (np.abs(an) + 1e-6 * scale)
+    print("256 x 256, h = 1e-3: %d of %d steps hold no kink, %d of them agree; relative error quantiles "
+          "50/75/90/95/99%%: %s" % (smooth.sum(), smooth.size, (ok & smooth).sum(),
+                                    np.array2string(np.quantile(rel, [0.5, 0.75, 0.9, 0.95, 0.99]), precision=3)))
+    fd, an, gp, gm = _fd_check(s["model"], s["test"][:8], s["w"], 64, np.random.default_rng(6), h=1e-6)
+    rel = np.abs(fd - an) / (np.abs(an) + 1e-6 * np.abs(an).max())
     q = np.quantile(rel, [0.5, 0.75, 0.9, 0.95, 0.99])
-    print("256 x 256 finite differences: %d of %d steps hold no kink, %d of them agree; relative error "
-          "quantiles 50/75/90/95/99%%: %s" % (smooth.sum(), smooth.size, (ok & smooth).sum(),
-                                              np.array2string(q, precision=3)))
-    assert q[0] < 1e-3, q
+    print("256 x 256, h = 1e-6: relative error quantiles 50/75/90/95/99%%: %s; within 1e-3: %d of %d"
+          % (np.array2string(q, precision=3), (rel < 1e-3).sum(), rel.size))
+    # measured: the quotient's error grows with h on both sides of 1e-6 (rank
+    # crossings of the Gini and order statistics over 65,536 pixels above it,
+    # the forward pass's rounding over 2h below it); half the pixels agree to
+    # ~1e-5, three quarters to ~1e-4
+    assert q[0] < 1e-4 and q[1] < 1e-3, q
     names = s["model"].plan.feature_names()
     zern = np.array([nm.startswith("Zernike") and "Edge" not in nm for nm in names])
     wz = np.where(zern, s["w"], 0.0)
     assert (wz > 0).sum() >= 10
     fd, an, gp, gm = _fd_check(s["model"], s["test"][:8], wz, 16, np.random.default_rng(8))
     smooth, ok = _smooth_and_ok(fd, an, gp, gm)
-    print("256 x 256, Zernike only: %d of %d steps hold no kink; %d of %d pixels agree"
+    print("256 x 256, Zernike only, h = 1e-3: %d of %d steps hold no kink; %d of %d pixels agree"
           % (smooth.sum(), smooth.size, ok.sum(), ok.size))
     assert ok.mean() >= 0.98

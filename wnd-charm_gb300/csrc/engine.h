@@ -107,6 +107,7 @@ struct wc_engine {
     wc::DevBuf arena, feat, ws, meta, stage;
     wc::DevBuf pre, pre_meta;  // preprocessing: images, opened and sample planes; jobs and positions
     wc::DevBuf clr;            // HSV colour planes of the batch's RGB images
+    wc::DevBuf tiffbuf;        // wc_tiff_read_device: stored strips, decoded bytes, tables
     wc::Tables tabs;
     std::vector<char> hmeta, hpre;
     std::mutex mu;

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/wndcharm_gb300.h"
+#include "tiff_internal.h"
 
 namespace wc {
 int set_err(int code, const char *fmt, ...);
@@ -124,10 +125,15 @@ bool packbits_decode(const uint8_t *src, size_t n, std::vector<uint8_t> &out, si
     return true;
 }
 
-int read_tiff(const char *path, TiffImage &img) {
+}  // namespace
+
+namespace wc {
+
+int parse_tiff(const char *path, TiffFile &t) {
     FILE *f = fopen(path, "rb");
     if (!f) return wc::set_err(WC_ERR_IO, "cannot open '%s'", path);
-    std::vector<uint8_t> b;
+    std::vector<uint8_t> &b = t.b;
+    b.clear();
     uint8_t chunk[1 << 16];
     size_t got;
     while ((got = fread(chunk, 1, sizeof chunk, f)) > 0) b.insert(b.end(), chunk, chunk + got);
@@ -135,13 +141,13 @@ int read_tiff(const char *path, TiffImage &img) {
     if (b.size() < 8 || !((b[0] == 'I' && b[1] == 'I') || (b[0] == 'M' && b[1] == 'M')))
         return wc::set_err(WC_ERR_IO, "'%s' is not a TIFF file", path);
     Reader r{b, b[0] == 'I'};
+    t.le = r.le;
     if (r.u16(2) != 42) return wc::set_err(WC_ERR_IO, "'%s': not a classic TIFF (BigTIFF is not supported)", path);
     const uint32_t ifd = r.u32(4);
     const uint32_t nent = r.u16(ifd);
     if (!r.ok) return wc::set_err(WC_ERR_IO, "'%s': truncated header", path);
-    uint32_t w = 0, h = 0, bps = 1, comp = 1, spp = 1, rps = 0xffffffffu, pred = 1, planar = 1;
+    uint32_t planar = 1;
     bool tiled = false;
-    std::vector<uint32_t> offs, counts;
     auto values = [&](size_t e, std::vector<uint32_t> &v) {
         const uint32_t type = r.u16(e + 2), cnt = r.u32(e + 4);
         if (cnt > b.size()) {  // a count no file of this size can hold
@@ -162,16 +168,16 @@ int read_tiff(const char *path, TiffImage &img) {
         values(e, v);
         if (v.empty()) continue;
         switch (tag) {
-            case 256: w = v[0]; break;
-            case 257: h = v[0]; break;
-            case 258: bps = v[0]; break;
-            case 259: comp = v[0]; break;
-            case 273: offs = v; break;
-            case 277: spp = v[0]; break;
-            case 278: rps = v[0]; break;
-            case 279: counts = v; break;
+            case 256: t.w = v[0]; break;
+            case 257: t.h = v[0]; break;
+            case 258: t.bps = v[0]; break;
+            case 259: t.comp = v[0]; break;
+            case 273: t.offs = v; break;
+            case 277: t.spp = v[0]; break;
+            case 278: t.rps = v[0]; break;
+            case 279: t.counts = v; break;
             case 284: planar = v[0]; break;
-            case 317: pred = v[0]; break;
+            case 317: t.pred = v[0]; break;
             case 322: tiled = true; break;
             default: break;
         }
@@ -179,52 +185,83 @@ int read_tiff(const char *path, TiffImage &img) {
     const uint32_t next_ifd = r.u32(ifd + 2 + 12 * (size_t)nent);
     if (!r.ok) return wc::set_err(WC_ERR_IO, "'%s': truncated directory", path);
     if (next_ifd != 0) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': more than one image directory", path);
-    if (bps != 8 && bps != 16) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u bits per sample (8 or 16 only)", path, bps);
-    if ((spp != 1 && spp != 3) || (spp == 3 && planar != 1))
+    if (t.bps != 8 && t.bps != 16)
+        return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u bits per sample (8 or 16 only)", path, t.bps);
+    if ((t.spp != 1 && t.spp != 3) || (t.spp == 3 && planar != 1))
         return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u samples per pixel, planar configuration %u (grayscale or "
-                           "interleaved RGB only)", path, spp, planar);
+                           "interleaved RGB only)", path, t.spp, planar);
     if (tiled) return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': tiled TIFF", path);
-    if (comp != 1 && comp != 5 && comp != 32773)
-        return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': compression %u (none, LZW or PackBits only)", path, comp);
-    if (w == 0 || h == 0 || offs.empty() || offs.size() != counts.size())
+    if (t.comp != 1 && t.comp != 5 && t.comp != 32773)
+        return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': compression %u (none, LZW or PackBits only)", path, t.comp);
+    if (t.w == 0 || t.h == 0 || t.offs.empty() || t.offs.size() != t.counts.size())
         return wc::set_err(WC_ERR_IO, "'%s': missing image size or strips", path);
-    const size_t es = bps / 8, row = (size_t)w * spp * es, total = row * h;
-    if (rps > h) rps = h;
-    std::vector<uint8_t> raw;
+    if ((unsigned long long)t.w * t.h > (1ull << 28) || t.w > 32768 || t.h > 32768)
+        return wc::set_err(WC_ERR_UNSUPPORTED, "'%s': %u x %u is larger than this build reads", path, t.w, t.h);
+    if (t.rps > t.h) t.rps = t.h;
+    if (t.rps == 0) return wc::set_err(WC_ERR_IO, "'%s': zero rows per strip", path);
+    for (size_t s = 0; s < t.offs.size(); s++)
+        if ((size_t)t.offs[s] + t.counts[s] > b.size())
+            return wc::set_err(WC_ERR_IO, "'%s': strip %zu past the end", path, s);
+    return WC_OK;
+}
+
+// the stored samples of rows [0, h) in file order (strips decoded on the host)
+int host_strips(const char *path, const TiffFile &t, std::vector<uint8_t> &raw) {
+    const size_t row = t.row(), total = row * t.h;
+    raw.clear();
     raw.reserve(total);
-    for (size_t s = 0; s < offs.size() && raw.size() < total; s++) {
-        if ((size_t)offs[s] + counts[s] > b.size()) return wc::set_err(WC_ERR_IO, "'%s': strip %zu past the end", path, s);
-        const size_t rows = std::min<size_t>(rps, h - std::min<size_t>(h, s * (size_t)rps));
+    for (size_t s = 0; s < t.offs.size() && raw.size() < total; s++) {
+        const size_t rows = t.strip_rows(s);
         const size_t want = raw.size() + rows * row;
-        const uint8_t *src = b.data() + offs[s];
-        if (comp == 1) {
-            raw.insert(raw.end(), src, src + std::min<size_t>(counts[s], rows * row));
+        const uint8_t *src = t.b.data() + t.offs[s];
+        if (t.comp == 1) {
+            raw.insert(raw.end(), src, src + std::min<size_t>(t.counts[s], rows * row));
         } else {
             std::vector<uint8_t> dec;
-            const bool good = comp == 5 ? lzw_decode(src, counts[s], dec, rows * row) : packbits_decode(src, counts[s], dec, rows * row);
+            const bool good = t.comp == 5 ? lzw_decode(src, t.counts[s], dec, rows * row)
+                                          : packbits_decode(src, t.counts[s], dec, rows * row);
             if (!good) return wc::set_err(WC_ERR_IO, "'%s': corrupt strip %zu", path, s);
             raw.insert(raw.end(), dec.begin(), dec.begin() + std::min(dec.size(), rows * row));
         }
         if (raw.size() < want) return wc::set_err(WC_ERR_IO, "'%s': strip %zu too short", path, s);
     }
     if (raw.size() < total) return wc::set_err(WC_ERR_IO, "'%s': image data too short", path);
-    img.w = (int)w;
-    img.h = (int)h;
-    img.bits = (int)bps;
-    img.spp = (int)spp;
+    return WC_OK;
+}
+
+bool tiff_lzw_strip(const uint8_t *src, size_t n, std::vector<uint8_t> &out, size_t want) {
+    return lzw_decode(src, n, out, want);
+}
+
+}  // namespace wc
+
+namespace {
+
+int read_tiff(const char *path, TiffImage &img) {
+    wc::TiffFile t;
+    int rc = wc::parse_tiff(path, t);
+    if (rc) return rc;
+    std::vector<uint8_t> raw;
+    if ((rc = wc::host_strips(path, t, raw))) return rc;
+    const size_t es = t.es(), row = t.row(), total = row * t.h, spp = t.spp;
+    img.w = (int)t.w;
+    img.h = (int)t.h;
+    img.bits = (int)t.bps;
+    img.spp = (int)t.spp;
     img.pix.assign(total, 0);
-    const size_t ns = (size_t)w * spp;  // samples per row; the predictor differences each sample with its left neighbour
-    for (size_t y = 0; y < h; y++) {
+    const size_t ns = (size_t)t.w * spp;  // samples per row; the predictor differences each sample with its left neighbour
+    for (size_t y = 0; y < t.h; y++) {
         const uint8_t *s = raw.data() + y * row;
         if (es == 1) {
             uint8_t *d = img.pix.data() + y * row;
             memcpy(d, s, row);
-            if (pred == 2)
+            if (t.pred == 2)
                 for (size_t x = spp; x < ns; x++) d[x] = (uint8_t)(d[x] + d[x - spp]);
         } else {
             uint16_t *d = (uint16_t *)(img.pix.data() + y * row);
-            for (size_t x = 0; x < ns; x++) d[x] = r.le ? (uint16_t)(s[2 * x] | (s[2 * x + 1] << 8)) : (uint16_t)((s[2 * x] << 8) | s[2 * x + 1]);
-            if (pred == 2)
+            for (size_t x = 0; x < ns; x++)
+                d[x] = t.le ? (uint16_t)(s[2 * x] | (s[2 * x + 1] << 8)) : (uint16_t)((s[2 * x] << 8) | s[2 * x + 1]);
+            if (t.pred == 2)
                 for (size_t x = spp; x < ns; x++) d[x] = (uint16_t)(d[x] + d[x - spp]);
         }
     }

@@ -17,6 +17,7 @@ Every computation runs in the CUDA library (libwndcharm_gb300.so) through its
 C ABI; importing works without a GPU, computing does not.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -367,6 +368,38 @@ class Engine(object):
         if out is None:
             out = np.zeros((n * per, plan.n_features))
         check(lib().wc_extract_samples(self._h, plan.handle, descs, n, ctypes.byref(st), out.ctypes.data, 0))
+        return out
+
+    def read_tiffs_device(self, paths):
+        """TIFF files decoded into device memory (wc_tiff_read_device): returns
+        (buffer, descs) -- a torch uint8 CUDA tensor holding every image's
+        samples and a wc_image_desc array (on_device) for extract_device /
+        extract_samples_device.  Keep the buffer alive while descs are used."""
+        import torch
+        arr = (ctypes.c_char_p * len(paths))(*[os.fsencode(p) for p in paths])
+        nb = ctypes.c_longlong()
+        check(lib().wc_tiff_device_bytes(arr, len(paths), ctypes.byref(nb)))
+        buf = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device="cuda")
+        descs = (_lib.wc_image_desc * len(paths))()
+        check(lib().wc_tiff_read_device(self._h, arr, len(paths), ctypes.c_void_p(buf.data_ptr()), buf.numel(),
+                                        descs))
+        return buf, descs
+
+    def extract_tiffs(self, plan, paths, sampling=None):
+        """Feature rows of TIFF files decoded on the GPU: with a Sampling, every
+        sample of every file (wc_extract_samples, image-major), else one row per
+        file (wc_extract_batch).  Host rows out."""
+        buf, descs = self.read_tiffs_device(paths)
+        n = len(paths)
+        if sampling is None:
+            out = np.zeros((n, plan.n_features))
+            check(lib().wc_extract_batch(self._h, plan.handle, descs, n, out.ctypes.data, 0))
+        else:
+            st = sampling.struct()
+            per = check(lib().wc_sampling_count(ctypes.byref(st)))
+            out = np.zeros((n * per, plan.n_features))
+            check(lib().wc_extract_samples(self._h, plan.handle, descs, n, ctypes.byref(st), out.ctypes.data, 0))
+        del buf
         return out
 
     def extract_device(self, plan, descs, n, out_dev_ptr):

@@ -81,6 +81,10 @@ def lib():
         L.wc_tiff_layout.argtypes = [ctypes.c_char_p, I, I, I, I]
         L.wc_tiff_read.argtypes = [ctypes.c_char_p, vp, ctypes.c_longlong]
         L.wc_engine_graph_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.wc_tiff_device_bytes.argtypes = [ctypes.POINTER(ctypes.c_char_p), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_longlong)]
+        L.wc_tiff_read_device.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, vp, ctypes.c_longlong,
+                                          ctypes.POINTER(wc_image_desc)]
         L.wc_wnd_fit.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D, D, D]
         L.wc_wnd_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D, I]
         L.wc_wnd_normalize.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, D, D, D]

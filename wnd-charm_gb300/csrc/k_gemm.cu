@@ -16,50 +16,72 @@ namespace wc {
 #define GT_K 16
 
 // C[i][j] = sum_k A(i,k) B(k,j); A(i,k) = A[i*sai + k*sak], B(k,j) = B[k*ldb + j],
-// C[i*ldc + j].  One CTA per 64x64 tile, 256 threads, 4x4 outputs each.
+// C[i*ldc + j].  One CTA per 64x64 tile, 256 threads, 4x4 outputs each.  The
+// K tiles are double-buffered: the next tile's global loads are issued into
+// registers before the current tile's products, and stored to the other
+// shared buffer after them, so the FP64 pipe does not wait on global memory
+// (every output still sums its terms in ascending k).
 __device__ void gemm_tile(const double *__restrict__ A, long long sai, long long sak, const double *__restrict__ B,
                           long long ldb, double *__restrict__ C, long long ldc, int M, int N, int K, int ti, int tj) {
-    __shared__ double As[GT_K][GT_M + 1];
-    __shared__ double Bs[GT_K][GT_N + 1];
+    __shared__ double As[2][GT_K][GT_M + 1];
+    __shared__ double Bs[2][GT_K][GT_N + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int i0 = ti * GT_M, j0 = tj * GT_N;
+    constexpr int PER = GT_K * GT_M / 256;  // elements of each tile per thread (4)
     double acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
         for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
+    double ra[PER], rb[PER];
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int q = threadIdx.x + 256 * u;
+            const int kk = q / GT_M, ii = q - kk * GT_M;
+            const int i = i0 + ii, j = j0 + ii, k = k0 + kk;
+            ra[u] = (i < M && k < K) ? A[(long long)i * sai + (long long)k * sak] : 0.0;
+            rb[u] = (j < N && k < K) ? B[(long long)k * ldb + j] : 0.0;
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int q = threadIdx.x + 256 * u;
+            const int kk = q / GT_M, ii = q - kk * GT_M;
+            As[buf][kk][ii] = ra[u];
+            Bs[buf][kk][ii] = rb[u];
+        }
+    };
+    load(0);
+    store(0);
+    __syncthreads();
+    int cur = 0;
     for (int k0 = 0; k0 < K; k0 += GT_K) {
-        for (int q = threadIdx.x; q < GT_K * GT_M; q += blockDim.x) {
-            int kk = q / GT_M, ii = q - kk * GT_M;
-            int i = i0 + ii, k = k0 + kk;
-            As[kk][ii] = (i < M && k < K) ? A[(long long)i * sai + (long long)k * sak] : 0.0;
-        }
-        for (int q = threadIdx.x; q < GT_K * GT_N; q += blockDim.x) {
-            int kk = q / GT_N, jj = q - kk * GT_N;
-            int j = j0 + jj, k = k0 + kk;
-            Bs[kk][jj] = (j < N && k < K) ? B[(long long)k * ldb + j] : 0.0;
-        }
-        __syncthreads();
+        const bool more = k0 + GT_K < K;
+        if (more) load(k0 + GT_K);
         const int kend = min(GT_K, K - k0);
         for (int kk = 0; kk < kend; kk++) {
             double a[4], b[4];
 #pragma unroll
-            for (int r = 0; r < 4; r++) a[r] = As[kk][ty + 16 * r];
+            for (int r = 0; r < 4; r++) a[r] = As[cur][kk][ty + 16 * r];
 #pragma unroll
-            for (int s = 0; s < 4; s++) b[s] = Bs[kk][tx + 16 * s];
+            for (int s2 = 0; s2 < 4; s2++) b[s2] = Bs[cur][kk][tx + 16 * s2];
 #pragma unroll
             for (int r = 0; r < 4; r++)
 #pragma unroll
-                for (int s = 0; s < 4; s++) acc[r][s] = __dadd_rn(acc[r][s], __dmul_rn(a[r], b[s]));
+                for (int s2 = 0; s2 < 4; s2++) acc[r][s2] = __dadd_rn(acc[r][s2], __dmul_rn(a[r], b[s2]));
         }
+        if (more) store(cur ^ 1);
         __syncthreads();
+        cur ^= 1;
     }
 #pragma unroll
     for (int r = 0; r < 4; r++)
 #pragma unroll
-        for (int s = 0; s < 4; s++) {
-            int i = i0 + ty + 16 * r, j = j0 + tx + 16 * s;
-            if (i < M && j < N) C[(long long)i * ldc + j] = acc[r][s];
+        for (int s2 = 0; s2 < 4; s2++) {
+            int i = i0 + ty + 16 * r, j = j0 + tx + 16 * s2;
+            if (i < M && j < N) C[(long long)i * ldc + j] = acc[r][s2];
         }
 }
 

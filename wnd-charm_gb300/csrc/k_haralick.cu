@@ -246,6 +246,19 @@ __device__ void hh_make(const double *v, int n, double *ess, double &tau, double
 // nonnegative terms, so only k in the nonzeros of row i and j in the nonzeros of
 // row k (= column k: the matrix is symmetric) are visited; every Q(i,j) still
 // receives its nonzero terms in ascending k, with the same roundings.
+// RN(rp / d) (P. Markstein, IBM J. Res. Develop. 34(1), 1990): with yh = RN(1/d)
+// and yl ~ 1/d - yh, q0 = RN(rp yh + RN(rp yl)) is within one ulp of rp/d, the
+// residual rp - d q0 is exact and RN(q0 + r yh) is the correctly rounded
+// quotient.  Here d = px py + 1e-13 lies in [1e-13, 1]; far from the normal
+// range (rp < 2^-900) the division itself is used.
+static __device__ __noinline__ double q_div_far(double a, double b) { return a / b; }
+__device__ __forceinline__ double q_quot(double rp, double d, double yh, double yl) {
+    if (rp < 0x1p-900) return q_div_far(rp, d);
+    const double q0 = fma(rp, yh, __dmul_rn(rp, yl));
+    const double r = fma(-q0, d, rp);
+    return fma(r, yh, q0);
+}
+
 #define Q_WARPS 8
 __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
     __shared__ double qrow[Q_WARPS][256];
@@ -278,10 +291,14 @@ __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict
                 const int k = k0 + b;
                 const double a = __shfl_sync(0xffffffffu, al, b);
                 const double d = __dadd_rn(__dmul_rn(di, py[k]), 0.0000000000001);
+                // rp / d for every j of the row by Markstein's method: one
+                // division per (i, k) for yh = RN(1/d), then four FP64
+                // operations per term give the correctly rounded quotient
+                const double yh = 1.0 / d, yl = __dmul_rn(fma(-yh, d, 1.0), yh);
                 const double *Pk = P + (long long)k * n;
                 for (int j = lo[k] + lane; j <= hi[k]; j += 32) {
                     const double rp = __dmul_rn(a, Pk[j]);
-                    if (rp != 0.0) q[j] = __dadd_rn(q[j], rp / d);
+                    if (rp != 0.0) q[j] = __dadd_rn(q[j], q_quot(rp, d, yh, yl));
                 }
                 __syncwarp();
             }

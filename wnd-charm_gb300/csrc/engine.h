@@ -76,6 +76,9 @@ struct Tables {
     const double *d() const { return (const double *)dev.p; }
 };
 
+// The FFT description of one length, its twiddles added to the tables (engine.cu).
+FFTPlan fft_plan(Tables &tabs, int n);
+
 // Runs a plan over a batch on the engine's stream (engine.cu).
 struct Plan;
 int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, double *dfeat,

@@ -18,18 +18,20 @@
 namespace wc {
 
 // batched 1-D complex DFTs: arrays blockIdx.y, line groups blockIdx.x; element
-// k of line l at data + arr*js + l*ls + k*es (units of complex elements).
+// k of line l at data + arr*js + l*ls + k*es (units of complex elements), or
+// at data + aoff[arr] + l*ls + k*es with a table of array offsets.
 // R = double is the FP64 form, R = float the mixed form.
 template <typename R>
 __global__ void k_cfft_lines(R *__restrict__ data, long long js, int nl, int n, long long ls, long long es,
-                             const FFTPlan *__restrict__ plan, const double *__restrict__ twd, int lpc) {
+                             const FFTPlan *__restrict__ plan, const double *__restrict__ twd, int lpc,
+                             const long long *__restrict__ aoff) {
     typedef cpx<R> C;
     extern __shared__ __align__(16) unsigned char fsm[];
     const FFTPlan P = *plan;
     const int l0 = blockIdx.x * lpc;
     if (l0 >= nl) return;
     const int lines = min(lpc, nl - l0);
-    C *base = (C *)data + (long long)blockIdx.y * js;
+    C *base = (C *)data + (aoff ? aoff[blockIdx.y] : (long long)blockIdx.y * js);
     C *b0 = (C *)fsm, *b1 = b0 + (long long)lpc * n;
     const cplx *tw = (const cplx *)(twd + P.tw_off);
     // the twiddles in the element type, rounded once per block (after the two line buffers)
@@ -77,12 +79,29 @@ static void cfft2(Ctx &c, double *data, int na, int fh, int fw, const FFTPlan *p
     lpc = lpc < 1 ? 1 : (lpc > 8 ? 8 : lpc);
     WC_LAUNCH(c);
     k_cfft_lines<R><<<dim3((fh + lpc - 1) / lpc, na), 256, ((size_t)lpc * 2 + 1) * fw * es, c.st>>>((R *)data, js, fh, fw, fw, 1,
-                                                                                            plan_w, tw, lpc);
+                                                                                            plan_w, tw, lpc, nullptr);
     int lpc2 = 96 * 1024 / (2 * es * fh);
     lpc2 = lpc2 < 1 ? 1 : (lpc2 > 8 ? 8 : lpc2);
     WC_LAUNCH(c);
     k_cfft_lines<R><<<dim3((fw + lpc2 - 1) / lpc2, na), 256, ((size_t)lpc2 * 2 + 1) * fh * es, c.st>>>((R *)data, js, fw, fh, 1, fw,
-                                                                                               plan_h, tw, lpc2);
+                                                                                               plan_h, tw, lpc2, nullptr);
+}
+
+// FP64 forward DFTs of na complex arrays of the same shape at complex offsets
+// aoff[] from data: the nl lines of length n (element stride es, line stride
+// ls) of each, in place (used by the Fourier node's backward pass)
+void cfft_lines_fp64(cudaStream_t st, long long *launches, double *data, const long long *aoff, int na, int nl, int n,
+                     long long ls, long long es, const FFTPlan *plan, const double *tw) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_cfft_lines<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    int lpc = 96 * 1024 / (2 * 16 * n);
+    lpc = lpc < 1 ? 1 : (lpc > 8 ? 8 : lpc);
+    ++*launches;
+    k_cfft_lines<double><<<dim3((nl + lpc - 1) / lpc, na), 256, ((size_t)lpc * 2 + 1) * n * 16, st>>>(
+        data, 0, nl, n, ls, es, plan, tw, lpc, aoff);
 }
 
 // zero-padded image (job) into a fh x fw complex array

@@ -651,41 +651,6 @@ __global__ void k_g_gemm(const MJob *__restrict__ jobs) {
     *c = J.acc ? *c + s : s;
 }
 
-// Direct DFT of the lines of every job's W x H complex array (rows = 0:
-// the H lines of length W; rows = 1: the W columns of length H), a line per
-// block: the line and the twiddles e^{-2 pi i k / n} (tw[len] per length,
-// offsets twoff) are staged in shared memory, out_k = sum_j in_j tw[(j k) mod n].
-__global__ void k_g_dft(const TJobG *__restrict__ jobs, const double2 *__restrict__ in, double2 *__restrict__ out,
-                        int rows, const double2 *__restrict__ tw, const long long *__restrict__ twoff) {
-    extern __shared__ double2 shd[];
-    const TJobG J = jobs[blockIdx.y];
-    const int W = J.pw, H = J.ph;
-    const int n = rows ? H : W, lines = rows ? W : H;
-    const int l = blockIdx.x;
-    if (l >= lines) return;
-    const long long ls = rows ? 1 : W, es = rows ? W : 1;
-    const double2 *src = in + J.scr / 2;
-    double2 *dst = out + J.scr / 2;
-    double2 *line = shd, *t = shd + n;
-    const double2 *twn = tw + twoff[blockIdx.y * 2 + rows];
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        line[j] = src[l * ls + j * es];
-        t[j] = twn[j];
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        double re = 0, im = 0;
-        int idx = 0;
-        for (int j = 0; j < n; j++) {
-            const double2 a = line[j], w = t[idx];
-            re += a.x * w.x - a.y * w.y;
-            im += a.x * w.y + a.y * w.x;
-            idx += k;
-            if (idx >= n) idx -= n;
-        }
-        dst[l * ls + k * es] = make_double2(re, im);
-    }
-}
 // the parent plane as complex numbers
 __global__ void k_g_real2c(const double *__restrict__ arena, const TJobG *__restrict__ jobs, double2 *__restrict__ X) {
     const TJobG J = jobs[blockIdx.y];
@@ -958,8 +923,8 @@ extern "C" int wc_wnd_grad(wc_engine *E, const wc_plan *plan, const double *trai
         if ((rc = B.put(&dtj[k], tjs[k], st))) return rc;
         scr_max = std::max(scr_max, tscr_elems[k]);
     }
-    double *tscratch = nullptr, *tscratch2 = nullptr;
-    if (scr_max && ((rc = B.get(&tscratch, (size_t)scr_max * 8)) || (rc = B.get(&tscratch2, (size_t)scr_max * 8))))
+    double *tscratch = nullptr;
+    if (scr_max && (rc = B.get(&tscratch, (size_t)scr_max * 8)))
         return rc;
     // Chebyshev factor matrices, per (length, N), and the products' temporaries
     std::map<std::pair<int, int>, double *> fac;
@@ -1004,29 +969,28 @@ extern "C" int wc_wnd_grad(wc_engine *E, const wc_plan *plan, const double *trai
         g1[k] = dim3((mo + 15) / 16, (mh + 15) / 16, n);
         g2[k] = dim3((mw + 15) / 16, (mh + 15) / 16, n);
     }
-    // Fourier twiddles per length, and each job's offsets
-    std::vector<double2 *> dtw(NN, nullptr);
-    std::vector<long long *> dtwo(NN, nullptr);
+    // Fourier nodes: the jobs grouped by shape, each group's complex-array
+    // offsets and its two FFT plans (row length, column length)
+    struct FGroup {
+        int w, h, na;
+        long long *aoff;
+        FFTPlan *plans;
+    };
+    std::vector<std::vector<FGroup>> fgroups(NN);
     for (int k = NN - 1; k >= 1; k--) {
         if (xf[k] != X_FOURIER) continue;
-        std::vector<double2> twv;
-        std::vector<long long> twoff(2 * n);
-        std::map<int, long long> at;
-        for (int i = 0; i < n; i++)
-            for (int r = 0; r < 2; r++) {
-                const int len = r ? tjs[k][i].ph : tjs[k][i].pw;
-                auto it = at.find(len);
-                if (it == at.end()) {
-                    it = at.emplace(len, (long long)twv.size()).first;
-                    for (int q = 0; q < len; q++) {
-                        const double a = -2.0 * M_PI * (double)q / (double)len;
-                        twv.push_back(make_double2(std::cos(a), std::sin(a)));
-                    }
-                }
-                twoff[2 * i + r] = it->second;
-            }
-        if ((rc = B.put(&dtw[k], twv, st)) || (rc = B.put(&dtwo[k], twoff, st))) return rc;
+        std::map<std::pair<int, int>, std::vector<long long>> by;
+        for (int i = 0; i < n; i++) by[std::make_pair(tjs[k][i].pw, tjs[k][i].ph)].push_back(tjs[k][i].scr / 2);
+        for (auto &kv : by) {
+            const int w = kv.first.first, h = kv.first.second;
+            if (w > kMaxFFT || h > kMaxFFT) return set_err(WC_ERR_UNSUPPORTED, "wc_wnd_grad: Fourier side > %d", kMaxFFT);
+            std::vector<FFTPlan> pl = {fft_plan(E->tabs, w), fft_plan(E->tabs, h)};
+            FGroup g{w, h, (int)kv.second.size(), nullptr, nullptr};
+            if ((rc = B.put(&g.aoff, kv.second, st)) || (rc = B.put(&g.plans, pl, st))) return rc;
+            fgroups[k].push_back(g);
+        }
     }
+    if ((rc = E->tabs.sync(st))) return rc;  // twiddles of any new length
     std::vector<long long> img_px(n), img_off(n);
     {
         long long o = 0;
@@ -1093,16 +1057,20 @@ extern "C" int wc_wnd_grad(wc_engine *E, const wc_plan *plan, const double *trai
                 k_g_gemm<<<g2[k], dim3(16, 16), 0, st>>>(dm2[k]);
             } else if (xf[k] == X_FOURIER) {
                 // X = DFT2(parent) (rows, then columns), H = g conj(X) / |X|,
-                // g_parent += Re DFT2(H); every image of the batch in each launch
-                double2 *X = (double2 *)tscratch, *Y = (double2 *)tscratch2;
-                const size_t sh = 2 * (size_t)std::max(maxw, maxh) * sizeof(double2);
-                *launches += 7;
+                // g_parent += Re DFT2(H): the DFTs are the engine's FP64 FFTs
+                // over every image of a shape group at once, in place
+                double2 *X = (double2 *)tscratch;
+                *launches += 3;
                 k_g_real2c<<<dim3(32, n), 256, 0, st>>>(arena, dj, X);
-                k_g_dft<<<dim3(maxh, n), 128, sh, st>>>(dj, X, Y, 0, dtw[k], dtwo[k]);
-                k_g_dft<<<dim3(maxw, n), 128, sh, st>>>(dj, Y, X, 1, dtw[k], dtwo[k]);
+                for (const FGroup &g : fgroups[k]) {
+                    cfft_lines_fp64(st, launches, (double *)X, g.aoff, g.na, g.h, g.w, g.w, 1, g.plans, E->tabs.d());
+                    cfft_lines_fp64(st, launches, (double *)X, g.aoff, g.na, g.w, g.h, 1, g.w, g.plans + 1, E->tabs.d());
+                }
                 k_g_fgrad<<<dim3(32, n), 256, 0, st>>>(garena, dj, X);
-                k_g_dft<<<dim3(maxh, n), 128, sh, st>>>(dj, X, Y, 0, dtw[k], dtwo[k]);
-                k_g_dft<<<dim3(maxw, n), 128, sh, st>>>(dj, Y, X, 1, dtw[k], dtwo[k]);
+                for (const FGroup &g : fgroups[k]) {
+                    cfft_lines_fp64(st, launches, (double *)X, g.aoff, g.na, g.h, g.w, g.w, 1, g.plans, E->tabs.d());
+                    cfft_lines_fp64(st, launches, (double *)X, g.aoff, g.na, g.w, g.h, 1, g.w, g.plans + 1, E->tabs.d());
+                }
                 k_g_addre<<<dim3(32, n), 256, 0, st>>>(dj, X, garena);
             } else {
                 return set_err(WC_ERR_UNSUPPORTED, "wc_wnd_grad: no adjoint for transform %d", xf[k]);

@@ -42,6 +42,10 @@ struct FFTPlan {  // device description of one length
     int radix[16];
     long long tw_off;  // offset of exp(-2 pi i k / n), k < n, in the twiddle table (interleaved re, im)
 };
+// k_gabor.cu: FP64 forward DFTs of na same-shape complex arrays at complex
+// offsets aoff[] from data (nl lines of length n each, in place)
+void cfft_lines_fp64(cudaStream_t st, long long *launches, double *data, const long long *aoff, int na, int nl, int n,
+                     long long ls, long long es, const FFTPlan *plan, const double *tw);
 void launch_fourier(Ctx &c, double *arena, const Plane *planes, const TJob *jobs, int njobs, int maxw, int maxh,
                     const FFTPlan *plans_d, const int *job_plan_y, const int *job_plan_x, const double *tw,
                     double *cbuf, const long long *cbuf_off);

@@ -191,6 +191,22 @@ int wc_wnd_classify(wc_engine *engine, const double *train, int N, int F, const 
 int wc_wnd_normalize(wc_engine *engine, const double *rows, int n, int F, const double *mins, const double *maxs,
                      double *out);
 
+/* wc_wnd_fit over training rows sharded across processes, in three stages of
+ * this process's statistics with an exchange between them (min / max, then
+ * sums; TrainingSet::normalize + SetFisherScores, TrainingSet.cpp:2090-2324):
+ *   stage 0: out = [mins (F), maxs (F)] of the finite values (FLT_MAX / -FLT_MAX
+ *            where none), counts = rows per label (C+1: slot 0 every labelled
+ *            row, slot c class c);
+ *   stage 1: with the global mins / maxs, out = per-label sums of the normalised
+ *            values ((C+1) x F, label-major);
+ *   stage 2: with the global class means ((C+1) x F: sums / counts, 0 where a
+ *            count is 0), out = per-label sums of squared deviations.
+ * wc_wnd_fisher turns the summed statistics into wc_wnd_fit's weights. */
+int wc_wnd_fit_stats(wc_engine *engine, int stage, const double *train, int N, int F, const int *labels, int C,
+                     const double *mins, const double *maxs, const double *means, double *out, long long *counts);
+int wc_wnd_fisher(wc_engine *engine, int F, int C, double frac, const double *sums, const long long *counts,
+                  const double *sq, double *weights);
+
 /* classify2's per-class partial sums over the training rows given (a shard of
  * the training set): sums[t*C + c-1] = sum of d(t,s)^-5 over the rows s of class c
  * with d >= DBL_EPSILON, counts[t*C + c-1] how many (FP64, the reference's

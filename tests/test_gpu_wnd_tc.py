@@ -154,3 +154,29 @@ def test_class_sums_over_shards_give_classify2():
     probs, pred, _ = wnd_finish(s1 + s2, c1 + c2)
     np.testing.assert_array_equal(pred, pr)
     np.testing.assert_allclose(probs, p, rtol=1e-12, atol=1e-15)
+
+
+def test_fit_stats_over_shards_give_wnd_fit():
+    """wc_wnd_fit_stats on three shards of the training rows, combined as the
+    sharded fit's all-reduces combine them (min, max, sums), and
+    wc_wnd_fisher: wc_wnd_fit's ranges exactly, its weights and selection."""
+    import wndcharm
+    from wndcharm import synth
+    from wndcharm.dist import class_means
+    xtr, ytr, _, _ = synth.feature_vectors(5000, 10, 2919, 10, 13)
+    xtr[17, 5] = np.nan
+    e = wndcharm.Engine(0, "fp64")
+    w, mn, mx = e.wnd_fit(xtr, ytr, 10, 0.15)
+    parts = [(xtr[a:b], ytr[a:b]) for a, b in ((0, 1700), (1700, 3300), (3300, 5000))]
+    st0 = [e.wnd_fit_stats(0, X, y, 10) for X, y in parts]
+    gmn = np.min([s[0] for s in st0], axis=0)
+    gmx = np.max([s[1] for s in st0], axis=0)
+    cnt = np.sum([s[2] for s in st0], axis=0)
+    np.testing.assert_array_equal(gmn, mn)
+    np.testing.assert_array_equal(gmx, mx)
+    sums = np.sum([e.wnd_fit_stats(1, X, y, 10, gmn, gmx) for X, y in parts], axis=0)
+    means = class_means(sums, cnt)
+    sq = np.sum([e.wnd_fit_stats(2, X, y, 10, gmn, gmx, means) for X, y in parts], axis=0)
+    w2 = e.wnd_fisher(10, 0.15, sums, cnt, sq)
+    np.testing.assert_array_equal(w2 == 0, w == 0)
+    np.testing.assert_allclose(w2, w, rtol=1e-12, atol=0)

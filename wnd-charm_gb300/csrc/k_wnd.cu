@@ -179,6 +179,17 @@ __global__ void k_wnd_fit_combine(const double *__restrict__ part, int R, int F,
     w[f] = dev / var;
 }
 
+// the ranges' partial sums added in range order: out[c * F + f]
+__global__ void k_wnd_fit_rsum(const double *__restrict__ part, int R, int F, int C, double *__restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    for (int c = 0; c <= C; c++) {
+        double t = 0;
+        for (int r = 0; r < R; r++) t += part[((long long)r * (C + 1) + c) * F + f];
+        out[(long long)c * F + f] = t;
+    }
+}
+
 // gather the kept features, normalised: Xc is K x rows (column-major per row
 // set) so lanes reading consecutive rows coalesce.
 __global__ void k_wnd_gather(const double *__restrict__ X, int rows, int F, const int *__restrict__ keep, int K,
@@ -522,6 +533,18 @@ using namespace wc;
         if (e_ != cudaSuccess) { rc = set_err(WC_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); goto done; } \
     } while (0)
 
+// SetFisherScores' selection: every weight below the one at sorted
+// (descending) rank floor(frac*F + 0.5) set to 0
+static void fisher_threshold(double *weights, int F, double frac) {
+    const int last = (int)std::floor((frac * (double)F) + 0.5);
+    if (last >= F) return;
+    std::vector<double> sw(weights, weights + F);
+    std::nth_element(sw.begin(), sw.begin() + last, sw.end(), std::greater<double>());
+    const double thr = sw[last];
+    for (int f = 0; f < F; f++)
+        if (weights[f] < thr) weights[f] = 0.0;
+}
+
 // normalize + SetFisherScores over device rows: dmin/dmax (device) get the
 // per-feature range, weights (host) the thresholded Fisher scores
 static int wnd_fit_dev(wc_engine *E, const double *dX, int N, int F, const int *dy, int C, double frac, double *weights,
@@ -553,17 +576,7 @@ static int wnd_fit_dev(wc_engine *E, const double *dX, int N, int F, const int *
     CKW(cudaGetLastError());
     CKW(cudaMemcpyAsync(weights, dw, F * sizeof(double), cudaMemcpyDeviceToHost, st));
     CKW(cudaStreamSynchronize(st));
-    {
-        // threshold at the weight of sorted (descending) rank floor(frac*F + 0.5)
-        int last = (int)std::floor((frac * (double)F) + 0.5);
-        if (last < F) {
-            std::vector<double> sw(weights, weights + F);
-            std::nth_element(sw.begin(), sw.begin() + last, sw.end(), std::greater<double>());
-            const double thr = sw[last];
-            for (int f = 0; f < F; f++)
-                if (weights[f] < thr) weights[f] = 0.0;
-        }
-    }
+    fisher_threshold(weights, F, frac);
 done:
     cudaFree(dpmin);
     cudaFree(dpmax);
@@ -947,6 +960,92 @@ extern "C" int wc_wnd_class_sums(wc_engine *E, const double *train, int N, int F
     CKR(cudaMemcpyAsync(sums, dsum, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
     CKR(cudaMemcpyAsync(counts, dcnt, (size_t)T * C * 8, cudaMemcpyDeviceToHost, st));
     CKR(cudaStreamSynchronize(st));
+    return WC_OK;
+}
+
+// TrainingSet::normalize + SetFisherScores over training rows sharded across
+// processes: the statistics of this process's rows, in three stages that an
+// exchange (min / max, then sums) separates.  stage 0: out = [mins (F), maxs (F)]
+// of the finite values (FLT_MAX / -FLT_MAX where none), counts = rows per label
+// (slot 0: every labelled row, slot c: class c); stage 1 (the global mins /
+// maxs): out = per-label sums of the normalised values ((C+1) x F); stage 2
+// (the global class means, (C+1) x F): out = per-label sums of squared
+// deviations from them.
+extern "C" int wc_wnd_fit_stats(wc_engine *E, int stage, const double *train, int N, int F, const int *labels, int C,
+                                const double *mins, const double *maxs, const double *means, double *out,
+                                long long *counts) {
+    if (!E || !train || !labels || !out || N < 1 || F < 1 || C < 1 || C > 16 || stage < 0 || stage > 2 ||
+        (stage == 0 && !counts) || (stage >= 1 && (!mins || !maxs)) || (stage == 2 && !means))
+        return set_err(WC_ERR_ARG, "wc_wnd_fit_stats: bad arguments");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    const int fb = (F + 31) / 32;
+    const int R = std::max(1, std::min((N + 255) / 256, (8 * engine_sms(E) + fb - 1) / fb));
+    const int rows_per = (N + R - 1) / R;
+    WBufs B;
+    double *dX, *dmin, *dmax, *dmean, *dpa, *dpb, *dout;
+    int *dy;
+    long long *dcnt;
+    if ((rc = B.get(&dX, (size_t)N * F * 8)) || (rc = B.get(&dy, (size_t)N * 4)) || (rc = B.get(&dmin, F * 8)) ||
+        (rc = B.get(&dmax, F * 8)) || (rc = B.get(&dmean, (size_t)(C + 1) * F * 8)) ||
+        (rc = B.get(&dpa, (size_t)R * (C + 1) * F * 8)) || (rc = B.get(&dpb, (size_t)R * F * 8)) ||
+        (rc = B.get(&dout, (size_t)(C + 1) * F * 8)) || (rc = B.get(&dcnt, 17 * 8)))
+        return rc;
+    CKR(cudaMemcpyAsync(dX, train, (size_t)N * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dy, labels, (size_t)N * 4, cudaMemcpyHostToDevice, st));
+    if (stage == 0) {
+        CKR(cudaMemsetAsync(dcnt, 0, 17 * 8, st));
+        *launches += 3;
+        k_wnd_fit_minmax<<<dim3(fb, R), 256, 0, st>>>(dX, N, F, rows_per, dpa, dpb);
+        k_wnd_fit_minmax_final<<<(F + 255) / 256, 256, 0, st>>>(dpa, dpb, R, F, dout, dout + F);
+        k_wnd_fit_count<<<std::min(1024, (N + 255) / 256), 256, 0, st>>>(dy, N, C, dcnt);
+        CKR(cudaGetLastError());
+        CKR(cudaMemcpyAsync(out, dout, (size_t)2 * F * 8, cudaMemcpyDeviceToHost, st));
+        CKR(cudaMemcpyAsync(counts, dcnt, (size_t)(C + 1) * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+        CKR(cudaMemcpyAsync(dmin, mins, F * 8, cudaMemcpyHostToDevice, st));
+        CKR(cudaMemcpyAsync(dmax, maxs, F * 8, cudaMemcpyHostToDevice, st));
+        if (stage == 2) CKR(cudaMemcpyAsync(dmean, means, (size_t)(C + 1) * F * 8, cudaMemcpyHostToDevice, st));
+        *launches += 2;
+        k_wnd_fit_moments<<<dim3(fb, R), 256, 0, st>>>(dX, dy, N, F, C, rows_per, dmin, dmax,
+                                                        stage == 2 ? dmean : nullptr, stage == 2, dpa);
+        k_wnd_fit_rsum<<<(F + 255) / 256, 256, 0, st>>>(dpa, R, F, C, dout);
+        CKR(cudaGetLastError());
+        CKR(cudaMemcpyAsync(out, dout, (size_t)(C + 1) * F * 8, cudaMemcpyDeviceToHost, st));
+    }
+    CKR(cudaStreamSynchronize(st));
+    return WC_OK;
+}
+
+// The Fisher weights from the exchanged statistics (wc_wnd_fit_stats summed
+// over every process): class means, between-class over mean within-class
+// variance as wc_wnd_fit computes them, and SetFisherScores' selection.
+extern "C" int wc_wnd_fisher(wc_engine *E, int F, int C, double frac, const double *sums, const long long *counts,
+                             const double *sq, double *weights) {
+    if (!E || !sums || !counts || !sq || !weights || F < 1 || C < 1 || C > 16)
+        return set_err(WC_ERR_ARG, "wc_wnd_fisher: bad arguments");
+    cudaStream_t st;
+    long long *launches;
+    int rc = engine_device(E, &st, &launches);
+    if (rc) return rc;
+    WBufs B;
+    double *dsum, *dsq, *dmean, *dw;
+    long long *dcnt;
+    if ((rc = B.get(&dsum, (size_t)(C + 1) * F * 8)) || (rc = B.get(&dsq, (size_t)(C + 1) * F * 8)) ||
+        (rc = B.get(&dmean, (size_t)(C + 1) * F * 8)) || (rc = B.get(&dw, F * 8)) || (rc = B.get(&dcnt, 17 * 8)))
+        return rc;
+    CKR(cudaMemcpyAsync(dsum, sums, (size_t)(C + 1) * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dsq, sq, (size_t)(C + 1) * F * 8, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(dcnt, counts, (size_t)(C + 1) * 8, cudaMemcpyHostToDevice, st));
+    *launches += 2;
+    k_wnd_fit_combine<<<(F + 255) / 256, 256, 0, st>>>(dsum, 1, F, C, dcnt, 0, dmean, nullptr);
+    k_wnd_fit_combine<<<(F + 255) / 256, 256, 0, st>>>(dsq, 1, F, C, dcnt, 1, dmean, dw);
+    CKR(cudaGetLastError());
+    CKR(cudaMemcpyAsync(weights, dw, F * 8, cudaMemcpyDeviceToHost, st));
+    CKR(cudaStreamSynchronize(st));
+    fisher_threshold(weights, F, frac);
     return WC_OK;
 }
 

@@ -451,6 +451,42 @@ class Engine(object):
                                      mx.ctypes.data_as(_lib.D), out.ctypes.data_as(_lib.D)))
         return out
 
+    def wnd_fit_stats(self, stage, train, labels, n_classes, mins=None, maxs=None, means=None):
+        """wc_wnd_fit_stats on these training rows (a shard): stage 0 ->
+        (mins, maxs, counts (C+1)); stage 1 -> per-label sums ((C+1), F);
+        stage 2 -> per-label sums of squared deviations ((C+1), F)."""
+        X = np.ascontiguousarray(train, dtype=np.float64)
+        y = np.ascontiguousarray(labels, dtype=np.int32)
+        N, F = X.shape
+        C = int(n_classes)
+        LL = ctypes.POINTER(ctypes.c_longlong)
+        arg = lambda v: None if v is None else np.ascontiguousarray(v, dtype=np.float64)  # noqa: E731
+        mn, mx, me = arg(mins), arg(maxs), arg(means)
+        ptr = lambda v: None if v is None else v.ctypes.data_as(_lib.D)  # noqa: E731
+        if stage == 0:
+            out = np.zeros(2 * F)
+            counts = np.zeros(C + 1, dtype=np.int64)
+            check(lib().wc_wnd_fit_stats(self._h, 0, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I), C,
+                                         None, None, None, out.ctypes.data_as(_lib.D), counts.ctypes.data_as(LL)))
+            return out[:F], out[F:], counts
+        out = np.zeros((C + 1, F))
+        check(lib().wc_wnd_fit_stats(self._h, int(stage), X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I),
+                                     C, ptr(mn), ptr(mx), ptr(me), out.ctypes.data_as(_lib.D), None))
+        return out
+
+    def wnd_fisher(self, n_classes, frac, sums, counts, sq):
+        """Fisher weights (SetFisherScores' selection included) from summed
+        wnd_fit_stats statistics."""
+        sums = np.ascontiguousarray(sums, dtype=np.float64)
+        sq = np.ascontiguousarray(sq, dtype=np.float64)
+        counts = np.ascontiguousarray(counts, dtype=np.int64)
+        F = sums.shape[1]
+        w = np.zeros(F)
+        check(lib().wc_wnd_fisher(self._h, F, int(n_classes), float(frac), sums.ctypes.data_as(_lib.D),
+                                  counts.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                  sq.ctypes.data_as(_lib.D), w.ctypes.data_as(_lib.D)))
+        return w
+
     def wnd_class_sums(self, train, labels, n_classes, weights, mins, maxs, test):
         """classify2's per-class sums of d^-5 and counts over these training
         rows (a shard): (sums (T, C) float64, counts (T, C) int64)."""

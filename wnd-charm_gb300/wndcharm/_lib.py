@@ -90,6 +90,9 @@ def lib():
         L.wc_wnd_normalize.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, D, D, D]
         L.wc_wnd_class_sums.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, ctypes.c_int, D,
                                         ctypes.POINTER(ctypes.c_longlong)]
+        LL = ctypes.POINTER(ctypes.c_longlong)
+        L.wc_wnd_fit_stats.argtypes = [vp, ctypes.c_int, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, D, D, D, D, LL]
+        L.wc_wnd_fisher.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, D, LL, D, D]
         L.wc_wnd_fit_classify.argtypes = [vp, D, ctypes.c_int, ctypes.c_int, I, ctypes.c_int, ctypes.c_double, D,
                                           ctypes.c_int, D, D, D, D, I]
         L.wc_wnd_fit_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp, vp,

@@ -95,3 +95,48 @@ def wnd_classify_sharded(engine, train_shard, labels_shard, n_classes, weights, 
         sums, counts = ts.numpy(), tc.numpy()
     probs, pred, _ = wnd_finish(sums, counts)
     return probs, pred
+
+
+def class_means(sums, counts):
+    """Per-label means of the exchanged sums (0 where a label has no row), as
+    wc_wnd_fit divides them."""
+    counts = np.asarray(counts, dtype=np.int64)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        m = np.asarray(sums, dtype=np.float64) / counts[:, None].astype(np.float64)
+    return np.where(counts[:, None] > 0, m, 0.0)
+
+
+def wnd_fit_sharded(engine, train_shard, labels_shard, n_classes, frac=0.15, group=None, stats_fn=None,
+                    fisher_fn=None):
+    """wnd_fit (TrainingSet::normalize + SetFisherScores) with the training
+    rows sharded across ranks: each rank's min / max and label counts, one
+    MIN / MAX / SUM all-reduce; its per-label sums of the normalised values,
+    one SUM all-reduce (the class means); its per-label sums of squared
+    deviations, one SUM all-reduce; then the Fisher weights (wc_wnd_fisher) on
+    every rank.  Returns (weights, mins, maxs), the same on every rank.
+    stats_fn(stage, train, labels, C, mins, maxs, means) and
+    fisher_fn(C, frac, sums, counts, sq) replace the engine calls where a test
+    runs the exchange without a GPU."""
+    import torch
+    import torch.distributed as dist
+    stats = stats_fn if stats_fn is not None else (
+        lambda st, X, y, C, mn=None, mx=None, me=None: engine.wnd_fit_stats(st, X, y, C, mn, mx, me))
+    fisher = fisher_fn if fisher_fn is not None else engine.wnd_fisher
+    C = int(n_classes)
+    multi = dist.is_initialized() and dist.get_world_size(group) > 1
+
+    def reduce(a, op):
+        if not multi:
+            return a
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        dist.all_reduce(t, op=op, group=group)
+        return t.numpy()
+
+    mins, maxs, counts = stats(0, train_shard, labels_shard, C)
+    mins = reduce(mins, dist.ReduceOp.MIN if multi else None)
+    maxs = reduce(maxs, dist.ReduceOp.MAX if multi else None)
+    counts = reduce(counts, dist.ReduceOp.SUM if multi else None)
+    sums = reduce(stats(1, train_shard, labels_shard, C, mins, maxs), dist.ReduceOp.SUM if multi else None)
+    means = class_means(sums, counts)
+    sq = reduce(stats(2, train_shard, labels_shard, C, mins, maxs, means), dist.ReduceOp.SUM if multi else None)
+    return fisher(C, frac, sums, counts, sq), mins, maxs

@@ -76,3 +76,60 @@ def test_wavelet_noalloc_one_column_at_the_scratch_limit():
     np.testing.assert_array_equal(d_out.cpu().numpy(), exp)
     rc = L.wc_wavelet_noalloc(ctypes.c_void_p(d_in.data_ptr()), 1, h + 2, ctypes.c_void_p(d_out.data_ptr()), None)
     assert rc == -1  # one row pair more than the scratch holds
+
+
+RESET_PROGRAM = r"""
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <cuda_runtime.h>
+#include "wndcharm_gb300.h"
+// wc_wavelet_noalloc before and after cudaDeviceReset (a new primary context:
+// the library's device code is loaded again and its static scratch may move)
+static int run(const std::vector<double> &in, int w, int h, std::vector<double> &out) {
+    double *din = nullptr, *dout = nullptr;
+    if (cudaMalloc(&din, in.size() * 8) != cudaSuccess || cudaMalloc(&dout, out.size() * 8) != cudaSuccess) return 1;
+    cudaMemcpy(din, in.data(), in.size() * 8, cudaMemcpyHostToDevice);
+    if (wc_wavelet_noalloc(din, w, h, dout, nullptr) != 0) { printf("rc: %s\n", wc_last_error()); return 2; }
+    if (cudaDeviceSynchronize() != cudaSuccess) return 3;
+    cudaMemcpy(out.data(), dout, out.size() * 8, cudaMemcpyDeviceToHost);
+    cudaFree(din);
+    cudaFree(dout);
+    return 0;
+}
+int main() {
+    const int w = 64, h = 48, ow = 2 * ((w + 9) / 2), oh = 2 * ((h + 9) / 2);
+    std::vector<double> in((size_t)w * h), a((size_t)ow * oh), b((size_t)ow * oh, -1.0);
+    for (int i = 0; i < w * h; i++) in[i] = (i * 37) % 4096;
+    int rc = run(in, w, h, a);
+    if (rc) return rc;
+    if (cudaDeviceReset() != cudaSuccess) return 4;
+    rc = run(in, w, h, b);
+    if (rc) return 10 + rc;
+    if (memcmp(a.data(), b.data(), a.size() * 8) != 0) { printf("differ\n"); return 20; }
+    printf("same after reset\n");
+    return 0;
+}
+"""
+
+
+def test_wavelet_noalloc_after_device_reset(tmp_path):
+    """A process calls the entry point, resets the device (cudaDeviceReset:
+    the primary context and the library's loaded device code are recreated,
+    so the static scratch's address may change), and calls it again: the
+    scratch is looked up on every call, and the output is the same."""
+    import os
+    import shutil
+    import subprocess
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = os.path.join(repo, "wnd-charm_gb300", "build")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = tmp_path / "reset.cu"
+    src.write_text(RESET_PROGRAM)
+    exe = tmp_path / "reset"
+    b = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-I" + os.path.join(repo, "include"),
+                        str(src), "-o", str(exe), "-L" + lib, "-lwndcharm_gb300", "-Xlinker", "-rpath=" + lib],
+                       capture_output=True, text=True, timeout=600)
+    assert b.returncode == 0, b.stderr[-2000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "same after reset" in r.stdout, (r.returncode, r.stdout, r.stderr)

@@ -114,6 +114,11 @@ void wc_engine_destroy(wc_engine *engine);
  *                      labelling; 0 (default): the plane's pixel count, a bound
  *                      no correct run reaches.  A run that reaches the cap
  *                      returns WC_ERR_DEVICE (the bounded-wait error path).
+ *   "cf_tensor_cores"  1 (default): in the mixed form, when every Chebyshev-
+ *                      Fourier plane of a batch has one size, its 23 x 23
+ *                      coefficient sums run on the tensor cores (three bf16
+ *                      digits per value, FP32 sums over 1024-pixel chunks
+ *                      added in FP64); 0: FP32 sums on the CUDA cores.
  *   "graph"            0 (default); 1: wc_extract / wc_extract_batch capture the
  *                      launches of a batch shape (plan, image types and sizes,
  *                      output) in a CUDA graph the second time the shape is seen,

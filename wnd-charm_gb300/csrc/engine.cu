@@ -327,6 +327,8 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
 
     // feature-family preparation (tables, workspace, metadata)
     FeatureSetup fs;
+    fs.prec = E->prec;
+    fs.cf_tc = E->opts.cf_tc;
     fs.planes = &planes;
     fs.fj = &fj;
     fs.tabs_add = [&](const std::string &k, const std::function<std::vector<double>()> &gen) {
@@ -780,6 +782,9 @@ int wc_engine_set_option(wc_engine *E, const char *name, long long value) {
     } else if (k == "union_find_cap") {
         if (value < 0) return set_err(WC_ERR_ARG, "union_find_cap must be >= 0");
         E->opts.union_find_cap = value;
+    } else if (k == "cf_tensor_cores") {
+        if (value != 0 && value != 1) return set_err(WC_ERR_ARG, "cf_tensor_cores must be 0 or 1");
+        E->opts.cf_tc = (int)value;
     } else if (k == "graph") {
         if (value != 0 && value != 1) return set_err(WC_ERR_ARG, "graph must be 0 or 1");
         E->graph = (int)value;

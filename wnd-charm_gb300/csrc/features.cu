@@ -71,6 +71,12 @@ int features_check(cudaStream_t st, int *dev_err) {
         cudaMemcpyToSymbolAsync(g_dev_err, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
         cudaStreamSynchronize(st);
     }
+    // the Chebyshev-Fourier tensor-core kernel's word (a bounded wait ran out)
+    int vc = 0;
+    if (cf_tc_err_take(st, &vc))
+        return set_err(WC_ERR_CUDA, "reading the tensor-core error word failed: %s",
+                       cudaGetErrorString(cudaGetLastError()));
+    if (vc && !v) v = vc;
     // the object kernels' word: a batch whose word cannot be read is failed,
     // never reported as good (a union-find cap hit would otherwise be lost)
     int vo = 0;
@@ -201,6 +207,18 @@ int features_prepare(FeatureSetup &fs) {
         }
         fs.off["cf_jobs"] = fs.put_copy(cj.data(), cj.size() * sizeof(CFJob));
         fs.off["cf_part"] = fs.ws_take(cj.size() * (size_t)nchunk_max * 2 * 529 * sizeof(double));
+        // the mixed form's tensor-core sums: every plane of one size, 23 x 23 coefficients
+        bool one_size = fs.prec == WC_PREC_MIXED && fs.cf_tc;
+        for (auto &c : cj) one_size = one_size && c.new_w == cj[0].new_w && c.new_h == cj[0].new_h;
+        if (one_size && std::min(cj[0].new_w, cj[0].new_h) >= 23) {
+            const CFTcPlan tp = cf_tc_plan((int)cj.size(), cj[0].new_h, cj[0].new_w);
+            fs.cf_tc_plan = tp;
+            fs.val["cf_tc"] = 1;
+            fs.off["cf_tc_a"] = fs.ws_take(tp.digA_bytes);
+            fs.off["cf_tc_b"] = fs.ws_take(tp.digB_bytes);
+            fs.off["cf_tc_p"] = fs.ws_take(tp.partial_bytes);
+            fs.off["cf_tc_u"] = fs.ws_take(tp.uA_bytes);
+        }
         fs.val["cf_nchunk"] = nchunk_max;
         fs.val["cf_cntx"] = max_cnt_x;
         fs.val["cf_w"] = max_w;
@@ -503,11 +521,17 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early) {
     {
         Ctx &c = fr.lanes[1];
         ProfScope ps(c, "Chebyshev-Fourier Coefficients");
+        CFTcBufs tb{};
+        const bool tc = fs.val.count("cf_tc") && fs.val["cf_tc"];
+        if (tc)
+            tb = CFTcBufs{fr.ws + fs.off["cf_tc_a"], fr.ws + fs.off["cf_tc_b"], (double *)(fr.ws + fs.off["cf_tc_p"]),
+                          (double *)(fr.ws + fs.off["cf_tc_u"])};
         if (nj(A_CHEBFOURIER))
         launch_chebfourier(c, fr.arena, fr.planes, jobs(A_CHEBFOURIER), nj(A_CHEBFOURIER),
                            maxw_of(P, fj[A_CHEBFOURIER]), maxh_of(P, fj[A_CHEBFOURIER]), (int)fs.val["cf_cntx"],
                            (int)fs.val["cf_w"], (int)fs.val["cf_h"], (const CFJob *)(fr.meta + fs.off["cf_jobs"]), fr.tabs,
-                           (double *)fr.ws, (double *)(fr.ws + fs.off["cf_part"]), (int)fs.val["cf_nchunk"], fr.feat);
+                           (double *)fr.ws, (double *)(fr.ws + fs.off["cf_part"]), (int)fs.val["cf_nchunk"], fr.feat,
+                           tc ? &fs.cf_tc_plan : nullptr, tc ? &tb : nullptr);
     }
     {
         Ctx &c = fr.lanes[2];

@@ -563,7 +563,7 @@ __global__ void __launch_bounds__(192) k_cf_accum_f32(const CFJob *__restrict__ 
 }
 
 __global__ void k_cf_finish(const FJob *__restrict__ jobs, const CFJob *__restrict__ cj, const double *__restrict__ part,
-                            int nchunk_max, double *__restrict__ feat) {
+                            int nchunk_max, int nch_force, double *__restrict__ feat) {
     __shared__ double co[529];
     __shared__ double sh[32];
     __shared__ unsigned int bins[32];
@@ -574,7 +574,7 @@ __global__ void k_cf_finish(const FJob *__restrict__ jobs, const CFJob *__restri
     if (N > Nmax) N = Nmax;
     const int NN = 2 * N + 1, NO = NN * NN;
     const long long npix = (long long)C.new_w * C.new_h;
-    const int nch = (int)((npix + CF_CHUNK - 1) / CF_CHUNK);
+    const int nch = nch_force > 0 ? nch_force : (int)((npix + CF_CHUNK - 1) / CF_CHUNK);
     double lo = 10E200, hi = -10E200;
     for (int o = threadIdx.x; o < NO; o += blockDim.x) {
         double sr = 0, si = 0;
@@ -602,7 +602,8 @@ __global__ void k_cf_finish(const FJob *__restrict__ jobs, const CFJob *__restri
 
 void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw,
                         int maxh, int max_cnt_x, int max_src_w, int max_src_h, const CFJob *cj, const double *tabs,
-                        double *ws, double *part, int nchunk_max, double *feat) {
+                        double *ws, double *part, int nchunk_max, double *feat, const CFTcPlan *tcp,
+                        const CFTcBufs *tcb) {
     if (njobs <= 0) return;
     dim3 b(32, 8);
     WC_LAUNCH(c);
@@ -616,20 +617,26 @@ void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const 
         cudaFuncSetAttribute(k_cf_accum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
-    WC_LAUNCH(c);
-    if (c.prec == WC_PREC_MIXED) {
-        const int sm32 = 3 * CF32_PX * 24 * sizeof(float);
-        static bool attr32 = false;
-        if (!attr32) {
-            cudaFuncSetAttribute(k_cf_accum_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32);
-            attr32 = true;
+    // the mixed form: the tensor-core sums where every plane has one size (the
+    // host planned their buffers), else FP32 SIMT sums
+    const bool tc = c.prec == WC_PREC_MIXED && tcp && tcb &&
+                    launch_cf_tc(c, cj, njobs, max_src_h, max_src_w, ws, *tcp, *tcb, part, nchunk_max);
+    if (!tc) {
+        WC_LAUNCH(c);
+        if (c.prec == WC_PREC_MIXED) {
+            const int sm32 = 3 * CF32_PX * 24 * sizeof(float);
+            static bool attr32 = false;
+            if (!attr32) {
+                cudaFuncSetAttribute(k_cf_accum_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32);
+                attr32 = true;
+            }
+            k_cf_accum_f32<<<dim3(nchunk_max, njobs), 192, sm32, c.st>>>(cj, ws, part, nchunk_max);
+        } else {
+            k_cf_accum<<<dim3(nchunk_max, njobs), 256, sm, c.st>>>(cj, ws, part, nchunk_max);
         }
-        k_cf_accum_f32<<<dim3(nchunk_max, njobs), 192, sm32, c.st>>>(cj, ws, part, nchunk_max);
     }
-    else
-        k_cf_accum<<<dim3(nchunk_max, njobs), 256, sm, c.st>>>(cj, ws, part, nchunk_max);
     WC_LAUNCH(c);
-    k_cf_finish<<<njobs, 256, 0, c.st>>>(jobs, cj, part, nchunk_max, feat);
+    k_cf_finish<<<njobs, 256, 0, c.st>>>(jobs, cj, part, nchunk_max, tc ? 1 : 0, feat);
 }
 
 }  // namespace wc

@@ -56,6 +56,7 @@
 
 #include "../../include/wndcharm_gb300.h"
 #include "kcommon.cuh"
+#include "ktcgen05.cuh"
 #include "wc_features.h"
 
 namespace wc {
@@ -74,7 +75,6 @@ constexpr int STAGE_BYTES = S * (A_SLICE + B_SLICE);
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
 constexpr int THREADS = 192;  // warp 0 TMA, warp 1 MMA + TMEM, warps 2..5 epilogue
 constexpr int MAX_K = 511;    // acc0 / acc1 exact below this many features
-constexpr long long WAIT_CAP = 1LL << 24;
 
 // digit pairs (i, j) and their accumulator; first[] marks the first MMA
 // into each accumulator (it overwrites instead of accumulating)
@@ -83,85 +83,24 @@ __constant__ unsigned char c_pj[13] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 3, 2, 1};
 __constant__ unsigned char c_pa[13] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 3, 3, 3};
 __constant__ unsigned char c_pf[13] = {1, 1, 0, 1, 0, 0, 1, 0, 0, 0, 0, 0, 0};
 
-// instruction descriptor, kind::f16: D = F32 (bits 4-5), A = B = BF16 (bits
-// 7-9, 10-12), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+constexpr uint32_t IDESC = tcg::idesc_bf16_f32(M, N);
+using tcg::mbar_arrive;
+using tcg::mbar_expect_tx;
+using tcg::mbar_init;
+using tcg::mbar_wait;
+using tcg::mma_commit;
+using tcg::sdesc;
+using tcg::smem_u32;
+using tcg::tc_fence_after;
+using tcg::tc_fence_before;
+using tcg::tma_load_3d;
+using tcg::tmem_ld16;
+using tcg::tmem_ld_wait;
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    tcg::mma_bf16(tmem_d, a, b, IDESC, accumulate);
+}
 
 __device__ int g_err_tc = 0;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
-// 128 bytes in 8-row (1024-byte) atoms; start address advanced by 32 bytes
-// per 16-element K step inside the swizzle row
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, bits 0-13
-    d |= (uint64_t)1 << 16;                     // leading byte offset (unused with this swizzle)
-    d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 bytes
-    d |= (uint64_t)1 << 46;                     // descriptor version
-    d |= (uint64_t)2 << 61;                     // 128-byte swizzle
-    return d;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t a) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
-}
-// bounded wait for the phase with the given parity to complete
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
-    for (long long i = 0; i < WAIT_CAP; i++) {
-        uint32_t ok;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return true;
-        if (i > 32) __nanosleep(64);
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
-            dst),
-        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-            tmem_d),
-        "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// 16 consecutive 32-bit TMEM columns of this thread's lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
-        "[%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // error-free transformations (explicit roundings: no contraction)
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
@@ -513,31 +452,9 @@ int set_err(int code, const char *fmt, ...);
 
 namespace {
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
-    return fn;
-}
-
 // 3-D map over the digit planes [4][rows_pad][Kp] (bf16), box 64 x box_rows x 4
 int digit_map(CUtensorMap *m, void *base, long long rows_pad, int Kp, int box_rows) {
-    auto fn = encode_fn();
-    if (!fn) return set_err(WC_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows_pad, 4};
-    const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows_pad * Kp * 2};
-    const cuuint32_t box[3] = {(cuuint32_t)tc::KB, (cuuint32_t)box_rows, 4};
-    const cuuint32_t es[3] = {1, 1, 1};
-    const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return set_err(WC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-    return WC_OK;
+    return tcg::digit_map_3d(m, base, rows_pad, Kp, box_rows, tc::KB, 4);
 }
 
 // device buffers of one classification, freed together

@@ -67,9 +67,27 @@ struct CFJob {
     int nchunk;
     double dx;
 };
+// k_cf_tc.cu: the mixed form's Chebyshev-Fourier sums on the tensor cores for
+// planes of one size (1058 basis columns padded to 17 tiles of 64)
+#define CF_TC_COLS 1088
+struct CFTcPlan {
+    long long K_pad = 0, M_pad = 0;
+    int nchunk = 0;
+    size_t digA_bytes = 0, digB_bytes = 0, partial_bytes = 0, uA_bytes = 0;
+};
+struct CFTcBufs {
+    void *digA, *digB;
+    double *partial, *uA;
+};
+CFTcPlan cf_tc_plan(int njobs, int m, int n);
+bool launch_cf_tc(Ctx &c, const CFJob *cj, int njobs, int m, int n, const double *ws, const CFTcPlan &p,
+                  const CFTcBufs &b, double *part, int nchunk_max);
+int cf_tc_err_take(cudaStream_t st, int *v);
+// tcp / tcb: the tensor-core form's plan and buffers (mixed form, one size), or null
 void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, int maxw,
                         int maxh, int max_cnt_x, int max_src_w, int max_src_h, const CFJob *cj, const double *tabs,
-                        double *ws, double *part, int nchunk_max, double *feat);
+                        double *ws, double *part, int nchunk_max, double *feat, const CFTcPlan *tcp = nullptr,
+                        const CFTcBufs *tcb = nullptr);
 
 // k_tamura.cu
 struct TamJob {

@@ -25,6 +25,9 @@ struct FeatureSetup {
     std::map<std::string, long long> val;
     std::vector<GabJob> gab_jobs;
     std::vector<GabSize> gab_sizes;
+    int prec = 0;   // the engine's form (WC_PREC_*)
+    int cf_tc = 1;  // mixed form: Chebyshev-Fourier sums on the tensor cores where every plane has one size
+    CFTcPlan cf_tc_plan;
 };
 
 #define WC_LANES 6

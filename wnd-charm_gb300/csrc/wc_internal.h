@@ -134,6 +134,8 @@ struct Opts {
     // union-find iterations allowed per pixel link in the object labelling;
     // 0: the plane's pixel count (a bound no correct run reaches)
     long long union_find_cap = 0;
+    // mixed form: Chebyshev-Fourier sums on the tensor cores (planes of one size)
+    int cf_tc = 1;
 };
 
 // Online autotuner of launch shapes (the engine's own): a stage with several

@@ -1,8 +1,8 @@
 """Chebyshev-Fourier coefficients on the tensor cores (the mixed form, planes
 of one size): against the oracle within the mixed form's stated rule for the
 group (at most 2 single-count moves per 32-bin histogram), on whole 512 x 512
-workload images (downsampled to 300 x 300 as the reference does) and on small
-images of one size; and the FP32 SIMT form (option cf_tensor_cores = 0) on the
+workload images and on 320 x 320 images (all their planes downsampled to
+300 x 300, as the reference does); and the FP32 SIMT form (option cf_tensor_cores = 0) on the
 same images under the same rule.  A batch of mixed sizes takes the SIMT form."""
 import numpy as np
 import pytest
@@ -43,7 +43,9 @@ def _check(eng, plan, imgs):
     return launches, moves
 
 
-@pytest.mark.parametrize("sizes", [[(512, 512)] * 3, [(96, 80)] * 5])
+# square images of 300 x 300 or more: every plane (the Wavelet ones included)
+# is downsampled to 300 x 300, one size for the whole batch
+@pytest.mark.parametrize("sizes", [[(512, 512)] * 3, [(320, 320)] * 4])
 def test_tensor_core_sums_within_the_rule(sizes):
     import wndcharm
     from wndcharm import synth

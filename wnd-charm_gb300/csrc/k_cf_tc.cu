@@ -33,27 +33,28 @@
 namespace wc {
 namespace cft {
 
-constexpr int M = 128, N = 64, KB = 64, S = 3, NACC = 3, STAGES = 2;
+constexpr int M = 128, N = 64, KB = 64, SA = 4, SB = 3, NACC = 4, STAGES = 2, NPAIR = 9;
 constexpr int A_SLICE = M * KB * 2;  // 16 KB
 constexpr int B_SLICE = N * KB * 2;  // 8 KB
-constexpr int STAGE_BYTES = S * (A_SLICE + B_SLICE);
+constexpr int STAGE_BYTES = SA * A_SLICE + SB * B_SLICE;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int THREADS = 192;
 constexpr int CHUNK_KB = 16;  // 1024 pixels per chunk
 constexpr uint32_t IDESC = tcg::idesc_bf16_f32(M, N);
 
-// digit pairs (i, j), their accumulator, and whether the pair is the first
-// into it (it then overwrites on a chunk's first K step)
-__constant__ unsigned char c_pi[6] = {0, 0, 1, 0, 1, 2};
-__constant__ unsigned char c_pj[6] = {0, 1, 0, 2, 1, 0};
-__constant__ unsigned char c_pa[6] = {0, 1, 1, 2, 2, 2};
-__constant__ unsigned char c_pf[6] = {1, 1, 0, 1, 0, 0};
+// digit pairs (i of the pixel, j of the basis) with i + j <= 3, their
+// accumulator i + j, and whether the pair is the first into it (it then
+// overwrites on a chunk's first K step)
+__constant__ unsigned char c_pi[NPAIR] = {0, 0, 1, 0, 1, 2, 1, 2, 3};
+__constant__ unsigned char c_pj[NPAIR] = {0, 1, 0, 2, 1, 0, 2, 1, 0};
+__constant__ unsigned char c_pa[NPAIR] = {0, 1, 1, 2, 2, 2, 3, 3, 3};
+__constant__ unsigned char c_pf[NPAIR] = {1, 1, 0, 1, 0, 0, 1, 0, 0};
 
 __device__ int g_err_cf = 0;
 
 struct Params {
     int M_pad, kb_total, nchunk;
-    const double *__restrict__ uA;  // per plane row: its digit scale times the basis' (2^-7)
+    const double *__restrict__ uA;  // [nchunk][M_pad]: each chunk's digit scale times the basis' (2^-7)
     double *__restrict__ partial;   // [nchunk][M_pad][CF_TC_COLS]
 };
 
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 for (int kb = kb0; kb < kb1; kb++, it++) {
                     const int st = it & 1;
                     if (!mbar_wait(empty0 + 8 * st, ((it >> 1) & 1) ^ 1)) { bad = true; break; }
-                    const uint32_t sA = smem_u32(smem + st * STAGE_BYTES), sB = sA + S * A_SLICE;
+                    const uint32_t sA = smem_u32(smem + st * STAGE_BYTES), sB = sA + SA * A_SLICE;
                     mbar_expect_tx(full0 + 8 * st, STAGE_BYTES);
                     tma_load_3d(sA, &mapA, kb * KB, mb * M, 0, full0 + 8 * st);
                     tma_load_3d(sB, &mapB, kb * KB, tile * N, 0, full0 + 8 * st);
@@ -118,11 +119,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const int st = it & 1;
                     if (!mbar_wait(full0 + 8 * st, (it >> 1) & 1)) { bad = true; break; }
                     tc_fence_after();
-                    const uint32_t sA = smem_u32(smem + st * STAGE_BYTES), sB = sA + S * A_SLICE;
+                    const uint32_t sA = smem_u32(smem + st * STAGE_BYTES), sB = sA + SA * A_SLICE;
 #pragma unroll
                     for (int ks = 0; ks < KB / 16; ks++) {
 #pragma unroll
-                        for (int p = 0; p < 6; p++) {
+                        for (int p = 0; p < NPAIR; p++) {
                             const uint64_t da = sdesc(sA + c_pi[p] * A_SLICE + ks * 32);
                             const uint64_t db = sdesc(sB + c_pj[p] * B_SLICE + ks * 32);
                             const uint32_t td = tmem + (uint32_t)((buf * NACC + c_pa[p]) * N);
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ---- epilogue: warps 2..5; warp w reads TMEM lanes 32 (w % 4) ..
         const int q = warp & 3;
         const int row = mb * M + q * 32 + lane;
-        const double scale = P.uA[row];
+        const double scale = P.uA[(long long)ch * P.M_pad + row];
         double *out = P.partial + ((long long)ch * P.M_pad + row) * CF_TC_COLS;
         const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
         for (int tile = 0; tile < ntiles; tile++) {
@@ -150,16 +151,18 @@ __global__ void __launch_bounds__(THREADS, 1)
             tc_fence_after();
 #pragma unroll 1
             for (int c0 = 0; c0 < N; c0 += 16) {
-                float a0[16], a1[16], a2[16];
+                float a0[16], a1[16], a2[16], a3[16];
                 const uint32_t base = lane_addr + (uint32_t)(buf * NACC * N + c0);
                 __syncwarp();
                 tmem_ld16(base, a0);
                 tmem_ld16(base + N, a1);
                 tmem_ld16(base + 2 * N, a2);
+                tmem_ld16(base + 3 * N, a3);
                 tmem_ld_wait();
 #pragma unroll
                 for (int i = 0; i < 16; i++)
-                    out[tile * N + c0 + i] = (((double)a0[i] + (double)a1[i]) + (double)a2[i]) * scale;
+                    out[tile * N + c0 + i] =
+                        ((((double)a0[i] + (double)a1[i]) + (double)a2[i]) + (double)a3[i]) * scale;
             }
             tc_fence_before();
             __syncwarp();
@@ -173,25 +176,28 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
 }
 
-// a / u (|a / u| <= 128) into three digits q_i 2^-8i, each exact in bf16
-__device__ __forceinline__ void cf_digits(double a, __nv_bfloat16 *d0, __nv_bfloat16 *d1, __nv_bfloat16 *d2) {
-    const double q0 = rint(a);
-    double r = (a - q0) * 256.0;
-    const double q1 = rint(r);
-    r = (r - q1) * 256.0;
-    const double q2 = rint(r);
-    *d0 = __float2bfloat16_rn((float)q0);
-    *d1 = __float2bfloat16_rn((float)ldexp(q1, -8));
-    *d2 = __float2bfloat16_rn((float)ldexp(q2, -16));
+// a (|a| < 128) into nd balanced digits q_i 2^-8i (|q_i| <= 128) at d[0],
+// d[step], ..., each exact in bf16: a is rounded once to the fixed point
+// X = RN(a 2^(8 nd - 8)), and the digits come from X by integer shifts (the
+// integer pipe, not the FP64 one)
+__device__ __forceinline__ void cf_digits(double a, __nv_bfloat16 *d, long long step, int nd) {
+    long long X = __double2ll_rn(ldexp(a, 8 * nd - 8));
+    for (int i = 0; i < nd; i++) {
+        const int sh = 8 * (nd - 1 - i);
+        const long long q = sh ? (X + (1LL << (sh - 1))) >> sh : X;  // arithmetic shift: floor
+        X -= q * (1LL << sh);
+        d[i * step] = __float2bfloat16_rn(ldexpf((float)q, -8 * i));
+    }
 }
 
-// the basis digits of one size: a thread per pixel k (x-major, k = x m + y, as
-// the reference walks them); pixels off the unit disc (the reference's FP64
-// test, rounded as k_cf_accum rounds it) and padding stay 0 (memset)
+// the basis digits of one size: a thread per pixel k = y n + x (row-major; the
+// order of the K dimension is the GEMM's own, the same for both operands);
+// pixels off the unit disc (the reference's FP64 test, rounded as k_cf_accum
+// rounds it) and padding stay 0 (memset)
 __global__ void __launch_bounds__(128) k_cf_tc_basis(int m, int n, long long K_pad, __nv_bfloat16 *__restrict__ dig) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= (long long)m * n) return;
-    const long long x = k / m, y = k - x * m;
+    const long long y = k / n, x = k - y * n;
     const double tn = 2.0 / ((double)n - 1), tm = 2.0 / ((double)m - 1);
     const double xi = __dadd_rn(-1.0, __dmul_rn((double)x, tn)), yi = __dadd_rn(-1.0, __dmul_rn((double)y, tm));
     const double r = sqrt(__dadd_rn(__dmul_rn(xi, xi), __dmul_rn(yi, yi)));
@@ -211,31 +217,44 @@ __global__ void __launch_bounds__(128) k_cf_tc_basis(int m, int n, long long K_p
         for (int a = 0; a < 23; a++) {
             const int o = im * 23 + a;
             __nv_bfloat16 *p = dig + (long long)(2 * o) * K_pad + k;
-            cf_digits(fc * T[a] * 128.0, p, p + plane, p + 2 * plane);
-            p += K_pad;
-            cf_digits(fs * T[a] * 128.0, p, p + plane, p + 2 * plane);
+            cf_digits(fc * T[a] * 128.0, p, plane, SB);
+            cf_digits(fs * T[a] * 128.0, p + K_pad, plane, SB);
         }
     }
 }
 
-// each plane's digit scale: the power of two u with max |I| / u in (64, 128]
-// (1 for a zero plane); uA[row] = u 2^-7 (the basis' scale folded in)
-__global__ void k_cf_tc_scale(const CFJob *__restrict__ cj, const double *__restrict__ ws, double *__restrict__ uA) {
+// the digit scale of every (plane, chunk of 1024 pixels): the power of two u
+// with max |I| / u in [64, 128) over the chunk (1 for zeros); uA[ch][row] =
+// u 2^-7 (the basis' scale folded in).  A scale per chunk keeps a plane's
+// small values (most of a Chebyshev or Fourier plane) at 32 bits of their
+// own chunk's largest.
+__global__ void k_cf_tc_scale(const CFJob *__restrict__ cj, const double *__restrict__ ws, long long M_pad,
+                              double *__restrict__ uA) {
     __shared__ double sh[32];
-    const CFJob C = cj[blockIdx.x];
+    const int row = blockIdx.y, ch = blockIdx.x;
+    const CFJob C = cj[row];
+    const int m = C.new_h, n = C.new_w;
     const double *img = ws + C.src_ws;
-    const long long npix = (long long)C.new_w * C.new_h;
-    double mx = 0;
-    for (long long i = threadIdx.x; i < npix; i += blockDim.x) mx = fmax(mx, fabs(img[i]));
+    const long long k0 = (long long)ch * CHUNK_KB * KB, k1 = min((long long)m * n, k0 + CHUNK_KB * KB);
+    double mx = 0, bad = 0;
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const double v = img[k];
+        if (isfinite(v)) mx = fmax(mx, fabs(v));
+        else bad = 1;
+    }
     mx = block_max(mx, sh);
+    bad = block_max(bad, sh);
     if (threadIdx.x == 0) {
         int e = 0;
-        if (mx > 0 && isfinite(mx)) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
-        uA[blockIdx.x] = mx > 0 && isfinite(mx) ? ldexp(1.0, e - 7) * 0x1p-7 : 0x1p-7;
+        if (mx > 0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+        // a non-finite pixel makes every coefficient of the plane NaN, as the
+        // FP64 sums would: the chunk's scale is NaN
+        uA[(long long)ch * M_pad + row] = bad ? __longlong_as_double(0x7ff8000000000000LL)
+                                              : (mx > 0 ? ldexp(1.0, e - 7) * 0x1p-7 : 0x1p-7);
     }
 }
 
-// the planes' digits, [3][M_pad][K_pad], pixel k = x m + y of plane row
+// the planes' digits, [4][M_pad][K_pad], pixel k = y n + x of plane row
 __global__ void k_cf_tc_pixels(const CFJob *__restrict__ cj, int njobs, const double *__restrict__ ws,
                                const double *__restrict__ uA, long long K_pad, long long M_pad,
                                __nv_bfloat16 *__restrict__ dig) {
@@ -244,13 +263,13 @@ __global__ void k_cf_tc_pixels(const CFJob *__restrict__ cj, int njobs, const do
     const CFJob C = cj[row];
     const int m = C.new_h, n = C.new_w;
     const double *img = ws + C.src_ws;
-    const double inv = 1.0 / (uA[row] * 0x1p7);  // a power of two: exact
     const long long plane = M_pad * K_pad;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < (long long)m * n;
          k += (long long)gridDim.x * blockDim.x) {
-        const long long x = k / m, y = k - x * m;
-        __nv_bfloat16 *p = dig + (long long)row * K_pad + k;
-        cf_digits(img[y * n + x] * inv, p, p + plane, p + 2 * plane);
+        const double u = uA[(k / (CHUNK_KB * KB)) * M_pad + row];
+        const double inv = isfinite(u) ? 1.0 / (u * 0x1p7) : 0.0;  // a power of two: exact
+        const double v = img[k];
+        cf_digits(isfinite(v) ? v * inv : 0.0, dig + (long long)row * K_pad + k, plane, SA);
     }
 }
 
@@ -286,10 +305,10 @@ CFTcPlan cf_tc_plan(int njobs, int m, int n) {
     p.M_pad = ((long long)njobs + cft::M - 1) / cft::M * cft::M;
     const int kb_total = (int)(p.K_pad / cft::KB);
     p.nchunk = (kb_total + cft::CHUNK_KB - 1) / cft::CHUNK_KB;
-    p.digA_bytes = (size_t)3 * p.M_pad * p.K_pad * 2;
-    p.digB_bytes = (size_t)3 * CF_TC_COLS * p.K_pad * 2;
+    p.digA_bytes = (size_t)cft::SA * p.M_pad * p.K_pad * 2;
+    p.digB_bytes = (size_t)cft::SB * CF_TC_COLS * p.K_pad * 2;
     p.partial_bytes = (size_t)p.nchunk * p.M_pad * CF_TC_COLS * 8;
-    p.uA_bytes = (size_t)p.M_pad * 8;
+    p.uA_bytes = (size_t)p.nchunk * p.M_pad * 8;
     return p;
 }
 
@@ -301,8 +320,8 @@ bool launch_cf_tc(Ctx &c, const CFJob *cj, int njobs, int m, int n, const double
                   const CFTcBufs &b, double *part, int nchunk_max) {
     using namespace cft;
     CUtensorMap mapA, mapB;
-    if (tcg::digit_map_3d(&mapA, b.digA, p.M_pad, p.K_pad, M, KB, S) != WC_OK ||
-        tcg::digit_map_3d(&mapB, b.digB, CF_TC_COLS, p.K_pad, N, KB, S) != WC_OK) {
+    if (tcg::digit_map_3d(&mapA, b.digA, p.M_pad, p.K_pad, M, KB, SA) != WC_OK ||
+        tcg::digit_map_3d(&mapB, b.digB, CF_TC_COLS, p.K_pad, N, KB, SB) != WC_OK) {
         cudaGetLastError();
         return false;
     }
@@ -316,7 +335,7 @@ bool launch_cf_tc(Ctx &c, const CFJob *cj, int njobs, int m, int n, const double
     cudaMemsetAsync(b.uA, 0, p.uA_bytes, c.st);
     *c.launches += 5;
     k_cf_tc_basis<<<(unsigned)(((long long)m * n + 127) / 128), 128, 0, c.st>>>(m, n, p.K_pad, (__nv_bfloat16 *)b.digB);
-    k_cf_tc_scale<<<njobs, 256, 0, c.st>>>(cj, ws, b.uA);
+    k_cf_tc_scale<<<dim3((unsigned)p.nchunk, njobs), 256, 0, c.st>>>(cj, ws, p.M_pad, b.uA);
     k_cf_tc_pixels<<<dim3(64, njobs), 256, 0, c.st>>>(cj, njobs, ws, b.uA, p.K_pad, p.M_pad,
                                                       (__nv_bfloat16 *)b.digA);
     Params P{(int)p.M_pad, (int)(p.K_pad / KB), p.nchunk, b.uA, b.partial};

@@ -67,50 +67,88 @@ __global__ void __launch_bounds__(256) k_rs_scan(const SortSeg *__restrict__ seg
     for (int t = 0; t < ntiles; t++) c[t] += base[d];
 }
 
+// One tile of RS_TILE keys per CTA: the tile is ranked by digit in shared
+// memory (warp w takes keys [512 w, 512 w + 512) in 16 rounds of 32, equal
+// digits ranked by lane with __match_any_sync, per-warp digit counters), so
+// its keys land there in digit order with the tile's order kept among equal
+// digits; then consecutive threads write each digit's run to consecutive
+// places (tbase[d] from the scan of every tile's counts): a stable pass with
+// coalesced writes.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(unsigned long long *__restrict__ keys, unsigned long long *__restrict__ tmp,
                                                            const SortSeg *__restrict__ seg, const int *__restrict__ cur,
                                                            const unsigned int *__restrict__ cnt, const int *__restrict__ skip,
                                                            int max_tiles, int shift) {
-    extern __shared__ unsigned short pre[];  // [RS_THREADS][256]
-    __shared__ unsigned int tbase[256];
+    constexpr int NW = RS_THREADS / 32, PER_W = RS_TILE / NW;  // 8 warps, 512 keys each
+    __shared__ unsigned long long sk[RS_TILE];
+    __shared__ unsigned int wcnt[NW][256];
+    __shared__ unsigned int tbase[256], lstart[256], scan[RS_THREADS];
     const SortSeg S = seg[blockIdx.y];
     const long long t0 = (long long)blockIdx.x * RS_TILE;
     if (t0 >= S.n || skip[blockIdx.y]) return;
     const int c = cur[blockIdx.y];
-    const unsigned long long *src = (c ? tmp : keys) + S.off;
+    const unsigned long long *src = (c ? tmp : keys) + S.off + t0;
     unsigned long long *dst = (c ? keys : tmp) + S.off;
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int ntile = (int)min((long long)RS_TILE, S.n - t0);
+    const unsigned lt = (1u << lane) - 1;
+    for (int i = t; i < NW * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
     tbase[t] = cnt[((long long)blockIdx.y * 256 + t) * max_tiles + blockIdx.x];
-    unsigned short *row = pre + (long long)t * 256;
-    for (int d = 0; d < 256; d++) row[d] = 0;
-    unsigned long long k[RS_ITEMS];
-    const long long k0 = t0 + (long long)t * RS_ITEMS;
+    __syncthreads();
+    unsigned long long k[PER_W / 32];
+    unsigned int off[PER_W / 32];
 #pragma unroll
-    for (int i = 0; i < RS_ITEMS; i++) {
-        const long long idx = k0 + i;
-        k[i] = idx < S.n ? src[idx] : 0;
-        if (idx < S.n) row[(k[i] >> shift) & 255]++;
+    for (int r = 0; r < PER_W / 32; r++) {
+        const int idx = w * PER_W + r * 32 + lane;
+        const bool ok = idx < ntile;
+        k[r] = ok ? src[idx] : 0ull;
+        const unsigned d = ok ? ((unsigned)(k[r] >> shift) & 255u) : 256u + lane;  // idle lanes: unique non-digits
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if (ok && lane == leader) {
+            base = wcnt[w][d];
+            wcnt[w][d] = base + __popc(peers);
+        }
+        base = __shfl_sync(0xffffffffu, base, leader);
+        off[r] = base + __popc(peers & lt);
+        __syncwarp();
     }
     __syncthreads();
-    {  // exclusive scan over threads, one digit per thread
-        unsigned int run = 0;
-        for (int u = 0; u < RS_THREADS; u++) {
-            const unsigned short v = pre[(long long)u * 256 + t];
-            pre[(long long)u * 256 + t] = (unsigned short)run;
+    {  // digit t: its warps' counts into bases, and its total
+        unsigned run = 0;
+        for (int u = 0; u < NW; u++) {
+            const unsigned v = wcnt[u][t];
+            wcnt[u][t] = run;
             run += v;
+        }
+        scan[t] = run;
+    }
+    __syncthreads();
+    {  // exclusive scan of the digit totals (Hillis-Steele over 256 values)
+        unsigned v = scan[t];
+        for (int o = 1; o < 256; o <<= 1) {
+            const unsigned y = t >= o ? scan[t - o] : 0u;
+            __syncthreads();
+            v += y;
+            scan[t] = v;
+            __syncthreads();
+        }
+        lstart[t] = t ? scan[t - 1] : 0u;  // the inclusive scan is complete after the loop's last barrier
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < PER_W / 32; r++) {
+        const int idx = w * PER_W + r * 32 + lane;
+        if (idx < ntile) {
+            const unsigned d = (unsigned)(k[r] >> shift) & 255u;
+            sk[lstart[d] + wcnt[w][d] + off[r]] = k[r];
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < RS_ITEMS; i++) {
-        const long long idx = k0 + i;
-        if (idx >= S.n) break;
-        const int d = (int)((k[i] >> shift) & 255);
-        int same = 0;
-#pragma unroll
-        for (int j = 0; j < RS_ITEMS; j++)
-            if (j < i && (int)((k[j] >> shift) & 255) == d) same++;
-        dst[tbase[d] + row[d] + same] = k[i];
+    for (int i = t; i < ntile; i += RS_THREADS) {
+        const unsigned long long key = sk[i];
+        const unsigned d = (unsigned)(key >> shift) & 255u;
+        dst[tbase[d] + (unsigned)i - lstart[d]] = key;
     }
 }
 
@@ -150,11 +188,6 @@ void launch_sort_planes(Ctx &c, const double *arena, const Plane *planes, const 
     unsigned int *cnt = (unsigned int *)scratch;
     int *cur = (int *)(cnt + (size_t)nseg * 256 * max_tiles);
     int *skip = cur + nseg;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_rs_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, RS_THREADS * 256 * 2);
-        attr = true;
-    }
     WC_LAUNCH(c);
     k_rs_keys<<<dim3(64, nseg), 256, 0, c.st>>>(arena, planes, ids, seg, keys, cur);
     for (int pass = 0; pass < 8; pass++) {
@@ -164,8 +197,7 @@ void launch_sort_planes(Ctx &c, const double *arena, const Plane *planes, const 
         WC_LAUNCH(c);
         k_rs_scan<<<nseg, 256, 0, c.st>>>(seg, cnt, skip, max_tiles);
         WC_LAUNCH(c);
-        k_rs_scatter<<<dim3(max_tiles, nseg), RS_THREADS, RS_THREADS * 256 * 2, c.st>>>(keys, tmp, seg, cur, cnt, skip,
-                                                                                      max_tiles, shift);
+        k_rs_scatter<<<dim3(max_tiles, nseg), RS_THREADS, 0, c.st>>>(keys, tmp, seg, cur, cnt, skip, max_tiles, shift);
         WC_LAUNCH(c);
         k_rs_flip<<<(nseg + 255) / 256, 256, 0, c.st>>>(cur, skip, nseg);
     }

@@ -306,10 +306,68 @@ __global__ void __launch_bounds__(512) k_fractal(const double *__restrict__ aren
     if (threadIdx.x == 0) feat[J.out + slot] = s / (double)(W * (W - k) + H * (H - k));
 }
 
+// The mixed form, on the FP32 and integer pipes: a CTA per (plane, group of 4
+// lags).  Each pixel is split into a pair of floats from the double's bits
+// (df_split), and so is each partner as it is read; every |I(p) - I(q)| is
+// formed in pairs (two-sum of the highs, the lows added: ~48 bits of the FP64
+// difference) and summed per lag in pairs, then the block's sums are added in
+// FP64 in a fixed order (deterministic).  Four lags per CTA keep the
+// accumulators few and the CTAs per SM many (the chains are latency-bound).
+#define FR_THREADS 512
+#define FR_LAGS 4
+__global__ void __launch_bounds__(FR_THREADS) k_fractal_df(const double *__restrict__ arena, const Plane *__restrict__ planes,
+                                                           const FJob *__restrict__ jobs, double *__restrict__ feat) {
+    __shared__ double red[FR_THREADS / 32][FR_LAGS];
+    const FJob J = jobs[blockIdx.y];
+    const Plane P = planes[J.plane];
+    const int W = P.w, H = P.h;
+    const int K = ((W > H) ? H : W) / 5;
+    int step = K / 20;
+    if (step < 1) step = 1;
+    const int l0 = blockIdx.x * FR_LAGS;
+    int kk[FR_LAGS];
+#pragma unroll
+    for (int l = 0; l < FR_LAGS; l++) {
+        const int k = 1 + (l0 + l) * step;
+        kk[l] = k < K ? k : H + W;  // past the last lag: no pair
+    }
+    const double *p = arena + P.off;
+    df acc[FR_LAGS];
+#pragma unroll
+    for (int l = 0; l < FR_LAGS; l++) acc[l] = {0.f, 0.f};
+    const int n = W * H;  // at most 2^28 pixels
+    for (int i = threadIdx.x; i < n; i += FR_THREADS) {
+        const int y = i / W, x = i - y * W;
+        const df a = df_split(p[i]);
+#pragma unroll
+        for (int l = 0; l < FR_LAGS; l++) {
+            const int k = kk[l];
+            if (y + k < H) acc[l] = df_add(acc[l], df_abs(df_sub(a, df_split(p[i + (long long)k * W]))));
+            if (x + k < W) acc[l] = df_add(acc[l], df_abs(df_sub(a, df_split(p[i + k]))));
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int l = 0; l < FR_LAGS; l++) {
+        double v = df_to_double(acc[l]);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[w][l] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < FR_LAGS) {
+        const int l = threadIdx.x, slot = l0 + l, k = 1 + slot * step;
+        double s = 0;
+        for (int u = 0; u < FR_THREADS / 32; u++) s += red[u][l];
+        if (slot < 20) feat[J.out + slot] = k < K ? s / (double)(W * (W - k) + H * (H - k)) : 0.0;
+    }
+}
+
 void launch_fractal(Ctx &c, const double *arena, const Plane *planes, const FJob *jobs, int njobs, double *feat) {
     if (njobs <= 0) return;
     WC_LAUNCH(c);
-    k_fractal<<<dim3(20, njobs), 512, 0, c.st>>>(arena, planes, jobs, feat);
+    if (c.prec == WC_PREC_MIXED)
+        k_fractal_df<<<dim3(20 / FR_LAGS, njobs), FR_THREADS, 0, c.st>>>(arena, planes, jobs, feat);
+    else k_fractal<<<dim3(20, njobs), 512, 0, c.st>>>(arena, planes, jobs, feat);
 }
 
 // ---------------------------------------------------------------- comb moments

@@ -859,15 +859,18 @@ def main():
     roof = {"stage": dom[0], "stage_ms_alone_per_step": dom[1], "stage_share": dom[1] / tot_prof,
             "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
             "peak_source": "measured" if peaks else "fallback"}
-    # DRAM bytes per image of the stage's kernels: a constant taken from one ncu
-    # capture (dram__bytes_read.sum + dram__bytes_write.sum over the four
-    # k_cheb_gemm launches of a 16-image step of this workload), scaled by the
-    # images of this step; not measured in this run
-    traffic_per_image = {"Chebyshev": 287e6 / 16}
+    # DRAM bytes per image of the stage's kernels: constants taken from one ncu
+    # capture each (dram__bytes_read.sum + dram__bytes_write.sum of the named
+    # kernel on a smaller step of this workload), scaled by the images of this
+    # step; not measured in this run
+    traffic_per_image = {"Chebyshev": (287e6 / 16, "k_cheb_gemm at batch 16 (287 MB DRAM read+write)"),
+                         "Haralick Textures": (6.26e9 / 32, "the real-Schur work queue k_har_qr_queue, the stage's "
+                                                            "largest kernel, at batch 32 (6.26 GB DRAM read+write: "
+                                                            "the matrices exceed the L2)")}
     if dom[0] in traffic_per_image:
-        roof["traffic"] = traffic_per_image[dom[0]] * B
-        roof["traffic_source"] = ("constant: one ncu capture of k_cheb_gemm at batch 16 (287 MB DRAM read+write), "
-                                  "scaled by images; bytes per step")
+        per, what = traffic_per_image[dom[0]]
+        roof["traffic"] = per * B
+        roof["traffic_source"] = "constant: one ncu capture of %s, scaled by images; bytes per step" % what
     if work:
         kind, amt = work
         sec = dom[1] / 1000.0

@@ -236,6 +236,8 @@ int features_prepare(FeatureSetup &fs) {
             t.sum_ws = (long long)(fs.ws_take(n * 8) / 8);
             t.sbest_ws = (long long)(fs.ws_take(n) / 8);
             t.phi_ws = (long long)(fs.ws_take(n * 8) / 8);
+            t.mk_ws = (long long)(fs.ws_take(n * 8) / 8);
+            t.emax_ws = (long long)(fs.ws_take(n * 8) / 8);
             tj.push_back(t);
         }
         fs.off["tam_jobs"] = fs.put_copy(tj.data(), tj.size() * sizeof(TamJob));

@@ -10,6 +10,7 @@
 //     where dH >= 1e-4, 125-bin histogram;
 //   contrast: std / (kurtosis / std^4)^(1/4) from Moments4 (no -3).
 // Output order: hist0, hist1, hist2, contrast, directionality, coarseness.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
@@ -107,8 +108,56 @@ static __device__ __noinline__ double2 tam_dir_slow(const double *__restrict__ n
     return make_double2(dH, dV);
 }
 
+// Coarseness (tamura.cpp:140-190): for k = 1..7 the window means of side
+// 2^k around every pixel position, then per pixel E_h = |mean(x + 2^(k-1)) -
+// mean(x - 2^(k-1))| and E_v the same along y, and the first strict maximum
+// over k, horizontal before vertical.  Every mean serves four pixels (as the
+// right and left, lower and upper window of its neighbours), so it is formed
+// once per position (k_tam_mean, the same operations as efficientLocalMean)
+// and the pixels compare them (k_tam_best), the running maximum kept per
+// pixel between the scales.
+__global__ void __launch_bounds__(256) k_tam_mean(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                                                  const TamJob *__restrict__ tj, double *__restrict__ ws, int k) {
+    const Plane P = planes[jobs[blockIdx.y].plane];
+    const TamJob T = tj[blockIdx.y];
+    const int W = P.w, H = P.h;
+    const long long n = (long long)W * H, len = 1LL << k;
+    const double *S = ws + T.sum_ws;
+    double *mk = ws + T.mk_ws;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long y = i / W, x = i - y * W;
+        mk[i] = local_mean(S, W, H, x, y, len);
+    }
+}
+
+// E values are |differences| (+0 or more, or NaN): compared as bit patterns,
+// NaN never greater, exactly as the double comparison
+__global__ void __launch_bounds__(256) k_tam_best(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
+                                                  const TamJob *__restrict__ tj, double *__restrict__ ws, int k) {
+    const Plane P = planes[jobs[blockIdx.y].plane];
+    const TamJob T = tj[blockIdx.y];
+    const int W = P.w, H = P.h;
+    const long long n = (long long)W * H;
+    const int k2 = 1 << (k - 1);
+    const double *mk = ws + T.mk_ws;
+    long long *emax = (long long *)(ws + T.emax_ws);
+    unsigned char *sb = (unsigned char *)(ws + T.sbest_ws);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int y = (int)(i / W), x = (int)(i - (long long)y * W);
+        long long maxE = k == 1 ? 0 : emax[i];
+        int maxk = k == 1 ? 0 : sb[i];
+        long long eh = 0, ev = 0;
+        if (x + k2 < W && x - k2 >= 0) eh = absdiff_bits(mk[i + k2], mk[i - k2]);
+        if (y + k2 < H && y - k2 >= 0) ev = absdiff_bits(mk[i + (long long)k2 * W], mk[i - (long long)k2 * W]);
+        if (eh > maxE && eh <= 0x7ff0000000000000LL) { maxE = eh; maxk = k; }
+        if (ev > maxE && ev <= 0x7ff0000000000000LL) { maxE = ev; maxk = k; }
+        emax[i] = maxE;
+        sb[i] = (unsigned char)maxk;
+    }
+}
+
 #define TAM_TILE 1024
-// per pixel: best coarseness scale, direction angle; per-CTA partials
+// per pixel: the best coarseness scale's statistics, direction angle; per-CTA partials
 __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                                                    const TamJob *__restrict__ tj, double *__restrict__ ws,
                                                    double *__restrict__ part, int nchunk) {
@@ -119,8 +168,8 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
     const TamJob T = tj[blockIdx.y];
     const int W = P.w, H = P.h;
     const long long n = (long long)W * H;
-    const double *nrm = ws + T.norm_ws, *S = ws + T.sum_ws;
-    unsigned char *sb = (unsigned char *)(ws + T.sbest_ws);
+    const double *nrm = ws + T.norm_ws;
+    const unsigned char *sb = (const unsigned char *)(ws + T.sbest_ws);
     double *phi = ws + T.phi_ws;
     long long ksum = 0;
     int kmin = 1 << 30, kmax = -1;
@@ -130,22 +179,8 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
     const long long i0 = (long long)blockIdx.x * TAM_TILE, i1 = min(n, i0 + TAM_TILE);
     for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int y = (int)(i / W), x = (int)(i - (long long)y * W);
-        // coarseness: first strict maximum over k = 1..7, horizontal before vertical.
-        // E values are |differences| (+0 or more, or NaN): compared as bit
-        // patterns, NaN never greater, exactly as the double comparison
-        long long maxE = 0;
-        int maxk = 0, k2 = 1;
-        for (int k = 1; k <= 7; k++, k2 *= 2) {
-            const long long len = 2 * k2;
-            long long eh = 0, ev = 0;
-            if (x + k2 < W && x - k2 >= 0)
-                eh = absdiff_bits(local_mean(S, W, H, x + k2, y, len), local_mean(S, W, H, x - k2, y, len));
-            if (y + k2 < H && y - k2 >= 0)
-                ev = absdiff_bits(local_mean(S, W, H, x, y + k2, len), local_mean(S, W, H, x, y - k2, len));
-            if (eh > maxE && eh <= 0x7ff0000000000000LL) { maxE = eh; maxk = k; }
-            if (ev > maxE && ev <= 0x7ff0000000000000LL) { maxE = ev; maxk = k; }
-        }
-        sb[i] = (unsigned char)maxk;
+        // coarseness: the best scale k_tam_best left for this pixel
+        const int maxk = sb[i];
         ksum += maxk;
         kmin = min(kmin, maxk);
         kmax = max(kmax, maxk);
@@ -296,6 +331,12 @@ void launch_tamura(Ctx &c, const Plane *planes, const PlaneStats *stats, const d
     const int nchunk = (int)((maxpix + TAM_TILE - 1) / TAM_TILE);
     WC_LAUNCH(c);
     k_tam_prefix<<<njobs, 1024, 0, c.st>>>(arena, planes, stats, jobs, tj, ws);
+    const int gx = (int)std::min<long long>((maxpix + 255) / 256, 256);
+    for (int k = 1; k <= 7; k++) {
+        *c.launches += 2;
+        k_tam_mean<<<dim3(gx, njobs), 256, 0, c.st>>>(planes, jobs, tj, ws, k);
+        k_tam_best<<<dim3(gx, njobs), 256, 0, c.st>>>(planes, jobs, tj, ws, k);
+    }
     WC_LAUNCH(c);
     k_tam_pixel<<<dim3(nchunk, njobs), 256, 0, c.st>>>(planes, jobs, tj, ws, part, nchunk);
     WC_LAUNCH(c);

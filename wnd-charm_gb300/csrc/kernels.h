@@ -92,6 +92,7 @@ void launch_chebfourier(Ctx &c, const double *arena, const Plane *planes, const 
 // k_tamura.cu
 struct TamJob {
     long long norm_ws, sum_ws, sbest_ws, phi_ws;  // offsets in doubles into the workspace
+    long long mk_ws, emax_ws;                     // window means of one scale; each pixel's best E so far
 };
 void launch_tamura(Ctx &c, const Plane *planes, const PlaneStats *stats, const double *arena, const FJob *jobs, int njobs,
                    const TamJob *tj, double *ws, double *part, long long maxpix, double *feat);

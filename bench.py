@@ -571,7 +571,9 @@ GRAD_METRIC = ("test images/sec, WND-5 class-evidence maps (d p_c / d pixel, eve
 GRAD_CONFIG = {"workload": "differentiation: 256 fp32 256x256 blob+grating images in [0, 1], 4 classes, seed 3; "
                            "WND-5 trained on 192, 400 Fisher-selected features of the continuous families "
                            "(Zernike, pixel statistics, fractal, Gini on nonnegative planes); 64 test images",
-               "parallelism": "replicas", "l2": "host buffers through wc_wnd_grad (inputs staged each call)"}
+               "parallelism": "replicas", "l2": "host buffers through wc_wnd_grad (inputs staged each call)",
+               "timing": "host clock around the public call (host images in, host maps out), bracketed by device "
+                         "synchronisation: value and e2e are this one end-to-end measurement"}
 
 
 def run_grad(args, reference=False):
@@ -914,7 +916,8 @@ def main():
             "forms": forms,
             "stages_ms": {n: round(ms, 3) for n, ms, _ in prof},
             "timeline_ms": {n: [round(a, 1), round(b, 1)] for n, a, b in timeline},
-            "stages_alone_ms": {n: round(ms, 3) for n, ms in prof_alone.items()}}
+            "stages_alone_ms": {n: round(ms, 3) for n, ms in prof_alone.items()},
+            "autotuned": {k: v[0] for k, v in eng.tuning().items()}}
     if rank == 0 and not args.no_cpu_baseline:
         nth = os.cpu_count() or 1
         ncpu = min(nth, B)

@@ -451,10 +451,12 @@ int run_batch(wc_engine *E, const Plan &plan, const wc_image_desc *imgs, int n, 
         launch_plane_stats(ctx, arena, dplanes, (int)planes.size(), dstats, NN, early ? 2 : 0);
     }
     // the other families are independent given the planes: fork them onto the
-    // remaining lanes, and join every lane back before the caller's next operation
+    // lanes (lane 3 takes plane scans after its early Gabor work; lane 4 has
+    // nothing that reads a transform), and join every lane back before the
+    // caller's next operation
     CK(cudaEventRecord(E->fork_ev, ctx.st));
     for (int k = 0; k < WC_LANES; k++)
-        if (!early || (k != 3 && k != 4)) CK(cudaStreamWaitEvent(E->lanes[k], E->fork_ev, 0));
+        if (!early || k != 4) CK(cudaStreamWaitEvent(E->lanes[k], E->fork_ev, 0));
     r = features_launch(fs, fr, 1, early);
     for (int k = 0; k < WC_LANES; k++) {
         CK(cudaEventRecord(E->join_ev[k], E->lanes[k]));
@@ -733,11 +735,14 @@ int wc_engine_create(int device, int precision, wc_engine **out) {
     set_radon_table(cs);
     features_init();
     // lane 0 carries the longest dependent chain (Haralick f14): it gets the
-    // highest priority, so its blocks are dispatched ahead of the other lanes'
+    // highest priority, so its blocks are dispatched ahead of the other lanes'.
+    // Lane 5 (the sorts: integer and shared-memory work, no FP64) gets it too:
+    // at the lowest priority its blocks waited for SM room until the FP64
+    // lanes were done and ended the batch alone.
     int prio_lo = 0, prio_hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
     for (int k = 0; k < WC_LANES; k++) {
-        CK(cudaStreamCreateWithPriority(&E->lanes[k], cudaStreamNonBlocking, k == 0 ? prio_hi : prio_lo));
+        CK(cudaStreamCreateWithPriority(&E->lanes[k], cudaStreamNonBlocking, (k == 0 || k == 5) ? prio_hi : prio_lo));
         CK(cudaEventCreateWithFlags(&E->join_ev[k], cudaEventDisableTiming));
     }
     CK(cudaEventCreateWithFlags(&E->fork_ev, cudaEventDisableTiming));

@@ -419,8 +419,10 @@ int features_prepare(FeatureSetup &fs) {
 int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early) {
     const auto &P = *fs.planes;
     const auto &fj = *fs.fj;
-    // lanes: 0 Haralick; 1 Zernike, Chebyshev-Fourier; 2 Tamura, Chebyshev coefficients;
-    // 3 Gabor; 4 objects, edge features; 5 sorts and the plane scans
+    // lanes: 0 Haralick; 1 Zernike, Chebyshev-Fourier; 2 Tamura;
+    // 3 Gabor, then Radon, fractal, multiscale histograms, comb moments;
+    // 4 objects, edge features; 5 sorts (PixStats, Gini), colour histogram,
+    // Chebyshev coefficients (lanes 0 and 5 at the higher stream priority)
     Ctx &c = fr.lanes[5];
     auto jobs = [&](int a) { return (const FJob *)(fr.meta + fs.off["jobs" + std::to_string(a)]); };
     auto nj = [&](int a) { return (int)fj[a].size(); };
@@ -467,6 +469,31 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early) {
                         fr.feat);
     }
 
+    // the plane scans on lane 3, after Gabor: beside the sorts rather than
+    // behind them (the sorts' integer work waits longest for SM room while the
+    // FP64 lanes run, and the scans would otherwise end the batch alone)
+    {
+        Ctx &c = fr.lanes[3];
+        ProfScope ps(c, "Radon Coefficients");
+        if (nj(A_RADON))
+        launch_radon(c, fr.arena, fr.planes, jobs(A_RADON), nj(A_RADON), maxw_of(P, fj[A_RADON]), maxh_of(P, fj[A_RADON]),
+                     fr.feat);
+    }
+    {
+        Ctx &c = fr.lanes[3];
+        ProfScope ps(c, "Fractal Features");
+        if (nj(A_FRACTAL)) launch_fractal(c, fr.arena, fr.planes, jobs(A_FRACTAL), nj(A_FRACTAL), fr.feat);
+    }
+    {
+        Ctx &c = fr.lanes[3];
+        ProfScope ps(c, "Multiscale Histograms");
+        if (nj(A_MSHIST)) launch_mshist(c, fr.arena, fr.planes, fr.stats, jobs(A_MSHIST), nj(A_MSHIST), fr.feat);
+    }
+    {
+        Ctx &c = fr.lanes[3];
+        ProfScope ps(c, "Comb Moments");
+        if (nj(A_COMB)) launch_comb(c, fr.arena, fr.planes, jobs(A_COMB), nj(A_COMB), fr.feat);
+    }
     if (fs.val.count("sort_n")) {
         ProfScope ps(c, "PixStats+Gini (sort)");
         launch_sort_planes(c, fr.arena, fr.planes, (const int *)(fr.meta + fs.off["sort_ids"]),
@@ -488,25 +515,7 @@ int features_launch(FeatureSetup &fs, FeatureRun &fr, int phase, bool early) {
                                                fr.fuzzy, fr.feat);
     }
     {
-        ProfScope ps(c, "Multiscale Histograms");
-        if (nj(A_MSHIST)) launch_mshist(c, fr.arena, fr.planes, fr.stats, jobs(A_MSHIST), nj(A_MSHIST), fr.feat);
-    }
-    {
-        ProfScope ps(c, "Fractal Features");
-        if (nj(A_FRACTAL)) launch_fractal(c, fr.arena, fr.planes, jobs(A_FRACTAL), nj(A_FRACTAL), fr.feat);
-    }
-    {
-        ProfScope ps(c, "Comb Moments");
-        if (nj(A_COMB)) launch_comb(c, fr.arena, fr.planes, jobs(A_COMB), nj(A_COMB), fr.feat);
-    }
-    {
-        ProfScope ps(c, "Radon Coefficients");
-        if (nj(A_RADON))
-        launch_radon(c, fr.arena, fr.planes, jobs(A_RADON), nj(A_RADON), maxw_of(P, fj[A_RADON]), maxh_of(P, fj[A_RADON]),
-                     fr.feat);
-    }
-    {
-        Ctx &c = fr.lanes[2];
+        Ctx &c = fr.lanes[5];
         ProfScope ps(c, "Chebyshev Coefficients");
         if (nj(A_CHEB))
         launch_chebcoef(c, fr.arena, fr.planes, jobs(A_CHEB), nj(A_CHEB), fr.tabs,

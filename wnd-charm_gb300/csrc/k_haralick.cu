@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q_df(const HarJob *__restr
 // matrix; products that the reference forms per element (tau * ess_r, tau * t)
 // are formed once, with the same value.
 __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj, char *__restrict__ wsb) {
-    __shared__ double v[256], ess[256], tess[256];
+    __shared__ double v[256], vsq[256], ess[256], tess[256];
     __shared__ double s_tau, s_beta, s_den;
     __shared__ int s_triv;
     const int ang = blockIdx.y;
@@ -384,11 +384,15 @@ __global__ void __launch_bounds__(256) k_har_hess(const HarJob *__restrict__ hj,
     double *A = (double *)(wsb + H.q_b) + (long long)ang * 256 * 256;
     for (int i = 0; i < n - 1; i++) {
         const int rem = n - i - 1;
-        for (int k = threadIdx.x; k < rem; k += blockDim.x) v[k] = A[(long long)(i + 1 + k) * n + i];
+        for (int k = threadIdx.x; k < rem; k += blockDim.x) {
+            const double x = A[(long long)(i + 1 + k) * n + i];
+            v[k] = x;
+            vsq[k] = __dmul_rn(x, x);  // the squares side by side; their sum stays sequential
+        }
         __syncthreads();
         if (threadIdx.x == 0) {  // makeHouseholder (Householder.h:65-90)
             double tail = 0;
-            for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, __dmul_rn(v[k], v[k]));
+            for (int k = 1; k < rem; k++) tail = __dadd_rn(tail, vsq[k]);
             const double c0 = v[0];
             if (rem == 1 || tail == 0) {
                 s_triv = 1;
@@ -463,26 +467,37 @@ __device__ __forceinline__ double plus_zero(double x) {
     return b == (long long)0x8000000000000000ULL ? 0.0 : x;
 }
 
+// x == 0 (either sign) and x >= 0 (-0 included, NaN excluded) from the bits:
+// integer instructions instead of FP64 comparisons
+__device__ __forceinline__ bool zero_bits(double x) { return (__double_as_longlong(x) << 1) == 0; }
+__device__ __forceinline__ bool nonneg_bits(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b <= 0x7ff0000000000000LL : b == (long long)0x8000000000000000ULL;
+}
+
 // makeHouseholder of a 3-vector with the scalar work spread over lanes: lanes
 // 1, 2 square v1, v2 at once, and lanes 0, 1, 2 form v1/(c0-beta),
 // v2/(c0-beta) and (beta-c0)/beta in one division.  Same operations and
 // roundings as the sequential form (0 + v1^2 = v1^2 exactly, as v1^2 >= +0).
+// beta - c0 is taken as -(c0 - beta): round-to-nearest is symmetric, and
+// c0 - beta is never zero here (beta has c0's opposite sign and |beta| > 0).
 __device__ __forceinline__ void hh_make3(const double v0, const double v1, const double v2, int lane, double &e0,
                                          double &e1, double &tau, double &beta) {
     const double vl = lane == 2 ? v2 : v1;
     const double sq = __dmul_rn(vl, vl);
     const double s1 = __shfl_sync(0xffffffffu, sq, 1), s2 = __shfl_sync(0xffffffffu, sq, 2);
     const double tail = __dadd_rn(s1, s2);
-    if (tail == 0) {
+    if (zero_bits(tail)) {
         tau = 0;
         beta = v0;
         e0 = e1 = 0;
         return;
     }
     beta = sqrt(__dadd_rn(__dmul_rn(v0, v0), tail));
-    if (v0 >= 0) beta = -beta;
+    if (nonneg_bits(v0)) beta = -beta;
     const double den = __dsub_rn(v0, beta);
-    const double num = lane == 0 ? v1 : (lane == 1 ? v2 : __dsub_rn(beta, v0));
+    const double nden = __longlong_as_double(__double_as_longlong(den) ^ (long long)0x8000000000000000ULL);
+    const double num = lane == 0 ? v1 : (lane == 1 ? v2 : nden);
     const double q = num / (lane < 2 ? den : beta);
     e0 = __shfl_sync(0xffffffffu, q, 0);
     e1 = __shfl_sync(0xffffffffu, q, 1);
@@ -708,12 +723,14 @@ __device__ void har_schur(double *__restrict__ A, const int n, double *__restric
                     if (first) hh_make3(fv0, fv1, fv2, lane, ess[0], ess[1], tau, beta);
                     else hh_make3(T_(k, k - 1), T_(k + 1, k - 1), T_(k + 2, k - 1), lane, ess[0], ess[1], tau, beta);
                     QR_SYNC();
-                    if (beta != 0) {
+                    if (!zero_bits(beta)) {
                         if (tid == 0) {
                             if (first && k > il) T_(k, k - 1) = -T_(k, k - 1);
                             else if (!first) T_(k, k - 1) = beta;
                         }
-                        const double te0 = __dmul_rn(tau, ess[0]), te1 = __dmul_rn(tau, ess[1]);  // per column alike
+                        // tau * ess[0] and tau * ess[1] (alike for every column) in one multiply
+                        const double tm = __dmul_rn(tau, lane == 0 ? ess[0] : ess[1]);
+                        const double te0 = __shfl_sync(0xffffffffu, tm, 0), te1 = __shfl_sync(0xffffffffu, tm, 1);
                         for (int cc = k + tid; cc <= iu; cc += GS) {  // left: rows k..k+2
                             const double a0 = T_(k, cc), a1 = T_(k + 1, cc), a2 = T_(k + 2, cc);
                             double t = plus_zero(__dmul_rn(ess[0], a1));

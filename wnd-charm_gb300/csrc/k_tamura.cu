@@ -244,6 +244,12 @@ __global__ void __launch_bounds__(256) k_tam_pixel(const Plane *__restrict__ pla
     }
 }
 
+// Moments4::add's filter (NaN and |v| > FLT_MAX skipped) on the bit pattern:
+// |v| <= FLT_MAX exactly when |v|'s pattern is at most FLT_MAX's (NaN above)
+__device__ __forceinline__ bool moments_take(double v) {
+    return (__double_as_longlong(v) & 0x7fffffffffffffffLL) <= 0x47efffffe0000000LL;
+}
+
 __global__ void __launch_bounds__(1024) k_tam_final(const Plane *__restrict__ planes, const FJob *__restrict__ jobs,
                                                     const TamJob *__restrict__ tj, const double *__restrict__ ws,
                                                     const double *__restrict__ part, int nchunk_max,
@@ -278,7 +284,7 @@ __global__ void __launch_bounds__(1024) k_tam_final(const Plane *__restrict__ pl
         atomicAdd(&hs[hist_bin((double)sb[i], kmin, ssc, 3)], 1u);
         atomicAdd(&hp[hist_bin(phi[i], pmn, psc, 125)], 1u);
         const double v = nrm[i];
-        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;
+        if (!moments_take(v)) continue;
         s1 += v;
         cnt++;
     }
@@ -289,7 +295,7 @@ __global__ void __launch_bounds__(1024) k_tam_final(const Plane *__restrict__ pl
     double m2 = 0, m4 = 0;
     for (long long i = threadIdx.x; i < n; i += blockDim.x) {
         const double v = nrm[i];
-        if (isnan(v) || v > FLT_MAX || v < -FLT_MAX) continue;
+        if (!moments_take(v)) continue;
         const double d = v - mean, d2 = d * d;
         m2 += d2;
         m4 += d2 * d2;

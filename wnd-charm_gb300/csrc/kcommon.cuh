@@ -118,12 +118,24 @@ __device__ __forceinline__ long long block_sum_ll(long long v, long long *sh) {
 // bin = (unsigned long)((v - lo) * scale), clamped to nbins-1, with
 // scale = nbins / (hi - lo) or 0 when hi == lo.  A NaN lands in the last bin
 // (what the x86-64 conversion of NaN to unsigned long gives before the clamp).
+// The comparisons and the truncation act on t's bit pattern (integer
+// instructions; the FP64 pipe issues only the subtraction and the product):
+// a non-negative double orders as its pattern, and for 1 <= t < 2^31 the
+// integer part is the significand shifted by 52 - exponent.
+__device__ __forceinline__ long long dbits_of_count(int n) {  // the pattern of (double)n, n >= 1
+    const int e = 31 - __clz(n);
+    return ((long long)(1023 + e) << 52) | (((long long)n << (52 - e)) & 0x000fffffffffffffLL);
+}
 __device__ __forceinline__ int hist_bin(double v, double lo, double scale, int nbins) {
-    double t = (v - lo) * scale;
-    if (!(t < (double)nbins)) return nbins - 1;  // also NaN
-    if (t < 0) return 0;
-    unsigned long long b = (unsigned long long)t;
-    return b >= (unsigned long long)nbins ? nbins - 1 : (int)b;
+    const double t = (v - lo) * scale;
+    const long long tb = __double_as_longlong(t);
+    if ((tb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return nbins - 1;  // NaN
+    if (tb < 0) return 0;                                                    // t < 0, or -0
+    if (tb >= dbits_of_count(nbins)) return nbins - 1;                       // t >= nbins, +inf
+    const int ex = (int)(tb >> 52) - 1023;
+    if (ex < 0) return 0;  // 0 <= t < 1
+    const long long b = ((tb & 0x000fffffffffffffLL) | 0x0010000000000000LL) >> (52 - ex);
+    return b >= nbins ? nbins - 1 : (int)b;
 }
 __host__ __device__ __forceinline__ double hist_scale(double lo, double hi, int nbins) {
     return (hi - lo > 0) ? (double)nbins / double(hi - lo) : 0.0;

@@ -144,10 +144,11 @@ def stage_work(name, B, precision="mixed", f14="exact"):
         # direction quotient and atan, about 45 FP64 operations per pixel
         "Tamura Textures": ("fp64", B * planes_c * px * 45),
         "Gabor Textures": ("bytes", B * px * 8 * 2),
-        # three 2-D Chebyshev transforms per image (of the image, of its Fourier
-        # and of its wavelet plane), each two 512^3 products; a multiply and an
-        # add per term (FP64 and unfused in both forms: the reference's rounding)
-        "Chebyshev": ("fp64", B * 3 * 2 * 2 * IMG ** 3),
+        # three 2-D Chebyshev transforms per image (of the image and of its
+        # Fourier plane, 512 x 512, and of its wavelet plane, 520 x 520), each
+        # two n^3 products; a multiply and an add per term (FP64 and unfused in
+        # both forms: the reference's rounding)
+        "Chebyshev": ("fp64", B * 2 * 2 * (2 * IMG ** 3 + (2 * ((IMG + 9) // 2)) ** 3)),
         "Comb Moments": ("bytes", B * planes_c * px * 8),
         "Radon Coefficients": ("bytes", B * planes_c * px * 8),
         "Fractal Features": ("bytes", B * planes_c * px * 8),

@@ -252,8 +252,10 @@ __device__ void hh_make(const double *v, int n, double *ess, double &tau, double
 // quotient.  Here d = px py + 1e-13 lies in [1e-13, 1]; far from the normal
 // range (rp < 2^-900) the division itself is used.
 static __device__ __noinline__ double q_div_far(double a, double b) { return a / b; }
+// rp >= +0 (a product of GLCM entries), so rp < 2^-900 compares as bit patterns
+// (integer instructions; a NaN takes the division as well)
 __device__ __forceinline__ double q_quot(double rp, double d, double yh, double yl) {
-    if (rp < 0x1p-900) return q_div_far(rp, d);
+    if (__double_as_longlong(rp) < 0x07b0000000000000LL) return q_div_far(rp, d);
     const double q0 = fma(rp, yh, __dmul_rn(rp, yl));
     const double r = fma(-q0, d, rp);
     return fma(r, yh, q0);
@@ -298,7 +300,7 @@ __global__ void __launch_bounds__(32 * Q_WARPS) k_har_q(const HarJob *__restrict
                 const double *Pk = P + (long long)k * n;
                 for (int j = lo[k] + lane; j <= hi[k]; j += 32) {
                     const double rp = __dmul_rn(a, Pk[j]);
-                    if (rp != 0.0) q[j] = __dadd_rn(q[j], q_quot(rp, d, yh, yl));
+                    if ((__double_as_longlong(rp) << 1) != 0) q[j] = __dadd_rn(q[j], q_quot(rp, d, yh, yl));
                 }
                 __syncwarp();
             }

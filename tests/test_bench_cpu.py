@@ -36,8 +36,9 @@ def test_reference_arm_other_ranks_exit_quietly():
 
 def test_stage_work_model():
     B = 128
-    # the Chebyshev transforms: 3 per image, two 512^3 products each, a multiply and an add per term
-    assert bench.stage_work("Chebyshev", B) == ("fp64", B * 3 * 2 * 2 * 512 ** 3)
+    # the Chebyshev transforms: 3 per image (the image and its Fourier plane at 512^2,
+    # its wavelet plane at 520^2), two n^3 products each, a multiply and an add per term
+    assert bench.stage_work("Chebyshev", B) == ("fp64", B * 2 * 2 * (2 * 512 ** 3 + 520 ** 3))
     assert bench.stage_work("Chebyshev", B, "fp64") == bench.stage_work("Chebyshev", B, "mixed")
     # f14 is FP64 work unless the mixed form runs its pairs-of-floats chain; Zernike only in the FP64 form
     assert bench.stage_work("Haralick Textures", B, "mixed", "pairs") is None

@@ -506,7 +506,7 @@ __device__ __forceinline__ void hh_make3(const double v0, const double v1, const
     tau = __shfl_sync(0xffffffffu, q, 2);
 }
 
-#define QR_BIG 96  // matrices with at least this many tones get a 4-warp group in k_har_qr
+#define QR_BIG 96  // matrices with at least this many tones get a 4-warp group in k_har_qr_queue
 
 // Matrices in descending Ng (counting sort; the order only schedules, every
 // matrix is computed alone), so the longest QR runs start first.

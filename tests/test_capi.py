@@ -63,3 +63,40 @@ def test_engine_without_gpu_fails_cleanly(capi):
         pytest.skip("a GPU is present")
     with pytest.raises(capi.WndcharmError):
         capi.Engine(0, "fp64")
+
+
+def test_output_buffers_are_checked(capi):
+    """A caller's `out` array must hold exactly the rows the library writes
+    (float64, C-contiguous, writable); anything else is refused before a call."""
+    import numpy as np
+    ob = capi._out_buffer
+    assert ob(None, 3, 5).shape == (3, 5)
+    good = np.zeros((3, 5))
+    assert ob(good, 3, 5) is good
+    ro = np.zeros((3, 5))
+    ro.flags.writeable = False
+    for bad in (np.zeros((3, 4)), np.zeros((5, 3)), np.zeros((3, 5), np.float32), np.zeros((5, 3)).T,
+                np.zeros((3, 10))[:, ::2], ro, [[0.0] * 5] * 3):
+        with pytest.raises(capi.WndcharmError):
+            ob(bad, 3, 5)
+
+
+def test_wnd_arguments_are_checked(capi):
+    """WND-5 wrappers hand the library pointers it reads N x F, N, T x F and F
+    values through: mismatched shapes are refused on the host, arrays that
+    already have the layout pass through without a copy."""
+    import numpy as np
+    X = np.zeros((6, 4))
+    y = np.arange(6, dtype=np.int32)
+    T = np.zeros((3, 4))
+    X2, y2, T2 = capi._wnd_rows(X, y, T)
+    assert X2 is X and y2 is y and T2 is T
+    assert capi._wnd_rows(X, list(range(6)))[1].dtype == np.int32
+    assert capi._wnd_rows(X, y, np.zeros(4))[2].shape == (1, 4)  # one test row
+    for args in ((X, y[:5]), (X, y.reshape(6, 1)), (np.zeros(6), y), (X, y, np.zeros((3, 5)))):
+        with pytest.raises(capi.WndcharmError):
+            capi._wnd_rows(*args)
+    w = np.ones(4)
+    assert capi._wnd_vecs(4, w, [0, 0, 0, 0])[0] is w
+    with pytest.raises(capi.WndcharmError):
+        capi._wnd_vecs(4, w, np.ones(3))

@@ -262,6 +262,46 @@ def _dtype_code(a):
     return _RGB[a.dtype] if a.ndim == 3 else _DT[a.dtype]
 
 
+def _out_buffer(out, rows, cols):
+    """The caller's output array, checked (a writable, C-contiguous float64
+    array of shape (rows, cols): the library writes rows * cols doubles
+    there), or a new zeroed one."""
+    if out is None:
+        return np.zeros((rows, cols))
+    if (not isinstance(out, np.ndarray) or out.dtype != np.float64 or not out.flags.c_contiguous
+            or not out.flags.writeable or out.shape != (rows, cols)):
+        raise WndcharmError("out must be a writable C-contiguous float64 array of shape (%d, %d)" % (rows, cols))
+    return out
+
+
+def _wnd_rows(train, labels, test=None):
+    """Training rows (N, F) float64, their N labels (int32) and test rows
+    (T, F) float64 (a single row may be 1-D), checked against each other: the
+    library reads N x F, N and T x F values through these pointers.  Arrays
+    that already have the layout are passed on as they are (no copy)."""
+    X = np.ascontiguousarray(train, dtype=np.float64)
+    y = np.ascontiguousarray(labels, dtype=np.int32)
+    if X.ndim != 2 or y.shape != (X.shape[0],):
+        raise WndcharmError("training rows must be an (N, F) array with N labels")
+    if test is None:
+        return X, y
+    T = np.ascontiguousarray(np.atleast_2d(test), dtype=np.float64)
+    if T.ndim != 2 or T.shape[1] != X.shape[1]:
+        raise WndcharmError("test rows must have the training rows' %d features" % X.shape[1])
+    return X, y, T
+
+
+def _wnd_vecs(F, *vecs):
+    """Per-feature vectors (weights, mins, maxs, means), F float64 values each."""
+    out = []
+    for v in vecs:
+        a = np.ascontiguousarray(v, dtype=np.float64)
+        if a.shape != (F,):
+            raise WndcharmError("per-feature vectors must hold %d values" % F)
+        out.append(a)
+    return out
+
+
 class Engine(object):
     """One GPU with its device memory pools.  precision: 'fp64' or 'mixed'."""
 
@@ -325,7 +365,9 @@ class Engine(object):
         through the FP64 chain, 1 by default), 'qr_iter_per_tone' (real-Schur
         iterations allowed per tone, 40), 'union_find_cap' (labelling
         iterations allowed per link, 0 = the pixel count), 'autotune' (1),
-        'graph' (0; 1: repeated batch shapes replay a captured CUDA graph)."""
+        'graph' (0; 1: repeated batch shapes replay a captured CUDA graph),
+        'cf_tensor_cores' (1: the mixed form's Chebyshev-Fourier sums on the
+        tensor cores where a batch's planes share one size)."""
         check(lib().wc_engine_set_option(self._h, name.encode(), int(value)))
 
     def extract(self, plan, images, bits=16, out=None):
@@ -335,8 +377,7 @@ class Engine(object):
         descs = (_lib.wc_image_desc * n)()
         for i, a in enumerate(imgs):
             descs[i] = _lib.wc_image_desc(a.ctypes.data, _dtype_code(a), a.shape[1], a.shape[0], bits, 0)
-        if out is None:
-            out = np.zeros((n, plan.n_features))
+        out = _out_buffer(out, n, plan.n_features)
         check(lib().wc_extract_batch(self._h, plan.handle, descs, n, out.ctypes.data, 0))
         return out
 
@@ -365,8 +406,7 @@ class Engine(object):
             descs[i] = _lib.wc_image_desc(a.ctypes.data, _dtype_code(a), a.shape[1], a.shape[0], bits, 0)
         st = sampling.struct()
         per = check(lib().wc_sampling_count(ctypes.byref(st)))
-        if out is None:
-            out = np.zeros((n * per, plan.n_features))
+        out = _out_buffer(out, n * per, plan.n_features)
         check(lib().wc_extract_samples(self._h, plan.handle, descs, n, ctypes.byref(st), out.ctypes.data, 0))
         return out
 
@@ -417,8 +457,7 @@ class Engine(object):
         return out[: ow.value * oh.value].reshape(oh.value, ow.value).copy()
 
     def wnd_fit(self, train, labels, n_classes, frac=0.15):
-        X = np.ascontiguousarray(train, dtype=np.float64)
-        y = np.ascontiguousarray(labels, dtype=np.int32)
+        X, y = _wnd_rows(train, labels)
         N, F = X.shape
         w, mn, mx = np.zeros(F), np.zeros(F), np.zeros(F)
         check(lib().wc_wnd_fit(self._h, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I), int(n_classes),
@@ -427,12 +466,10 @@ class Engine(object):
         return w, mn, mx
 
     def wnd_classify(self, train, labels, n_classes, weights, mins, maxs, test):
-        X = np.ascontiguousarray(train, dtype=np.float64)
-        y = np.ascontiguousarray(labels, dtype=np.int32)
-        T = np.ascontiguousarray(test, dtype=np.float64)
+        X, y, T = _wnd_rows(train, labels, test)
         N, F = X.shape
         nt = T.shape[0]
-        w, mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (weights, mins, maxs))
+        w, mn, mx = _wnd_vecs(F, weights, mins, maxs)
         probs = np.zeros((nt, n_classes))
         pred = np.zeros(nt, dtype=np.int32)
         check(lib().wc_wnd_classify(self._h, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I), int(n_classes),
@@ -443,9 +480,11 @@ class Engine(object):
 
     def wnd_normalize(self, rows, mins, maxs):
         """signatures::normalize of each row against (mins, maxs): values in [0, 100]."""
-        X = np.ascontiguousarray(rows, dtype=np.float64)
+        X = np.ascontiguousarray(np.atleast_2d(rows), dtype=np.float64)
+        if X.ndim != 2:
+            raise WndcharmError("rows must be an (n, F) array")
         n, F = X.shape
-        mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (mins, maxs))
+        mn, mx = _wnd_vecs(F, mins, maxs)
         out = np.zeros_like(X)
         check(lib().wc_wnd_normalize(self._h, X.ctypes.data_as(_lib.D), n, F, mn.ctypes.data_as(_lib.D),
                                      mx.ctypes.data_as(_lib.D), out.ctypes.data_as(_lib.D)))
@@ -455,13 +494,15 @@ class Engine(object):
         """wc_wnd_fit_stats on these training rows (a shard): stage 0 ->
         (mins, maxs, counts (C+1)); stage 1 -> per-label sums ((C+1), F);
         stage 2 -> per-label sums of squared deviations ((C+1), F)."""
-        X = np.ascontiguousarray(train, dtype=np.float64)
-        y = np.ascontiguousarray(labels, dtype=np.int32)
+        X, y = _wnd_rows(train, labels)
         N, F = X.shape
         C = int(n_classes)
         LL = ctypes.POINTER(ctypes.c_longlong)
-        arg = lambda v: None if v is None else np.ascontiguousarray(v, dtype=np.float64)  # noqa: E731
-        mn, mx, me = arg(mins), arg(maxs), arg(means)
+        arg = lambda v: None if v is None else _wnd_vecs(F, v)[0]  # noqa: E731
+        mn, mx = arg(mins), arg(maxs)
+        me = None if means is None else np.ascontiguousarray(means, dtype=np.float64)
+        if me is not None and me.shape != (C + 1, F):
+            raise WndcharmError("means must be a (%d, %d) array" % (C + 1, F))
         ptr = lambda v: None if v is None else v.ctypes.data_as(_lib.D)  # noqa: E731
         if stage == 0:
             out = np.zeros(2 * F)
@@ -480,6 +521,9 @@ class Engine(object):
         sums = np.ascontiguousarray(sums, dtype=np.float64)
         sq = np.ascontiguousarray(sq, dtype=np.float64)
         counts = np.ascontiguousarray(counts, dtype=np.int64)
+        C1 = int(n_classes) + 1
+        if sums.ndim != 2 or sums.shape[0] != C1 or sq.shape != sums.shape or counts.shape != (C1,):
+            raise WndcharmError("sums and sq must be (%d, F) arrays and counts %d values" % (C1, C1))
         F = sums.shape[1]
         w = np.zeros(F)
         check(lib().wc_wnd_fisher(self._h, F, int(n_classes), float(frac), sums.ctypes.data_as(_lib.D),
@@ -490,12 +534,10 @@ class Engine(object):
     def wnd_class_sums(self, train, labels, n_classes, weights, mins, maxs, test):
         """classify2's per-class sums of d^-5 and counts over these training
         rows (a shard): (sums (T, C) float64, counts (T, C) int64)."""
-        X = np.ascontiguousarray(train, dtype=np.float64)
-        y = np.ascontiguousarray(labels, dtype=np.int32)
-        T = np.ascontiguousarray(test, dtype=np.float64)
+        X, y, T = _wnd_rows(train, labels, test)
         N, F = X.shape
         nt = T.shape[0]
-        w, mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (weights, mins, maxs))
+        w, mn, mx = _wnd_vecs(F, weights, mins, maxs)
         sums = np.zeros((nt, n_classes))
         counts = np.zeros((nt, n_classes), dtype=np.int64)
         check(lib().wc_wnd_class_sums(self._h, X.ctypes.data_as(_lib.D), N, F, y.ctypes.data_as(_lib.I),
@@ -508,9 +550,7 @@ class Engine(object):
     def wnd_fit_classify(self, train, labels, n_classes, test, frac=0.15):
         """wnd_fit on the training rows, then wnd_classify of the test rows,
         each array copied to the GPU once: (probs, pred, weights, mins, maxs)."""
-        X = np.ascontiguousarray(train, dtype=np.float64)
-        y = np.ascontiguousarray(labels, dtype=np.int32)
-        T = np.ascontiguousarray(test, dtype=np.float64)
+        X, y, T = _wnd_rows(train, labels, test)
         N, F = X.shape
         nt = T.shape[0]
         w, mn, mx = np.zeros(F), np.zeros(F), np.zeros(F)
@@ -554,14 +594,12 @@ class Engine(object):
         """TrainingSet::ClassifyImage with WND-5 for images of `tiles`
         consecutive test rows: (probs (n_images, C), pred (n_images,),
         normalisation factors (n_images,))."""
-        X = np.ascontiguousarray(train, dtype=np.float64)
-        y = np.ascontiguousarray(labels, dtype=np.int32)
-        T = np.ascontiguousarray(test, dtype=np.float64)
+        X, y, T = _wnd_rows(train, labels, test)
         N, F = X.shape
         if T.shape[0] % tiles:
             raise WndcharmError("%d test rows are not whole images of %d tiles" % (T.shape[0], tiles))
         n_img = T.shape[0] // tiles
-        w, mn, mx = (np.ascontiguousarray(v, dtype=np.float64) for v in (weights, mins, maxs))
+        w, mn, mx = _wnd_vecs(F, weights, mins, maxs)
         probs = np.zeros((n_img, n_classes))
         pred = np.zeros(n_img, dtype=np.int32)
         norm = np.zeros(n_img)
